@@ -1,0 +1,130 @@
+// Small-K matrix products C[b] (=|+=) A @ B[b] of the sweep and of the image.
+//
+// The contractions of the scattering source (Y [D x N_sh] @ T [N_sh x J]), of the moment accumulation
+// (Yw^T [N_sh x D] @ psi [D x J]) and of the multiple-collision source all have a short inner dimension
+// (N_sh <= 64, D <= 240) and a very long column dimension J (cells x groups x 4), so they are streaming products: each
+// block keeps A in shared memory, streams a 128-column slab of B through shared memory in 32-row chunks, and holds
+// an (8 R) x 128 tile of C in registers, R rows and one float4 of columns per thread. B and C move once through HBM.
+#include "common.cuh"
+
+namespace citrus {
+namespace {
+
+constexpr int kThreads = 256;  // 8 warps; warp w owns rows w, w + 8, ... of the block's row tile
+constexpr int kCols = 128;     // columns per block: 32 lanes x float4
+constexpr int kChunk = 32;     // rows of B per shared-memory chunk
+
+template <int R>
+__global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __restrict__ A, int64_t lda,
+                                                                const float* __restrict__ B, int64_t ldb,
+                                                                float* __restrict__ C, int64_t ldc, int M, int K,
+                                                                int64_t J, int64_t stride_b, int64_t stride_c,
+                                                                int accumulate) {
+  extern __shared__ float smem[];
+  float* As = smem;                       // [8R][K] rows of this block's row tile
+  float* Bs = smem + (size_t)8 * R * K;   // [kChunk][kCols]
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int64_t col0 = (int64_t)blockIdx.x * kCols;
+  const int row0 = blockIdx.y * 8 * R;
+  const int64_t batch = blockIdx.z;
+  B += batch * stride_b;
+  C += batch * stride_c;
+  for (int i = threadIdx.x; i < 8 * R * K; i += kThreads) {
+    const int r = i / K, k = i % K;
+    As[i] = (row0 + r < M) ? A[(int64_t)(row0 + r) * lda + k] : 0.f;
+  }
+  float4 acc[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int64_t col = col0 + 4 * lane;
+  for (int k0 = 0; k0 < K; k0 += kChunk) {
+    const int kc = min(kChunk, K - k0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kc * (kCols / 4); i += kThreads) {
+      const int r = i / (kCols / 4), c4 = i % (kCols / 4);
+      const int64_t gc = col0 + 4 * c4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gc < J) v = *reinterpret_cast<const float4*>(B + (int64_t)(k0 + r) * ldb + gc);
+      *reinterpret_cast<float4*>(Bs + r * kCols + 4 * c4) = v;
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kc; ++kk) {
+      const float4 b = *reinterpret_cast<const float4*>(Bs + kk * kCols + 4 * lane);
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const float a = As[(warp + 8 * i) * K + k0 + kk];
+        acc[i].x = fmaf(a, b.x, acc[i].x);
+        acc[i].y = fmaf(a, b.y, acc[i].y);
+        acc[i].z = fmaf(a, b.z, acc[i].z);
+        acc[i].w = fmaf(a, b.w, acc[i].w);
+      }
+    }
+  }
+  if (col >= J) return;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int row = row0 + warp + 8 * i;
+    if (row >= M) break;
+    float4* out = reinterpret_cast<float4*>(C + (int64_t)row * ldc + col);
+    float4 v = acc[i];
+    if (accumulate) {
+      const float4 o = *out;
+      v.x += o.x;
+      v.y += o.y;
+      v.z += o.z;
+      v.w += o.w;
+    }
+    *out = v;
+  }
+}
+
+template <int R>
+int launch(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K, int64_t J,
+           int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t stream) {
+  const size_t smem = ((size_t)8 * R * K + (size_t)kChunk * kCols) * sizeof(float);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(small_k_gemm_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
+  }
+  dim3 grid((unsigned)cdiv(J, kCols), (unsigned)cdiv(M, 8 * R), (unsigned)batch);
+  small_k_gemm_kernel<R><<<grid, kThreads, smem, stream>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b, stride_c,
+                                                           accumulate);
+  return launch_status("citrus_small_k_gemm");
+}
+
+}  // namespace
+}  // namespace citrus
+
+using namespace citrus;
+
+extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                                   int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
+                                   int32_t accumulate, void* stream) {
+  CITRUS_REQUIRE(A && B && C, "citrus_small_k_gemm: null pointer argument");
+  CITRUS_REQUIRE(M >= 1 && K >= 1 && J >= 0 && batch >= 1 && batch <= 65535,
+                 "citrus_small_k_gemm: bad sizes M %lld K %lld J %lld batch %lld", (long long)M, (long long)K,
+                 (long long)J, (long long)batch);
+  CITRUS_REQUIRE(K <= 1024 && M <= (1 << 20), "citrus_small_k_gemm: K %lld or M %lld too large", (long long)K,
+                 (long long)M);
+  CITRUS_REQUIRE(J % 4 == 0 && ldb % 4 == 0 && ldc % 4 == 0 && stride_b % 4 == 0 && stride_c % 4 == 0,
+                 "citrus_small_k_gemm: J, ldb, ldc and the batch strides must be multiples of 4");
+  CITRUS_REQUIRE(((uintptr_t)B % 16) == 0 && ((uintptr_t)C % 16) == 0, "citrus_small_k_gemm: B and C must be "
+                 "16-byte aligned");
+  CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "citrus_small_k_gemm: leading dimensions too small");
+  if (J == 0) return CITRUS_OK;
+  const int m = (int)M, k = (int)K;
+  const int rows = (m + 7) / 8;
+  cudaStream_t s = as_stream(stream);
+  if (8ll * 16 * K * 4 + kChunk * kCols * 4 > 200 * 1024)
+    return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: K %lld too large for the shared-memory tile", (long long)K);
+  if (rows <= 1) return launch<1>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 2) return launch<2>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 3) return launch<3>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 4) return launch<4>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 5) return launch<5>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 6) return launch<6>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 8) return launch<8>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  if (rows <= 12) return launch<12>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  return launch<16>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+}

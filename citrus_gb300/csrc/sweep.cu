@@ -1,0 +1,214 @@
+// Linear-discontinuous discrete-ordinates sweep: the closed-form cell solve of every (entry, direction, group) of a
+// diagonal wavefront plane, in place in the chunk's cell-major store [views, 8, Dc, N, 4G].
+//
+// The cell equations are those of citrus/scatter_solver/linear_discontinuous_cell.py:14-87 (right-hand sides from the
+// source and the three upstream neighbours, then the closed-form 4 x 4 solve), evaluated term by term in float32 with
+// IEEE division. Two drivers share the lane body: one launch per plane (the reference's plan,
+// sweep_kernels.py:265-290) and one persistent cooperative launch that walks all planes with a bounded grid barrier
+// between them, so a whole chunk is a single launch.
+#include "common.cuh"
+
+namespace citrus {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <bool kCoherent>
+__device__ __forceinline__ float4 load4(const float* p) {
+  if (kCoherent) return __ldcg(reinterpret_cast<const float4*>(p));  // L2 only: written by other SMs this launch
+  return *reinterpret_cast<const float4*>(p);
+}
+
+// One lane: entry e of the plane, direction d of the chunk, group g, view v. Upstream neighbours lie on the previous
+// plane (already swept); an upstream index N is a vacuum face and reads zeros.
+template <int kG, bool kCoherent>
+__device__ __forceinline__ void solve_lane(int64_t lane, float* __restrict__ store, const float* __restrict__ mu,
+                                           const float* __restrict__ c, const int* __restrict__ octant,
+                                           const int* __restrict__ cell, const int* __restrict__ upstream,
+                                           int64_t start, int64_t E, int64_t N, int G_runtime, int64_t Dc,
+                                           int64_t view_stride) {
+  const int G = kG > 0 ? kG : G_runtime;
+  const int g = (int)(lane % G);
+  int64_t t = lane / G;
+  const int64_t d = t % Dc;
+  t /= Dc;
+  const int64_t e = start + t % E;
+  const int64_t v = t / E;
+  const int o = __ldg(octant + e);
+  const int64_t n = __ldg(cell + e);
+  const int64_t ux = __ldg(upstream + 3 * e), uy = __ldg(upstream + 3 * e + 1), uz = __ldg(upstream + 3 * e + 2);
+  const int64_t od = (int64_t)o * Dc + d;
+  const float cx = __ldg(c + 3 * od), cy = __ldg(c + 3 * od + 1), cz = __ldg(c + 3 * od + 2);
+  const float sx = (o & 4) ? -1.f : 1.f, sy = (o & 2) ? -1.f : 1.f, sz = (o & 1) ? -1.f : 1.f;
+  const float m = __ldg(mu + n * G + g);
+  const int64_t Q = 4 * (int64_t)G;
+  float* base = store + v * view_stride + od * N * Q + 4 * g;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 s = load4<kCoherent>(base + n * Q);
+  const float4 X = ux < N ? load4<kCoherent>(base + ux * Q) : zero;  // (psi0, psi_x, psi_y, psi_z) of the x neighbour
+  const float4 Y = uy < N ? load4<kCoherent>(base + uy * Q) : zero;
+  const float4 Z = uz < N ? load4<kCoherent>(base + uz * Q) : zero;
+  // face-averaged inflow psibar_a = psi_0[N_a] + s_a psi_a[N_a]
+  const float pbx = X.x + sx * X.y;
+  const float pby = Y.x + sy * Y.z;
+  const float pbz = Z.x + sz * Z.w;
+  const float r0 = s.x + (cx * pbx + cy * pby + cz * pbz);
+  // R_a = S_a - 3 s_a c_a psibar_a + sum_{b != a} c_b psi_a[N_b]
+  const float rx = s.y - 3.f * sx * cx * pbx + (cy * Y.y + cz * Z.y);
+  const float ry = s.z - 3.f * sy * cy * pby + (cx * X.z + cz * Z.z);
+  const float rz = s.w - 3.f * sz * cz * pbz + (cx * X.w + cy * Y.w);
+  const float csum = cx + cy + cz;
+  const float dx = 3.f * cx + (csum - cx) + m;
+  const float dy = 3.f * cy + (csum - cy) + m;
+  const float dz = 3.f * cz + (csum - cz) + m;
+  const float qx = cx / dx, qy = cy / dy, qz = cz / dz;
+  const float denom = csum + m + 3.f * (cx * qx + cy * qy + cz * qz);
+  const float p0 = (r0 - (sx * qx * rx + sy * qy * ry + sz * qz * rz)) / denom;
+  float4 out;
+  out.x = p0;
+  out.y = (rx + 3.f * sx * cx * p0) / dx;
+  out.z = (ry + 3.f * sy * cy * p0) / dy;
+  out.w = (rz + 3.f * sz * cz * p0) / dz;
+  *reinterpret_cast<float4*>(base + n * Q) = out;
+}
+
+template <int kG>
+__global__ void __launch_bounds__(kThreads) plane_kernel(float* __restrict__ store, const float* __restrict__ mu,
+                                                         const float* __restrict__ c, const int* __restrict__ octant,
+                                                         const int* __restrict__ cell, const int* __restrict__ upstream,
+                                                         int64_t start, int64_t E, int64_t N, int G, int64_t Dc,
+                                                         int64_t views, int64_t view_stride) {
+  const int64_t lane = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int64_t total = views * E * Dc * (kG > 0 ? kG : G);
+  if (lane >= total) return;
+  solve_lane<kG, false>(lane, store, mu, c, octant, cell, upstream, start, E, N, G, Dc, view_stride);
+}
+
+template <int kG>
+__global__ void __launch_bounds__(kThreads) persistent_kernel(
+    float* __restrict__ store, const float* __restrict__ mu, const float* __restrict__ c,
+    const int* __restrict__ octant, const int* __restrict__ cell, const int* __restrict__ upstream,
+    const int* __restrict__ offsets, int num_planes, int64_t N, int G, int64_t Dc, int64_t views,
+    int64_t view_stride, unsigned* sync, uint64_t timeout_ns, int skip) {
+  const int64_t stride = (int64_t)gridDim.x * kThreads;
+  const int64_t per_entry = Dc * (kG > 0 ? kG : G) * views;
+  for (int p = 0; p < num_planes; ++p) {
+    const int64_t start = __ldg(offsets + p);
+    const int64_t E = __ldg(offsets + p + 1) - start;
+    const int64_t total = E * per_entry;
+    for (int64_t lane = (int64_t)blockIdx.x * kThreads + threadIdx.x; lane < total; lane += stride)
+      solve_lane<kG, true>(lane, store, mu, c, octant, cell, upstream, start, E, N, G, Dc, view_stride);
+    if (p + 1 < num_planes && !grid_barrier(sync, gridDim.x, timeout_ns, skip)) return;
+  }
+}
+
+template <int kG>
+int launch_planes(float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                  const int* upstream, const int64_t* offsets, int64_t num_planes, int64_t N, int G, int64_t Dc,
+                  int64_t views, cudaStream_t stream) {
+  const int64_t view_stride = 8 * Dc * N * 4 * (int64_t)G;
+  for (int64_t p = 0; p < num_planes; ++p) {
+    const int64_t start = offsets[p], E = offsets[p + 1] - offsets[p];
+    const int64_t total = views * E * Dc * G;
+    if (total <= 0) continue;
+    plane_kernel<kG><<<(unsigned)cdiv(total, kThreads), kThreads, 0, stream>>>(
+        store, mu, c, octant, cell, upstream, start, E, N, G, Dc, views, view_stride);
+  }
+  return launch_status("citrus_sweep_planes");
+}
+
+template <int kG>
+int launch_persistent(float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                      const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
+                      int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
+                      cudaStream_t stream) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG>, kThreads, 0);
+  if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: occupancy query failed");
+  int64_t blocks = (int64_t)per_sm * num_sms();
+  if (max_blocks > 0 && max_blocks < blocks) blocks = max_blocks;
+  if (skip >= blocks) skip = (int)blocks - 1;
+  int64_t view_stride = 8 * Dc * N * 4 * (int64_t)G;
+  cudaError_t z = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned), stream);
+  if (z != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: %s", cudaGetErrorString(z));
+  void* args[] = {&store, &mu, &c, &octant, &cell, &upstream, &offsets, &num_planes, &N, &G, &Dc, &views,
+                  &view_stride, &sync, &timeout_ns, &skip};
+  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG>, dim3((unsigned)blocks), dim3(kThreads), args, 0,
+                                  stream);
+  if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_persistent: %s", cudaGetErrorString(e));
+  return CITRUS_OK;
+}
+
+int check_sweep_args(const float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                     const int* upstream, int64_t num_planes, int64_t N, int64_t G, int64_t Dc, int64_t views) {
+  CITRUS_REQUIRE(store && mu && c && octant && cell && upstream, "sweep: null pointer argument");
+  CITRUS_REQUIRE(num_planes >= 1 && N >= 1 && G >= 1 && Dc >= 1 && views >= 1,
+                 "sweep: sizes must be positive (planes %lld, cells %lld, groups %lld, dc %lld, views %lld)",
+                 (long long)num_planes, (long long)N, (long long)G, (long long)Dc, (long long)views);
+  CITRUS_REQUIRE(N < (1ll << 31) / 8, "sweep: %lld cells exceed the int32 entry tables", (long long)N);
+  CITRUS_REQUIRE(G <= 4096, "sweep: too many groups (%lld)", (long long)G);
+  CITRUS_REQUIRE(((uintptr_t)store % 16) == 0, "sweep: store must be 16-byte aligned");
+  return CITRUS_OK;
+}
+
+}  // namespace
+}  // namespace citrus
+
+using namespace citrus;
+
+extern "C" int citrus_sweep_planes(float* store, const float* mu_cells, const float* c, const int32_t* octant,
+                                   const int32_t* cell, const int32_t* upstream, const int64_t* plane_offsets_host,
+                                   int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
+                                   int64_t views, void* stream) {
+  int status = check_sweep_args(store, mu_cells, c, octant, cell, upstream, num_planes, num_cells, num_groups, dc,
+                                views);
+  if (status) return status;
+  CITRUS_REQUIRE(plane_offsets_host != nullptr, "citrus_sweep_planes: null plane offsets");
+  const int G = (int)num_groups;
+  cudaStream_t s = as_stream(stream);
+  switch (G) {
+    case 1: return launch_planes<1>(store, mu_cells, c, octant, cell, upstream, plane_offsets_host, num_planes,
+                                    num_cells, G, dc, views, s);
+    case 2: return launch_planes<2>(store, mu_cells, c, octant, cell, upstream, plane_offsets_host, num_planes,
+                                    num_cells, G, dc, views, s);
+    case 4: return launch_planes<4>(store, mu_cells, c, octant, cell, upstream, plane_offsets_host, num_planes,
+                                    num_cells, G, dc, views, s);
+    case 8: return launch_planes<8>(store, mu_cells, c, octant, cell, upstream, plane_offsets_host, num_planes,
+                                    num_cells, G, dc, views, s);
+    case 16: return launch_planes<16>(store, mu_cells, c, octant, cell, upstream, plane_offsets_host, num_planes,
+                                      num_cells, G, dc, views, s);
+    default: return launch_planes<0>(store, mu_cells, c, octant, cell, upstream, plane_offsets_host, num_planes,
+                                     num_cells, G, dc, views, s);
+  }
+}
+
+extern "C" int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c, const int32_t* octant,
+                                       const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_dev,
+                                       int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
+                                       int64_t views, uint32_t* sync, int64_t max_blocks, int64_t timeout_ns,
+                                       int64_t skip_block, void* stream) {
+  int status = check_sweep_args(store, mu_cells, c, octant, cell, upstream, num_planes, num_cells, num_groups, dc,
+                                views);
+  if (status) return status;
+  CITRUS_REQUIRE(plane_offsets_dev != nullptr && sync != nullptr, "citrus_sweep_persistent: null offsets or sync");
+  CITRUS_REQUIRE(num_planes < (1ll << 30), "citrus_sweep_persistent: too many planes");
+  CITRUS_REQUIRE(timeout_ns > 0, "citrus_sweep_persistent: timeout_ns must be positive");
+  const int G = (int)num_groups, P = (int)num_planes, skip = skip_block < 0 ? -1 : (int)skip_block;
+  const uint64_t t = (uint64_t)timeout_ns;
+  unsigned* sy = reinterpret_cast<unsigned*>(sync);
+  cudaStream_t s = as_stream(stream);
+  switch (G) {
+    case 1: return launch_persistent<1>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
+                                        G, dc, views, sy, max_blocks, t, skip, s);
+    case 2: return launch_persistent<2>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
+                                        G, dc, views, sy, max_blocks, t, skip, s);
+    case 4: return launch_persistent<4>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
+                                        G, dc, views, sy, max_blocks, t, skip, s);
+    case 8: return launch_persistent<8>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
+                                        G, dc, views, sy, max_blocks, t, skip, s);
+    case 16: return launch_persistent<16>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P,
+                                          num_cells, G, dc, views, sy, max_blocks, t, skip, s);
+    default: return launch_persistent<0>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
+                                         G, dc, views, sy, max_blocks, t, skip, s);
+  }
+}

@@ -1,0 +1,232 @@
+"""Python face of the sm_103a kernels, with the names, arguments and errors of the reference's kernel modules.
+
+Each function validates its tensors on the host (float32, CUDA, contiguous where required, matching shapes; a
+``ValueError`` otherwise, as in ``citrus/scatter_solver/kernels/*.py``) and then calls one C-ABI entry point of
+``libcitrus_gb300.so`` on the current stream. There is no other implementation behind them: on a machine without the
+library or without CUDA the calls raise.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import Optional
+
+import torch
+from torch import Tensor
+
+from . import _lib
+
+LAYOUTS = ("contiguous", "moment_major", "cell_major")
+DEFAULT_BARRIER_TIMEOUT_NS = 2_000_000_000
+
+
+def kernels_usable(device) -> tuple:
+    """(usable, reason) for ``device``: a CUDA device and a loadable library of the current ABI; never raises."""
+    device = torch.device(device)
+    if device.type != "cuda":
+        return False, "not a CUDA device"
+    if not torch.cuda.is_available():
+        return False, "CUDA is not available"
+    try:
+        version = _lib.library().citrus_abi_version()
+    except Exception as e:  # noqa: BLE001
+        return False, f"library unavailable ({type(e).__name__}: {e})"
+    return True, f"libcitrus_gb300 ABI {version} on {torch.cuda.get_device_name(device)}"
+
+
+def _check_cuda_f32(name: str, t: Tensor, contiguous: bool = True) -> None:
+    if not isinstance(t, Tensor) or t.device.type != "cuda" or t.dtype != torch.float32:
+        raise ValueError(f"{name} must be a float32 CUDA tensor")
+    if contiguous and not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+# =====================================================================================================================
+# transport sweep
+# =====================================================================================================================
+
+@dataclass(frozen=True, eq=False)
+class FlatPlaneIndex:
+    """Plane-sorted int32 entry tables of a sweep plan on the sweep device (reference ``sweep_kernels.py:44-78``).
+
+    Attributes:
+        octant: [E] octant code of each entry (E = 8 N), sorted by plane.
+        cell: [E] flat cell index.
+        upstream: [E * 3] upstream neighbour along x, y, z, N for vacuum.
+        offsets: num_planes + 1 host ints.
+        offsets_host: the offsets as an int64 CPU tensor (for the per-plane launches).
+        offsets_device: the offsets as an int32 device tensor (for the persistent launch).
+    """
+
+    octant: Tensor
+    cell: Tensor
+    upstream: Tensor
+    offsets: tuple
+    offsets_host: Tensor
+    offsets_device: Tensor
+
+    @property
+    def num_planes(self) -> int:
+        return len(self.offsets) - 1
+
+
+def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tensor, *, method: str = "persistent",
+                 sync: Optional[Tensor] = None, max_blocks: int = 0,
+                 timeout_ns: int = DEFAULT_BARRIER_TIMEOUT_NS, skip_block: int = -1) -> Optional[Tensor]:
+    """Sweep one direction chunk in place (reference ``sweep_kernels.py:265-290``).
+
+    Args:
+        index: the plane-sorted entry tables.
+        store: [8, Dc, N, 4G] or [V, 8, Dc, N, 4G] float32 contiguous source moments, overwritten with the
+            angular-fluence moments (V views sharing ``mu_cells``).
+        mu_cells: [N, G] float32 contiguous total attenuation per cell in 1/cm.
+        c: [8, Dc, 3] float32 contiguous ``|Omega_a| / Delta_a`` of the chunk directions.
+        method: "persistent" (one cooperative launch, grid barrier between planes) or "planes" (one launch per plane).
+        sync: [4] int32 device scratch of the persistent launch; allocated when None.
+        max_blocks: cap on the persistent grid (0: as many blocks as fit).
+        timeout_ns: bound of every barrier wait of the persistent launch.
+        skip_block: test hook forcing a barrier timeout (-1 in normal use).
+
+    Returns:
+        The sync words of the persistent launch (``sync[2] != 0`` means a barrier wait ran out), or None.
+    """
+    if store.dim() == 4:
+        views, (_, Dc, N, Q) = 1, store.shape
+    elif store.dim() == 5:
+        views, _, Dc, N, Q = store.shape
+    else:
+        raise ValueError(f"store must be [8, Dc, N, 4G] or [V, 8, Dc, N, 4G], got {tuple(store.shape)}")
+    if store.shape[-4] != 8 or Q % 4:
+        raise ValueError(f"store must be [.., 8, Dc, N, 4G], got {tuple(store.shape)}")
+    G = Q // 4
+    _check_cuda_f32("store", store)
+    _check_cuda_f32("mu_cells", mu_cells)
+    _check_cuda_f32("c", c)
+    if tuple(mu_cells.shape) != (N, G):
+        raise ValueError(f"mu_cells must be [{N}, {G}], got {tuple(mu_cells.shape)}")
+    if tuple(c.shape) != (8, Dc, 3):
+        raise ValueError(f"c must be [8, {Dc}, 3], got {tuple(c.shape)}")
+    if index.octant.numel() != 8 * N:
+        raise ValueError("the plane index does not belong to this grid")
+    stream = _lib.stream_handle(store.device)
+    if method == "planes":
+        _lib.call("citrus_sweep_planes", store.data_ptr(), mu_cells.data_ptr(), c.data_ptr(), index.octant.data_ptr(),
+                  index.cell.data_ptr(), index.upstream.data_ptr(), index.offsets_host.data_ptr(), index.num_planes,
+                  N, G, Dc, views, stream)
+        return None
+    if method != "persistent":
+        raise ValueError(f"method must be 'persistent' or 'planes', got {method!r}")
+    if sync is None:
+        sync = torch.empty(4, dtype=torch.int32, device=store.device)
+    _lib.call("citrus_sweep_persistent", store.data_ptr(), mu_cells.data_ptr(), c.data_ptr(), index.octant.data_ptr(),
+              index.cell.data_ptr(), index.upstream.data_ptr(), index.offsets_device.data_ptr(), index.num_planes, N,
+              G, Dc, views, sync.data_ptr(), int(max_blocks), int(timeout_ns), int(skip_block), stream)
+    return sync
+
+
+# =====================================================================================================================
+# small-K products
+# =====================================================================================================================
+
+def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False) -> Tensor:
+    """``C (=|+=) A @ B`` for A [M, K] and B, C [.., K or M, J] row-major 2-D (or batched 3-D) views.
+
+    B and C may be strided views whose last axis is contiguous; J must be a multiple of 4.
+    """
+    _check_cuda_f32("A", A, contiguous=False)
+    _check_cuda_f32("B", B, contiguous=False)
+    _check_cuda_f32("C", C, contiguous=False)
+    if A.dim() != 2 or A.stride(1) != 1:
+        raise ValueError("A must be a 2-D row-major matrix")
+    if B.dim() == 2:
+        B, C = B[None], C[None]
+    if B.dim() != 3 or C.dim() != 3 or B.shape[0] != C.shape[0]:
+        raise ValueError("B and C must be 2-D matrices or equal batches of them")
+    M, K = A.shape
+    batch, KB, J = B.shape
+    if KB != K or tuple(C.shape) != (batch, M, J):
+        raise ValueError(f"shape mismatch: A {tuple(A.shape)}, B {tuple(B.shape)}, C {tuple(C.shape)}")
+    if B.stride(2) != 1 or C.stride(2) != 1:
+        raise ValueError("B and C need a contiguous last axis")
+    _lib.call("citrus_small_k_gemm", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(), C.stride(1),
+              M, K, J, batch, B.stride(0) if batch > 1 else 0, C.stride(0) if batch > 1 else 0, int(bool(accumulate)),
+              _lib.stream_handle(A.device))
+    return C
+
+
+# =====================================================================================================================
+# scattering moments
+# =====================================================================================================================
+
+def cell_major_view(storage: Tensor, num_spatial: int) -> Tensor:
+    """The ``[G, N, (4), *spatial]`` view of cell-major storage ``[N, *spatial, G, (4)]``."""
+    g = num_spatial + 1
+    spatial_axes = list(range(1, num_spatial + 1))
+    if storage.dim() == num_spatial + 3:
+        return storage.permute(g, 0, g + 1, *spatial_axes)
+    return storage.permute(g, 0, *spatial_axes)
+
+
+def _merged_stride(t: Tensor, first: int) -> Optional[int]:
+    sizes, strides = t.shape[first:], t.stride()[first:]
+    kept = [(n, s) for n, s in zip(sizes, strides) if n != 1]
+    if not kept:
+        return 1
+    for (n0, s0), (n1, s1) in zip(kept, kept[1:]):
+        if s0 != s1 * n1:
+            return None
+    return kept[-1][1]
+
+
+def scattering_moments(transfer: Tensor, phi: Tensor, layout: str = "contiguous") -> Tensor:
+    """Scattering-source moments ``T[g, n] = sum_g' transfer[g', g, l(n)] phi[g', n]`` (reference
+    ``scattering_kernels.py:206-252``), in a new tensor of the requested storage.
+
+    Args:
+        transfer: [G_in, G_out, L_x+1, *spatial] Legendre transfer moments in 1/cm.
+        phi: [G_in, N, *rest] moments, rest = spatial or (4, *spatial), any strides.
+        layout: "contiguous" ([G_out, N, *rest]), "moment_major" ([N, G_out, *rest]) or "cell_major"
+            ([N, *spatial, G_out, (4)], the sweep's storage).
+
+    Returns:
+        [G_out, N, *rest] view of the requested storage.
+    """
+    if layout not in LAYOUTS:
+        raise ValueError(f"layout must be one of {LAYOUTS}, got {layout!r}")
+    _check_cuda_f32("transfer", transfer, contiguous=False)
+    _check_cuda_f32("phi", phi, contiguous=False)
+    G_in, G_out, num_legendre = (int(v) for v in transfer.shape[:3])
+    spatial = tuple(int(v) for v in transfer.shape[3:])
+    N = int(phi.shape[1])
+    rest = tuple(int(v) for v in phi.shape[2:])
+    if phi.shape[0] != G_in:
+        raise ValueError(f"phi has {phi.shape[0]} groups, transfer has {G_in}")
+    L = math.isqrt(N) - 1
+    if (L + 1) ** 2 != N or L + 1 > num_legendre:
+        raise ValueError(f"phi has {N} moments, not (L+1)^2 with L < {num_legendre}")
+    has_k = rest != spatial
+    if has_k and (len(rest) != len(spatial) + 1 or rest[0] != 4 or rest[1:] != spatial):
+        raise ValueError(f"phi trailing shape {rest} must be spatial {spatial} or (4, *spatial)")
+    X = math.prod(spatial)
+    transfer = transfer.contiguous()
+    ps_x = _merged_stride(phi, phi.dim() - len(spatial))
+    if ps_x is None:
+        phi = phi.contiguous()
+        ps_x = 1
+    if layout == "contiguous":
+        out = torch.empty((G_out, N) + rest, device=phi.device, dtype=phi.dtype)
+    elif layout == "moment_major":
+        out = torch.empty((N, G_out) + rest, device=phi.device, dtype=phi.dtype).movedim(0, 1)
+    else:
+        storage = torch.empty((N,) + spatial + (G_out,) + ((4,) if has_k else ()), device=phi.device,
+                              dtype=phi.dtype)
+        out = cell_major_view(storage, len(spatial))
+    os_x = _merged_stride(out, out.dim() - len(spatial))
+    if X == 0:
+        return out
+    _lib.call("citrus_scattering_moments", transfer.data_ptr(), phi.data_ptr(), out.data_ptr(), G_in, G_out,
+              num_legendre, N, 4 if has_k else 1, X, phi.stride(0), phi.stride(1), phi.stride(2) if has_k else 0,
+              ps_x, out.stride(0), out.stride(1), out.stride(2) if has_k else 0, os_x,
+              _lib.stream_handle(phi.device))
+    return out

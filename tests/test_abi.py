@@ -1,0 +1,63 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point that ``include/*.h`` declares (no GPU
+needed: nothing is launched)."""
+
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from citrus_gb300 import _lib
+from citrus_gb300.build import build
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared_functions() -> list:
+    names = []
+    for header in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?(?:int|char\s*\*|const char\s*\*)\s*\*?\s*(citrus_\w+)\s*\(", text,
+                            flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def library():
+    build()
+    return ctypes.CDLL(str(_lib.LIBRARY_PATH))
+
+
+def test_header_declares_entry_points():
+    names = _declared_functions()
+    assert "citrus_abi_version" in names and "citrus_sweep_persistent" in names
+    assert len(names) >= 6
+
+
+def test_library_exports_every_declared_symbol(library):
+    missing = [n for n in _declared_functions() if not hasattr(library, n)]
+    assert not missing, missing
+
+
+def test_bindings_cover_the_header():
+    declared = set(_declared_functions()) - {"citrus_last_error_string"}
+    assert declared == set(_lib.SIGNATURES), declared ^ set(_lib.SIGNATURES)
+
+
+def test_abi_version_and_error_string(library):
+    library.citrus_abi_version.restype = ctypes.c_int
+    assert library.citrus_abi_version() == 1
+    library.citrus_last_error_string.restype = ctypes.c_char_p
+    assert isinstance(library.citrus_last_error_string(), bytes)
+
+
+def test_bad_arguments_are_rejected_before_any_launch(library):
+    """Null pointers and bad sizes return CITRUS_EINVAL with a message; nothing touches a device."""
+    lib = _lib.library()
+    status = lib.citrus_small_k_gemm(None, 1, None, 4, None, 4, 1, 1, 4, 1, 0, 0, 0, None)
+    assert status == 1
+    assert b"null" in lib.citrus_last_error_string()
+    status = lib.citrus_sweep_planes(None, None, None, None, None, None, None, 1, 1, 1, 1, 1, None)
+    assert status == 1

@@ -1,0 +1,108 @@
+"""The oracle and the host set-up tables against fixtures generated from the reference (CPU only)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+from citrus_gb300.geometry import Grid
+from citrus_gb300.quadrature import Quadrature, hemisphere_quadrature, product_quadrature, real_spherical_harmonics
+from citrus_gb300.transport_sweep import build_sweep_plan
+from oracle import sweep as osweep
+
+
+def test_product_quadrature_and_harmonics_match_reference():
+    g = golden("quadrature_tables")
+    for p, a, L in ((4, 12, 3), (6, 20, 5), (10, 24, 7)):
+        q = product_quadrature(p, a)
+        np.testing.assert_allclose(q.omega, g[f"omega_{p}x{a}"], rtol=0, atol=1e-15)
+        np.testing.assert_allclose(q.weight, g[f"weight_{p}x{a}"], rtol=0, atol=1e-15)
+        np.testing.assert_allclose(real_spherical_harmonics(L, q.omega), g[f"Y_{p}x{a}_L{L}"], rtol=0, atol=1e-13)
+
+
+def test_cone_set_with_cell_widths_matches_reference():
+    g = golden("quadrature_tables")
+    cone = hemisphere_quadrature([0.3, -0.9, 0.1], 8, 16, 0.4, tangent_axes=((0.9, 0.3, 0.0), (0.0, 0.0, 1.0)))
+    np.testing.assert_allclose(cone.omega, g["cone_omega"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(cone.weight, g["cone_weight"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(cone.cell_width, g["cone_width"], rtol=1e-12, atol=1e-14)
+
+
+def test_sweep_plan_matches_reference():
+    g = golden("sweep_small")
+    plan = build_sweep_plan(tuple(g["shape"]))
+    np.testing.assert_array_equal(plan.plane_offsets, g["plane_offsets"])
+    np.testing.assert_array_equal(plan.octant, g["octant"])
+    np.testing.assert_array_equal(plan.cell, g["cell"])
+    np.testing.assert_array_equal(plan.upstream, g["upstream"])
+    offsets, octant, cell, upstream = osweep.plan(tuple(g["shape"]))
+    np.testing.assert_array_equal(offsets, g["plane_offsets"])
+    np.testing.assert_array_equal(upstream, g["upstream"])
+
+
+def test_octant_reordering_matches_reference():
+    g = golden("sweep_small")
+    q = product_quadrature(4, 8)
+    perm = q.by_octant()
+    np.testing.assert_array_equal(perm, g["permutation"])
+    np.testing.assert_allclose(q.omega[perm], g["omega"], atol=0)
+
+
+def test_oracle_sweep_matches_reference():
+    g = golden("sweep_small")
+    phi, psi = osweep.sweep(tuple(g["shape"]), tuple(g["deltas"]), g["omega"], g["weight"], int(g["L"]), g["mu"],
+                            g["source"], direction_chunk=3)
+    assert rel_err(psi, g["psi"]) < 1e-13
+    assert rel_err(phi, g["phi"]) < 1e-13
+
+
+def test_oracle_scatter_moments_matches_reference():
+    g = golden("scatter_moments_small")
+    assert rel_err(osweep.scatter_moments(g["transfer"], g["phi4"]), g["T4"]) < 1e-14
+    assert rel_err(osweep.scatter_moments(g["transfer"], g["phi1"]), g["T1"]) < 1e-14
+
+
+@pytest.mark.parametrize("axis, sign", [(a, s) for a in range(3) for s in (1, -1)])
+def test_oracle_slab_against_one_dimensional_solution(axis, sign):
+    """A slab along one axis, direction along that axis: the 3-D LD solve reduces to the 1-D textbook cell equations
+    (reference tests/oracles/linear_discontinuous_slab_1d.py), solved here independently."""
+    rng = np.random.default_rng(10 + axis)
+    K, G = 7, 2
+    deltas = (0.7, 1.3, 0.9)
+    shape = [2, 2, 2]
+    dim = {0: 1, 1: 0, 2: 2}[axis]
+    shape[dim] = K
+    direction = np.zeros(3)
+    direction[axis] = sign
+    # one direction per octant; the slab direction replaces its own octant's entry
+    base = np.array([0.3, 0.5, 0.81]) / np.linalg.norm([0.3, 0.5, 0.81])
+    omega = base[None] * osweep.SIGNS
+    code = int((direction < 0) @ np.array([4, 2, 1]))
+    omega[code] = direction
+    weight = np.full(8, 4 * np.pi / 8)
+    mu1 = rng.random((G, K)) * 1.5 + 0.05
+    S0, S1 = rng.random((G, K)), rng.standard_normal((G, K)) * 0.3
+
+    def along(v):
+        view = [G, 1, 1, 1]
+        view[1 + dim] = K
+        return np.broadcast_to(v.reshape(view), (G, *shape)).copy()
+
+    mu = along(mu1)
+    src = np.zeros((8, G, 4, *shape))
+    src[:, :, 0] = along(S0)
+    src[:, :, 1 + axis] = along(S1)
+    _, psi = osweep.sweep(tuple(shape), deltas, omega, weight, 1, mu, src)
+    c = 1.0 / deltas[axis]
+    for g in range(G):
+        p0, p1 = np.zeros(K), np.zeros(K)
+        psi_in = 0.0
+        for kk in (range(K) if sign > 0 else range(K - 1, -1, -1)):
+            A = np.array([[c + mu1[g, kk], c], [-3 * c, 3 * c + mu1[g, kk]]])
+            b = np.array([S0[g, kk] + c * psi_in, sign * S1[g, kk] - 3 * c * psi_in])
+            a0, a1 = np.linalg.solve(A, b)
+            p0[kk], p1[kk] = a0, sign * a1
+            psi_in = a0 + a1
+        np.testing.assert_allclose(psi[code, g, 0], along(p0[None].repeat(G, 0))[g], atol=1e-12)
+        np.testing.assert_allclose(psi[code, g, 1 + axis], along(p1[None].repeat(G, 0))[g], atol=1e-12)

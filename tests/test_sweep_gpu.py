@@ -1,0 +1,154 @@
+"""Parity of the sm_103a sweep, small-K products and scattering moments with the float64 oracle."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden, rel_err
+from citrus_gb300 import kernels
+from citrus_gb300.geometry import Grid
+from citrus_gb300.quadrature import product_quadrature
+from citrus_gb300.source_iteration import scatter_moments, scatter_source_function, source_iteration
+from citrus_gb300.transport_sweep import make_sweep_context, sweep
+from oracle import sweep as osweep
+
+pytestmark = pytest.mark.gpu
+F32_REL = 1e-5  # float32 sweep vs float64 oracle, relative to the field maximum
+
+
+def _direction_source(src):
+    return lambda idx: src.index_select(0, idx)
+
+
+@pytest.mark.parametrize("method", ["persistent", "planes"])
+@pytest.mark.parametrize("chunk", [None, 3])
+def test_sweep_matches_reference_fixture(cuda_device, method, chunk):
+    g = golden("sweep_small")
+    grid = Grid(tuple(g["shape"]), 0.7, 1.3 / 0.7, 0.9 / 0.7)
+    ctx = make_sweep_context(grid, product_quadrature(4, 8), int(g["L"]), cuda_device)
+    mu = torch.as_tensor(g["mu"], dtype=torch.float32, device=cuda_device)
+    src = torch.as_tensor(g["source"], dtype=torch.float32, device=cuda_device)
+    phi, psi = sweep(ctx, mu, _direction_source(src), direction_chunk=chunk, return_psi=True, method=method)
+    assert rel_err(psi, g["psi"]) < F32_REL
+    assert rel_err(phi, g["phi"]) < F32_REL
+
+
+@pytest.mark.parametrize("shape, G, L, polar, azimuthal", [((9, 7, 8), 1, 3, 4, 12), ((6, 10, 5), 8, 5, 6, 20),
+                                                           ((2, 2, 2), 12, 1, 2, 4), ((1, 5, 3), 16, 2, 4, 8)])
+def test_sweep_matches_oracle(cuda_device, shape, G, L, polar, azimuthal):
+    rng = np.random.default_rng(sum(shape) + G)
+    grid = Grid(shape, 0.5, 1.2, 0.8)
+    q = product_quadrature(polar, azimuthal)
+    ctx = make_sweep_context(grid, q, L, cuda_device)
+    mu = rng.random((G, *shape)) * 2.0 + 0.05
+    src = rng.standard_normal((q.num_directions, G, 4, *shape))
+    phi_ref, psi_ref = osweep.sweep(shape, grid.deltas, ctx.quadrature.omega, ctx.quadrature.weight, L, mu, src)
+    for method in ("persistent", "planes"):
+        phi, psi = sweep(ctx, torch.as_tensor(mu, dtype=torch.float32, device=cuda_device),
+                         _direction_source(torch.as_tensor(src, dtype=torch.float32, device=cuda_device)),
+                         return_psi=True, method=method)
+        assert rel_err(psi, psi_ref) < F32_REL, method
+        assert rel_err(phi, phi_ref) < F32_REL, method
+
+
+def test_persistent_and_per_plane_sweeps_agree_bitwise(cuda_device):
+    rng = np.random.default_rng(5)
+    shape, G = (12, 9, 10), 8
+    ctx = make_sweep_context(Grid(shape, 0.4), product_quadrature(6, 20), 5, cuda_device)
+    mu = torch.as_tensor(rng.random((G, *shape)) + 0.1, dtype=torch.float32, device=cuda_device)
+    src = torch.as_tensor(rng.standard_normal((120, G, 4, *shape)), dtype=torch.float32, device=cuda_device)
+    a = sweep(ctx, mu, _direction_source(src), method="persistent")
+    b = sweep(ctx, mu, _direction_source(src), method="planes")
+    assert torch.equal(a, b)
+
+
+def test_batched_views_sweep_matches_single_views(cuda_device):
+    rng = np.random.default_rng(6)
+    shape, G, V = (6, 5, 7), 4, 3
+    ctx = make_sweep_context(Grid(shape, 0.5), product_quadrature(4, 8), 2, cuda_device)
+    N = ctx.num_cells
+    mu = torch.as_tensor(rng.random((N, G)) + 0.1, dtype=torch.float32, device=cuda_device)
+    c = ctx.c.contiguous()
+    stores = torch.as_tensor(rng.standard_normal((V, 8, 4, N, 4 * G)), dtype=torch.float32, device=cuda_device)
+    single = stores.clone()
+    for v in range(V):
+        kernels.sweep_planes(ctx.flat_index, single[v], mu, c, method="planes")
+    batched = stores.clone()
+    kernels.sweep_planes(ctx.flat_index, batched, mu, c, method="persistent")
+    assert torch.equal(single, batched)
+
+
+def test_persistent_barrier_timeout_is_reported(cuda_device):
+    """A block that never arrives makes every barrier wait run out after the bounded timeout; the kernel returns and
+    the sync word records it (no hang, the context stays usable)."""
+    ctx = make_sweep_context(Grid((4, 4, 4), 1.0), product_quadrature(2, 4), 1, cuda_device)
+    N, G = ctx.num_cells, 2
+    store = torch.zeros(8, 1, N, 4 * G, device=cuda_device)
+    mu = torch.ones(N, G, device=cuda_device)
+    sync = kernels.sweep_planes(ctx.flat_index, store, mu, ctx.c.contiguous(), max_blocks=4,
+                                timeout_ns=20_000_000, skip_block=1)
+    torch.cuda.synchronize()
+    assert int(sync[2]) != 0
+    ok = kernels.sweep_planes(ctx.flat_index, store, mu, ctx.c.contiguous(), max_blocks=4)
+    torch.cuda.synchronize()
+    assert int(ok[2]) == 0
+
+
+@pytest.mark.parametrize("M, K, J, batch, accumulate", [(120, 36, 4096, 1, False), (36, 120, 1028, 1, True),
+                                                        (5, 7, 64, 3, True), (240, 64, 512, 2, False),
+                                                        (1, 1, 4, 1, False)])
+def test_small_k_gemm_matches_numpy(cuda_device, M, K, J, batch, accumulate):
+    rng = np.random.default_rng(M * 7 + K)
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((batch, K, J))
+    C0 = rng.standard_normal((batch, M, J))
+    expected = np.einsum("mk,bkj->bmj", A, B) + (C0 if accumulate else 0)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    C = dev(C0)
+    kernels.small_k_gemm(dev(A), dev(B), C, accumulate=accumulate)
+    assert rel_err(C, expected) < 1e-5
+
+
+def test_scattering_moments_match_reference_fixture(cuda_device):
+    g = golden("scatter_moments_small")
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    for layout in kernels.LAYOUTS:
+        assert rel_err(kernels.scattering_moments(dev(g["transfer"]), dev(g["phi4"]), layout), g["T4"]) < 1e-5
+        assert rel_err(kernels.scattering_moments(dev(g["transfer"]), dev(g["phi1"]), layout), g["T1"]) < 1e-5
+    # a strided view of cell-major storage, as the sweep returns it
+    storage = dev(np.ascontiguousarray(np.moveaxis(g["phi4"], (0, 2), (4, 5))))  # [N, R, C, S, G, 4]
+    view = kernels.cell_major_view(storage, 3)
+    assert rel_err(scatter_moments(dev(g["transfer"]), view), g["T4"]) < 1e-5
+
+
+def test_source_iteration_matches_oracle(cuda_device):
+    rng = np.random.default_rng(8)
+    shape, G, L = (5, 6, 4), 3, 3
+    grid = Grid(shape, 0.6)
+    q = product_quadrature(4, 8)
+    ctx = make_sweep_context(grid, q, L, cuda_device)
+    mu = rng.random((G, *shape)) * 1.0 + 0.5
+    transfer = np.zeros((G, G, L + 1, *shape))
+    for gi in range(G):
+        for go in range(gi, G):
+            transfer[gi, go, 0] = 0.2 * (0.5 ** (go - gi)) * mu[gi]
+            transfer[gi, go, 1] = 0.05 * transfer[gi, go, 0]
+    first = np.abs(rng.standard_normal((32, G, 4, *shape)))
+    total, n, history = osweep.source_iteration(shape, grid.deltas, ctx.quadrature.omega, ctx.quadrature.weight, L,
+                                                mu, transfer, first, 1e-3, 12)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    result = source_iteration(ctx, dev(mu), dev(transfer), _direction_source(dev(first)), 1e-3, 12)
+    assert result.num_iterations == n
+    assert rel_err(result.phi_total, total) < 2e-5
+    np.testing.assert_allclose(result.history, history, rtol=1e-3)
+    # the cell-major source function of the scattering source against the oracle's expansion
+    T = scatter_moments(dev(transfer), result.phi_total)
+    source = scatter_source_function(ctx, T)
+    idx = torch.arange(ctx.num_directions, device=cuda_device)
+    got = source(idx).permute(0, 4, 5, 1, 2, 3)
+    from citrus_gb300.quadrature import real_spherical_harmonics
+    expected = osweep.scatter_source(real_spherical_harmonics(L, ctx.quadrature.omega),
+                                     osweep.scatter_moments(transfer, result.phi_total.double().cpu().numpy()))
+    assert rel_err(got, expected) < 1e-5
