@@ -1,0 +1,265 @@
+"""Benchmark of the CITRUS scatter step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload step|sweep]
+
+Prints one JSON line. The default workload is the batched circular cone-beam scatter step: 64^3 cells of 0.4 cm,
+8 groups (30-120 keV), P5, 120 sweep directions, a 256 x 192 curved panel, 60 views per outer iteration; one step
+is the full scatter step of every view (uncollided fluence, one accumulator sweep, the signal-only collapsed-cone
+image). ``--workload sweep`` times the accumulator sweep alone (scattering moments, source expansion, wavefront
+sweep, moment accumulation) of one view.
+
+The reference arm (``--impl reference``) times the float64 CPU restatement of the same path on the host cores, on a
+bounded sample of the same workload, and reports the same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+
+def _parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="sweep", choices=["sweep"])
+    p.add_argument("--method", default="persistent", choices=["persistent", "planes"])
+    p.add_argument("--dc", type=int, default=0, help="directions per octant per sweep chunk (0: all)")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    return p.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._thread = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                vals = [v.strip() for v in out.stdout.strip().split(",")]
+                if len(vals) >= 7:
+                    self.samples.append(vals)
+            except Exception:  # noqa: BLE001
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thread = threading.Thread(target=self._run, daemon=True)
+        self._thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._thread.join(timeout=10)
+
+    def summary(self) -> dict:
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for s in self.samples for n, v in zip(names, s[3:7]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _peaks() -> dict:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return {"hbm_gbs": float(data["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# =====================================================================================================================
+# workloads
+# =====================================================================================================================
+
+def sweep_workload(device):
+    """One view's accumulator sweep at 64^3, G = 8, P5, 120 directions."""
+    import numpy as np
+    import torch
+
+    from citrus_gb300 import kernels
+    from citrus_gb300.workloads import config2_sweep_problem
+
+    prob = config2_sweep_problem(device)
+    return prob
+
+
+def run_gb300(args):
+    import torch
+
+    from citrus_gb300 import kernels
+    from citrus_gb300.source_iteration import scatter_moments, scatter_source_function
+    from citrus_gb300.transport_sweep import sweep
+    from citrus_gb300.workloads import config2_sweep_problem
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+
+    prob = config2_sweep_problem(device)
+    ctx, mu_t, transfer, phi0 = prob["ctx"], prob["mu_t"], prob["transfer"], prob["phi"]
+    N, G = ctx.num_cells, int(mu_t.shape[0])
+    D8 = args.dc if 0 < args.dc < ctx.directions_per_octant else ctx.directions_per_octant
+    updates = 8 * D8 * N * G
+
+    # events around the sweep kernel itself, on the stream it runs on
+    sweep_times = []
+    stream = torch.cuda.current_stream(device)
+
+    def one_step(phi, record):
+        T = scatter_moments(transfer, phi)
+        source = scatter_source_function(ctx, T)
+        mu_cells = mu_t.reshape(G, N).t().contiguous()
+        store = torch.empty(8, D8, N, 4 * G, device=device)
+        idx = ctx.direction_indices(0, D8)
+        source(idx, out=store.view(8 * D8, *ctx.shape, G, 4))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c[:, :D8].contiguous(), method=args.method)
+        e1.record(stream)
+        moments = torch.empty(ctx.num_moments, N * 4 * G, device=device)
+        kernels.small_k_gemm(ctx.Y_weighted.index_select(0, idx).t().contiguous(), store.view(8 * D8, -1), moments)
+        if record:
+            sweep_times.append((e0, e1))
+        return moments.view(ctx.num_moments, N, G, 4).permute(2, 0, 3, 1).reshape(G, ctx.num_moments, 4, *ctx.shape)
+
+    phi = phi0
+    for _ in range(args.warmup):
+        one_step(phi, False)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with sampler:
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            one_step(phi, True)
+        end.record(stream)
+        torch.cuda.synchronize()
+    elapsed = start.elapsed_time(end) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t)
+    kernel_s = statistics.mean(a.elapsed_time(b) / 1e3 for a, b in sweep_times)
+    # e2e through host buffers: the accumulator moments in from pinned host memory, the new ones out
+    host_phi = torch.empty(phi0.shape, dtype=torch.float32, pin_memory=True)
+    host_phi.copy_(phi0.cpu())
+    host_out = torch.empty(phi0.shape, dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    e2e0, e2e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e0.record(stream)
+    for _ in range(args.steps):
+        dev_phi = host_phi.to(device, non_blocking=True).view(phi0.shape)
+        new = one_step(dev_phi, False)
+        host_out.copy_(new, non_blocking=True)
+    e2e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = e2e0.elapsed_time(e2e1) / 1e3
+    peaks = _peaks()
+    achieved = updates * 32 / kernel_s / 1e9
+    line = {
+        "metric": "accumulator sweep cell*dir*group updates/s (scatter-step sweep stage)",
+        "value": updates * args.steps * world / elapsed, "unit": "updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"64^3 cells x 0.4 cm, G=8, P5 (36 moments), {8 * D8} of 120 directions (6x20), one view "
+                               f"per step",
+                   "l2": "inputs larger than L2 (4.0 GB store)", "sweep_method": args.method},
+        "e2e": {"value": updates * args.steps / e2e_s, "unit": "updates/s",
+                "h2d_bytes_per_step": host_phi.numel() * 4, "d2h_bytes_per_step": host_out.numel() * 4},
+        "gpu_launches": 4 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
+                     "kernel": "sweep persistent wavefront", "kernel_ms": kernel_s * 1e3,
+                     "algorithmic_bytes": updates * 32},
+        "clocks": sampler.summary(),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = None if args.no_cpu else cpu_baseline_sweep()
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline_sweep(budget_s: float = 20.0) -> dict:
+    """The C restatement of the sweep (float64, OpenMP on every host core) on whole-grid chunks of one direction per
+    octant, as many of the view's 15 chunks as fit the time budget."""
+    import numpy as np
+
+    from citrus_gb300.workloads import config2_sweep_problem_host
+    from oracle import native
+    from oracle import sweep as osweep
+
+    prob = config2_sweep_problem_host()
+    shape, G = prob["shape"], prob["G"]
+    N = int(np.prod(shape))
+    plan = osweep.plan(shape)
+    rng = np.random.default_rng(0)
+    mu_cells = np.ascontiguousarray(prob["mu_t"].reshape(G, N).T)
+    source = rng.random((8, 1, N, G, 4))
+    native.sweep_chunk(plan, prob["c"][:, :1], mu_cells, source)  # warm-up (threads, pages)
+    done = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and done < 15:
+        native.sweep_chunk(plan, prob["c"][:, done:done + 1], mu_cells, source)
+        done += 1
+    elapsed = time.perf_counter() - t0
+    return {"value": 8 * done * N * G / elapsed, "unit": "updates/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{done} of 15 direction chunks (8 directions each) of one 64^3 x G=8 view sweep, float64 C "
+                      f"restatement, OpenMP"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    base = cpu_baseline_sweep(budget_s=max(5.0, 60.0 / max(1, args.steps + args.warmup)))
+    line = {"metric": "accumulator sweep cell*dir*group updates/s (scatter-step sweep stage)", "value": base["value"],
+            "unit": "updates/s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "64^3 cells x 0.4 cm, G=8, P5 (36 moments), 120 directions (6x20), one view"},
+            "cpu_baseline": base, "e2e": {"value": base["value"], "unit": "updates/s", "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = _parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

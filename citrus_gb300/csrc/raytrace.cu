@@ -1,0 +1,446 @@
+// Exact line integrals of voxel fields (Siddon / Amanatides-Woo traversal), the five ray operations of the
+// reference's Projectors protocol (citrus/scatter_solver/ray_tracing.py:27-115, 141-202 and the Triton kernels of
+// kernels/ray_tracing_kernels.py:215-639).
+//
+// Each ray is clipped to the grid box (the segment parameters of ray_tracing.py:160-173), then walked voxel by voxel.
+// The walk keeps the ray's position as integer voxel indices plus a fractional position inside the current voxel, so
+// every segment length is computed from quantities of voxel size (relative error ~ float epsilon per segment), and the
+// travelled distance is summed with a compensated (Kahan) sum, so the end of the ray is placed to float epsilon of its
+// total length. Rays that must meet 1e-6 relative path lengths (upstream to points, primary) do their set-up in
+// float64; the dense image rays (downstream, oblique) do it in float32.
+//
+// Volumes are read voxel-major, [V, C] with the C channels (groups or materials) of a voxel contiguous, so one voxel
+// visit is one or two 16-byte loads for every channel at once.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace citrus {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxChannels = 32;
+
+struct Box {
+  double lo[3];     // lower corner (x, y, z) in cm
+  double delta[3];  // voxel sizes (x, y, z) in cm
+  int n[3];         // voxel counts (x = columns, y = rows, z = slices)
+};
+
+Box make_box(const double* box, const int64_t* dims) {
+  Box b;
+  for (int a = 0; a < 3; ++a) {
+    b.lo[a] = box[a];
+    b.delta[a] = box[3 + a];
+    b.n[a] = (int)dims[a];
+  }
+  return b;
+}
+
+template <typename T>
+struct Setup {
+  bool hit;
+  float total;      // length of the clipped segment in cm
+  float v[3];       // direction in voxel units per cm
+  int idx[3];       // voxel index at the entry point
+  float f[3];       // fractional position inside that voxel, in [0, 1]
+};
+
+// Clip p0 -> p1 to the box and locate the entry voxel. T is the arithmetic type of the set-up (double or float).
+template <typename T>
+__device__ __forceinline__ Setup<T> ray_setup(const Box& b, const T p0[3], const T p1[3]) {
+  Setup<T> s;
+  T d[3];
+  T a_lo = 0, a_hi = 1;
+  for (int a = 0; a < 3; ++a) {
+    d[a] = p1[a] - p0[a];
+    const T lo = (T)b.lo[a], hi = (T)b.lo[a] + (T)b.delta[a] * (T)b.n[a];
+    if (d[a] != 0) {
+      const T inv = (T)1 / d[a];
+      const T t1 = (lo - p0[a]) * inv, t2 = (hi - p0[a]) * inv;
+      a_lo = fmax(a_lo, fmin(t1, t2));
+      a_hi = fmin(a_hi, fmax(t1, t2));
+    } else if (!(p0[a] >= lo && p0[a] <= hi)) {
+      a_hi = -1;  // parallel to this slab and outside it
+    }
+  }
+  const T len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  s.hit = a_hi > a_lo && len > 0;
+  if (!s.hit) {
+    s.total = 0.f;
+    return s;
+  }
+  s.total = (float)((a_hi - a_lo) * len);
+  for (int a = 0; a < 3; ++a) {
+    const T u = d[a] / len;
+    s.v[a] = (float)(u / (T)b.delta[a]);
+    const T q = (p0[a] + a_lo * d[a] - (T)b.lo[a]) / (T)b.delta[a];
+    T fl = floor(q);
+    int i = (int)fl;
+    if (i < 0) i = 0;
+    if (i > b.n[a] - 1) i = b.n[a] - 1;
+    T fr = q - (T)i;
+    if (fr < 0) fr = 0;
+    if (fr > 1) fr = 1;
+    s.idx[a] = i;
+    s.f[a] = (float)fr;
+  }
+  return s;
+}
+
+// Walk one clipped ray and add the integral of the C channels to acc (in cm times the field unit).
+template <int kC, bool kCompensated>
+__device__ __forceinline__ void ray_walk(const Box& b, const Setup<float>& s, const float* __restrict__ vol, int C,
+                                         float* acc) {
+  const int nC = kC > 0 ? kC : C;
+  float comp_acc[kC > 0 ? kC : kMaxChannels];
+  if (kCompensated)
+    for (int c = 0; c < nC; ++c) comp_acc[c] = 0.f;
+  int ix = s.idx[0], iy = s.idx[1], iz = s.idx[2];
+  float fx = s.f[0], fy = s.f[1], fz = s.f[2];
+  const float vx = s.v[0], vy = s.v[1], vz = s.v[2];
+  const float ivx = vx != 0.f ? 1.f / fabsf(vx) : INFINITY;
+  const float ivy = vy != 0.f ? 1.f / fabsf(vy) : INFINITY;
+  const float ivz = vz != 0.f ? 1.f / fabsf(vz) : INFINITY;
+  const int stx = vx > 0.f ? 1 : -1, sty = vy > 0.f ? 1 : -1, stz = vz > 0.f ? 1 : -1;
+  float t = 0.f, t_comp = 0.f;  // travelled distance, Kahan-compensated
+  const int max_steps = b.n[0] + b.n[1] + b.n[2] + 3;
+  for (int step = 0; step < max_steps; ++step) {
+    const float dx = (vx > 0.f ? 1.f - fx : fx) * ivx;
+    const float dy = (vy > 0.f ? 1.f - fy : fy) * ivy;
+    const float dz = (vz > 0.f ? 1.f - fz : fz) * ivz;
+    int axis = 0;
+    float dt = dx;
+    if (dy < dt) { dt = dy; axis = 1; }
+    if (dz < dt) { dt = dz; axis = 2; }
+    const float remaining = (s.total - t) + t_comp;
+    const bool last = dt >= remaining;
+    if (last) dt = fmaxf(remaining, 0.f);
+    const float* vox = vol + ((int64_t)(iy * b.n[0] + ix) * b.n[2] + iz) * nC;
+    if (kC == 8 || kC == 4) {
+#pragma unroll
+      for (int c = 0; c < (kC > 0 ? kC : 1); c += 4) {
+        const float4 w = __ldg(reinterpret_cast<const float4*>(vox + c));
+        if (kCompensated) {
+          const float vals[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float y = dt * vals[q] - comp_acc[c + q];
+            const float tt = acc[c + q] + y;
+            comp_acc[c + q] = (tt - acc[c + q]) - y;
+            acc[c + q] = tt;
+          }
+        } else {
+          acc[c] = fmaf(dt, w.x, acc[c]);
+          acc[c + 1] = fmaf(dt, w.y, acc[c + 1]);
+          acc[c + 2] = fmaf(dt, w.z, acc[c + 2]);
+          acc[c + 3] = fmaf(dt, w.w, acc[c + 3]);
+        }
+      }
+    } else {
+      for (int c = 0; c < nC; ++c) {
+        const float w = __ldg(vox + c);
+        if (kCompensated) {
+          const float y = dt * w - comp_acc[c];
+          const float tt = acc[c] + y;
+          comp_acc[c] = (tt - acc[c]) - y;
+          acc[c] = tt;
+        } else {
+          acc[c] = fmaf(dt, w, acc[c]);
+        }
+      }
+    }
+    if (last) break;
+    {  // t += dt, compensated
+      const float y = dt - t_comp;
+      const float tt = t + y;
+      t_comp = (tt - t) - y;
+      t = tt;
+    }
+    fx = fminf(fmaxf(fmaf(dt, vx, fx), 0.f), 1.f);
+    fy = fminf(fmaxf(fmaf(dt, vy, fy), 0.f), 1.f);
+    fz = fminf(fmaxf(fmaf(dt, vz, fz), 0.f), 1.f);
+    if (axis == 0) {
+      ix += stx;
+      fx = stx > 0 ? 0.f : 1.f;
+      if (ix < 0 || ix >= b.n[0]) break;
+    } else if (axis == 1) {
+      iy += sty;
+      fy = sty > 0 ? 0.f : 1.f;
+      if (iy < 0 || iy >= b.n[1]) break;
+    } else {
+      iz += stz;
+      fz = stz > 0 ? 0.f : 1.f;
+      if (iz < 0 || iz >= b.n[2]) break;
+    }
+  }
+}
+
+template <int kC, bool kCompensated, typename T>
+__device__ __forceinline__ void integrate(const Box& b, const T p0[3], const T p1[3], const float* vol, int C,
+                                          float* acc) {
+  const Setup<T> st = ray_setup<T>(b, p0, p1);
+  if (!st.hit) return;
+  Setup<float> s;
+  s.hit = true;
+  s.total = st.total;
+  for (int a = 0; a < 3; ++a) {
+    s.v[a] = st.v[a];
+    s.idx[a] = st.idx[a];
+    s.f[a] = st.f[a];
+  }
+  ray_walk<kC, kCompensated>(b, s, vol, C, acc);
+}
+
+// ---- generic segments ----------------------------------------------------------------------------------------
+template <int kC>
+__global__ void __launch_bounds__(kThreads) segments_kernel(Box b, const float* __restrict__ vol, int C,
+                                                            const float* __restrict__ starts,
+                                                            const float* __restrict__ ends, int64_t R,
+                                                            float* __restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (r >= R) return;
+  double p0[3], p1[3];
+  for (int a = 0; a < 3; ++a) {
+    p0[a] = starts[3 * r + a];
+    p1[a] = ends[3 * r + a];
+  }
+  float acc[kC > 0 ? kC : kMaxChannels];
+  const int nC = kC > 0 ? kC : C;
+  for (int c = 0; c < nC; ++c) acc[c] = 0.f;
+  integrate<kC, true, double>(b, p0, p1, vol, C, acc);
+  for (int c = 0; c < nC; ++c) out[(int64_t)c * R + r] = acc[c];
+}
+
+// ---- from a source point to points (explicit float64 points, or the centres of a point grid) ----------------
+template <int kC>
+__global__ void __launch_bounds__(kThreads) from_source_kernel(Box b, const float* __restrict__ vol, int C, double sx,
+                                                               double sy, double sz, const double* __restrict__ pts,
+                                                               const double* __restrict__ ax_x,
+                                                               const double* __restrict__ ax_y,
+                                                               const double* __restrict__ ax_z, int gc, int gs,
+                                                               int64_t P, float* __restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (r >= P) return;
+  double p1[3];
+  if (pts != nullptr) {
+    p1[0] = pts[3 * r];
+    p1[1] = pts[3 * r + 1];
+    p1[2] = pts[3 * r + 2];
+  } else {  // flat index (row * cols + col) * slices + slice of the point grid
+    const int64_t row = r / ((int64_t)gc * gs);
+    const int64_t rem = r - row * (int64_t)gc * gs;
+    const int64_t col = rem / gs;
+    p1[0] = ax_x[col];
+    p1[1] = ax_y[row];
+    p1[2] = ax_z[rem - col * gs];
+  }
+  const double p0[3] = {sx, sy, sz};
+  float acc[kC > 0 ? kC : kMaxChannels];
+  const int nC = kC > 0 ? kC : C;
+  for (int c = 0; c < nC; ++c) acc[c] = 0.f;
+  integrate<kC, true, double>(b, p0, p1, vol, C, acc);
+  for (int c = 0; c < nC; ++c) out[(int64_t)c * P + r] = acc[c];
+}
+
+// ---- downstream: from every voxel centre along each direction to the panel ----------------------------------
+struct Panel {
+  int curved;
+  double center[3], normal[3];  // flat panel: a point of the plane and its normal (toward the source)
+  double source[3], radius;     // curved panel: the cylinder about the vertical axis through the source
+};
+
+__device__ __forceinline__ float panel_distance(const Panel& p, const float r[3], const float w[3]) {
+  if (!p.curved) {
+    const float den = w[0] * (float)p.normal[0] + w[1] * (float)p.normal[1] + w[2] * (float)p.normal[2];
+    const float num = ((float)p.center[0] - r[0]) * (float)p.normal[0] + ((float)p.center[1] - r[1]) * (float)p.normal[1] +
+                      ((float)p.center[2] - r[2]) * (float)p.normal[2];
+    return num / den;
+  }
+  const float dx = r[0] - (float)p.source[0], dy = r[1] - (float)p.source[1];
+  const float a = w[0] * w[0] + w[1] * w[1];
+  const float bb = dx * w[0] + dy * w[1];
+  const float c = dx * dx + dy * dy - (float)(p.radius * p.radius);
+  const float disc = bb * bb - a * c;
+  const float root = sqrtf(fmaxf(disc, 0.f));
+  const bool pos = bb >= 0.f;
+  const float den = pos ? bb + root : (a > 0.f ? a : 1.f);
+  const float num = pos ? -c : root - bb;
+  if (!(a > 0.f) || !(disc >= 0.f) || den == 0.f) return INFINITY;
+  return num / den;
+}
+
+template <int kC>
+__global__ void __launch_bounds__(kThreads) downstream_kernel(Box b, const float* __restrict__ vol, int C,
+                                                              const float* __restrict__ omegas,
+                                                              const uint8_t* __restrict__ toward, Panel panel,
+                                                              float diagonal, int64_t V, float* __restrict__ out) {
+  const int64_t v = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int k = blockIdx.y;
+  if (v >= V) return;
+  const int nC = kC > 0 ? kC : C;
+  float* o = out + (int64_t)k * nC * V + v;
+  if (toward != nullptr && toward[k] == 0) {
+    for (int c = 0; c < nC; ++c) o[(int64_t)c * V] = INFINITY;
+    return;
+  }
+  const int64_t nzx = (int64_t)b.n[0] * b.n[2];
+  const int iy = (int)(v / nzx);
+  const int64_t rem = v - (int64_t)iy * nzx;
+  const int ix = (int)(rem / b.n[2]);
+  const int iz = (int)(rem - (int64_t)ix * b.n[2]);
+  const float r[3] = {(float)(b.lo[0] + b.delta[0] * (ix + 0.5)), (float)(b.lo[1] + b.delta[1] * (iy + 0.5)),
+                      (float)(b.lo[2] + b.delta[2] * (iz + 0.5))};
+  const float w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
+  float t = panel_distance(panel, r, w);
+  t = fminf(fmaxf(t, 0.f), diagonal);
+  const float p1[3] = {r[0] + t * w[0], r[1] + t * w[1], r[2] + t * w[2]};
+  float acc[kC > 0 ? kC : kMaxChannels];
+  for (int c = 0; c < nC; ++c) acc[c] = 0.f;
+  integrate<kC, false, float>(b, r, p1, vol, C, acc);
+  for (int c = 0; c < nC; ++c) o[(int64_t)c * V] = acc[c];
+}
+
+// ---- oblique: through every pixel centre along each direction, clipped to the box on both sides --------------
+template <int kC>
+__global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* __restrict__ vol, int C,
+                                                           int64_t field_stride, const float* __restrict__ omegas,
+                                                           const float* __restrict__ pixels, int64_t P, float cx,
+                                                           float cy, float cz, float half,
+                                                           float* __restrict__ out, int64_t os_k, int64_t os_c,
+                                                           int64_t os_r, int64_t os_col, int64_t cols) {
+  const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int k = blockIdx.y;
+  if (p >= P) return;
+  const float w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
+  const float px = pixels[3 * p], py = pixels[3 * p + 1], pz = pixels[3 * p + 2];
+  const float w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  const float cp = ((cx - px) * w[0] + (cy - py) * w[1] + (cz - pz) * w[2]) / w2;
+  const float h = half / sqrtf(w2);
+  const float a[3] = {px + (cp - h) * w[0], py + (cp - h) * w[1], pz + (cp - h) * w[2]};
+  const float e[3] = {px + (cp + h) * w[0], py + (cp + h) * w[1], pz + (cp + h) * w[2]};
+  const int nC = kC > 0 ? kC : C;
+  float acc[kC > 0 ? kC : kMaxChannels];
+  for (int c = 0; c < nC; ++c) acc[c] = 0.f;
+  integrate<kC, false, float>(b, a, e, vol + (int64_t)k * field_stride, C, acc);
+  const int64_t row = p / cols;
+  float* o = out + (int64_t)k * os_k + row * os_r + (p - row * cols) * os_col;
+  for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = acc[c];
+}
+
+int check_common(const float* vol, int64_t C, const double* box, const int64_t* dims, const void* out) {
+  CITRUS_REQUIRE(vol && box && dims && out, "ray tracing: null pointer argument");
+  CITRUS_REQUIRE(C >= 1 && C <= kMaxChannels, "ray tracing: %lld channels outside [1, %d]", (long long)C,
+                 kMaxChannels);
+  CITRUS_REQUIRE(dims[0] >= 1 && dims[1] >= 1 && dims[2] >= 1 && dims[0] * dims[1] * dims[2] < (1ll << 31),
+                 "ray tracing: bad grid dimensions");
+  CITRUS_REQUIRE(box[3] > 0 && box[4] > 0 && box[5] > 0, "ray tracing: voxel sizes must be positive");
+  if (C % 4 == 0) CITRUS_REQUIRE(((uintptr_t)vol % 16) == 0, "ray tracing: volume must be 16-byte aligned");
+  return CITRUS_OK;
+}
+
+#define CITRUS_CHANNEL_DISPATCH(C, KERNEL, GRID, STREAM, ...)                            \
+  switch (C) {                                                                            \
+    case 1: KERNEL<1><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;                \
+    case 2: KERNEL<2><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;                \
+    case 4: KERNEL<4><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;                \
+    case 8: KERNEL<8><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;                \
+    default: KERNEL<0><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;               \
+  }
+
+}  // namespace
+}  // namespace citrus
+
+using namespace citrus;
+
+extern "C" int citrus_line_integrals(const float* volume, int64_t channels, const double* box, const int64_t* dims,
+                                     const float* starts, const float* ends, int64_t num_rays, float* out,
+                                     void* stream) {
+  int status = check_common(volume, channels, box, dims, out);
+  if (status) return status;
+  CITRUS_REQUIRE(num_rays >= 0 && (num_rays == 0 || (starts && ends)), "citrus_line_integrals: bad rays");
+  if (num_rays == 0) return CITRUS_OK;
+  const Box b = make_box(box, dims);
+  const int C = (int)channels;
+  dim3 grid((unsigned)cdiv(num_rays, kThreads));
+  CITRUS_CHANNEL_DISPATCH(C, segments_kernel, grid, as_stream(stream), b, volume, C, starts, ends, num_rays, out)
+  return launch_status("citrus_line_integrals");
+}
+
+extern "C" int citrus_trace_from_source(const float* volume, int64_t channels, const double* box, const int64_t* dims,
+                                        const double* source, const double* points, const double* axis_x,
+                                        const double* axis_y, const double* axis_z, const int64_t* point_dims,
+                                        int64_t num_points, float* out, void* stream) {
+  int status = check_common(volume, channels, box, dims, out);
+  if (status) return status;
+  CITRUS_REQUIRE(source != nullptr, "citrus_trace_from_source: null source");
+  CITRUS_REQUIRE(points != nullptr || (axis_x && axis_y && axis_z && point_dims),
+                 "citrus_trace_from_source: give explicit points or the axes of a point grid");
+  int gc = 1, gs = 1;
+  if (points == nullptr) {
+    CITRUS_REQUIRE(point_dims[0] * point_dims[1] * point_dims[2] == num_points,
+                   "citrus_trace_from_source: point grid dims disagree with num_points");
+    gc = (int)point_dims[1];
+    gs = (int)point_dims[2];
+  }
+  if (num_points == 0) return CITRUS_OK;
+  const Box b = make_box(box, dims);
+  const int C = (int)channels;
+  dim3 grid((unsigned)cdiv(num_points, kThreads));
+  CITRUS_CHANNEL_DISPATCH(C, from_source_kernel, grid, as_stream(stream), b, volume, C, source[0], source[1],
+                          source[2], points, axis_x, axis_y, axis_z, gc, gs, num_points, out)
+  return launch_status("citrus_trace_from_source");
+}
+
+extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channels, const double* box,
+                                            const int64_t* dims, const float* omegas, const uint8_t* toward,
+                                            int64_t num_directions, const double* panel, double diagonal,
+                                            float* out, void* stream) {
+  int status = check_common(volume, channels, box, dims, out);
+  if (status) return status;
+  CITRUS_REQUIRE(omegas && panel, "citrus_downstream_cumulative: null directions or panel");
+  CITRUS_REQUIRE(num_directions >= 0 && num_directions <= 65535, "citrus_downstream_cumulative: bad direction count");
+  if (num_directions == 0) return CITRUS_OK;
+  Panel p;
+  p.curved = panel[0] != 0.0;
+  for (int a = 0; a < 3; ++a) {
+    p.center[a] = panel[1 + a];
+    p.normal[a] = panel[4 + a];
+    p.source[a] = panel[7 + a];
+  }
+  p.radius = panel[10];
+  const Box b = make_box(box, dims);
+  const int64_t V = dims[0] * dims[1] * dims[2];
+  const int C = (int)channels;
+  dim3 grid((unsigned)cdiv(V, kThreads), (unsigned)num_directions);
+  CITRUS_CHANNEL_DISPATCH(C, downstream_kernel, grid, as_stream(stream), b, volume, C, omegas, toward, p,
+                          (float)diagonal, V, out)
+  return launch_status("citrus_downstream_cumulative");
+}
+
+extern "C" int citrus_oblique_project(const float* field, int64_t channels, int64_t field_stride, const double* box,
+                                      const int64_t* dims, const float* omegas, int64_t num_directions,
+                                      const float* pixels, int64_t num_rows, int64_t num_cols, float* out,
+                                      int64_t os_k, int64_t os_c, int64_t os_r, int64_t os_col, void* stream) {
+  int status = check_common(field, channels, box, dims, out);
+  if (status) return status;
+  CITRUS_REQUIRE(omegas && pixels, "citrus_oblique_project: null directions or pixels");
+  CITRUS_REQUIRE(num_directions >= 0 && num_directions <= 65535 && num_rows >= 0 && num_cols >= 1,
+                 "citrus_oblique_project: bad sizes");
+  const int64_t num_pixels = num_rows * num_cols;
+  if (num_directions == 0 || num_pixels == 0) return CITRUS_OK;
+  const Box b = make_box(box, dims);
+  double ext[3], center[3], diag2 = 0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] = b.delta[a] * b.n[a];
+    center[a] = b.lo[a] + 0.5 * ext[a];
+    diag2 += ext[a] * ext[a];
+  }
+  const double half = 0.5 * sqrt(diag2) * (1 + 1e-6) + 1e-6;
+  const int C = (int)channels;
+  dim3 grid((unsigned)cdiv(num_pixels, kThreads), (unsigned)num_directions);
+  CITRUS_CHANNEL_DISPATCH(C, oblique_kernel, grid, as_stream(stream), b, field, C, field_stride, omegas, pixels,
+                          num_pixels, (float)center[0], (float)center[1], (float)center[2], (float)half, out, os_k,
+                          os_c, os_r, os_col, num_cols)
+  return launch_status("citrus_oblique_project");
+}

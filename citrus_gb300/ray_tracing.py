@@ -1,0 +1,215 @@
+"""The ``Projectors`` protocol and its sm_103a implementation (mirrors ``citrus/scatter_solver/ray_tracing.py``).
+
+``Projectors`` is the plugin point of the solver (``ScatterSolver(projectors=...)``): five ray operations for one view
+angle, batched over a leading channel axis (groups or materials), the field zero outside its grid box.
+``GB300Projectors`` runs each operation as one kernel of ``libcitrus_gb300.so`` (``csrc/raytrace.cu``); the volumes
+are handed to the kernels voxel-major ([V, C], every channel of a voxel in one load).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Optional, Protocol
+
+import numpy as np
+import torch
+from torch import Tensor
+
+from . import _lib
+from .geometry import ConeGeometry, Grid
+
+
+class Projectors(Protocol):
+    """The five ray operations of the scatter solver (reference ``ray_tracing.py:27-115``)."""
+
+    def upstream_cumulative(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float) -> Tensor: ...
+
+    def upstream_to_points(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                           points: Tensor) -> Tensor: ...
+
+    def primary_project(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float) -> Tensor: ...
+
+    def downstream_cumulative(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                              omegas: Tensor) -> Tensor: ...
+
+    def oblique_project(self, field: Tensor, grid: Grid, geometry: ConeGeometry, angle: float, omegas: Tensor,
+                        out: Optional[Tensor] = None) -> Tensor: ...
+
+
+class HostArgs:
+    """Keeps ctypes host arrays alive for one call and hands out their addresses."""
+
+    def __init__(self):
+        self._keep = []
+
+    def doubles(self, values) -> int:
+        arr = (ctypes.c_double * len(values))(*[float(v) for v in values])
+        self._keep.append(arr)
+        return ctypes.addressof(arr)
+
+    def int64s(self, values) -> int:
+        arr = (ctypes.c_int64 * len(values))(*[int(v) for v in values])
+        self._keep.append(arr)
+        return ctypes.addressof(arr)
+
+
+def _grid_args(host: HostArgs, grid: Grid) -> tuple:
+    return host.doubles(list(grid.lower_corner()) + list(grid.deltas)), host.int64s(
+        (grid.num_cols, grid.num_rows, grid.num_slices))
+
+
+def _voxel_major(volume: Tensor, grid: Grid) -> Tensor:
+    """[C, R, Cc, S] -> contiguous float32 [V, C]."""
+    if volume.dim() != 4 or tuple(volume.shape[1:]) != tuple(grid.shape):
+        raise ValueError(f"volume must be [C, {grid.shape}], got {tuple(volume.shape)}")
+    if volume.device.type != "cuda" or volume.dtype != torch.float32:
+        raise ValueError("volume must be a float32 CUDA tensor")
+    return volume.reshape(volume.shape[0], -1).t().contiguous()
+
+
+def panel_args(host: HostArgs, geometry: ConeGeometry, angle: float) -> int:
+    _, _, n_hat = geometry.panel_axes(angle)
+    return host.doubles([1.0 if geometry.use_curved_detector else 0.0, *geometry.panel_center(angle), *n_hat,
+                         *geometry.source_position(angle), float(geometry.source_detector_dist)])
+
+
+def subpixel_points(geometry: ConeGeometry, angle: float, n: int) -> np.ndarray:
+    """float64 [Rd, Cd, n, n, 3] centres of the n x n sub-pixels of every pixel (reference ``geometry.py:617-634``)."""
+    u, v = geometry.pixel_uv()
+    offsets = (2 * np.arange(n) + 1) / (2 * n) - 0.5
+    u_sub = u[None, :, None, None] + (offsets * geometry.delta_det_channel)[None, None, None, :]
+    v_sub = v[:, None, None, None] + (offsets * geometry.delta_det_row)[None, None, :, None]
+    return geometry.panel_points_np(u_sub, v_sub, angle)
+
+
+class GB300Projectors:
+    """Exact Siddon projectors on sm_103a (reference ``SiddonProjectors``, ``ray_tracing.py:291-620``).
+
+    Args:
+        samples_per_pixel_axis: default sub-rays per pixel axis of ``primary_project``.
+    """
+
+    def __init__(self, samples_per_pixel_axis: int = 1):
+        if samples_per_pixel_axis < 1:
+            raise ValueError("samples_per_pixel_axis must be >= 1")
+        self.samples_per_pixel_axis = int(samples_per_pixel_axis)
+
+    # ---- core ---------------------------------------------------------------------------------------------------
+    def line_integrals(self, volume: Tensor, starts: Tensor, ends: Tensor, grid: Grid) -> Tensor:
+        """[C, R] integrals along starts -> ends ([R, 3]) (reference ``ray_tracing.py:205-244``)."""
+        vol = _voxel_major(volume, grid)
+        starts = starts.to(device=volume.device, dtype=torch.float32).reshape(-1, 3).contiguous()
+        ends = ends.to(device=volume.device, dtype=torch.float32).reshape(-1, 3).contiguous()
+        if starts.shape != ends.shape:
+            raise ValueError("starts and ends must have the same number of rays")
+        out = torch.empty(volume.shape[0], starts.shape[0], device=volume.device, dtype=torch.float32)
+        host = HostArgs()
+        box, dims = _grid_args(host, grid)
+        _lib.call("citrus_line_integrals", vol.data_ptr(), volume.shape[0], box, dims, starts.data_ptr(),
+                  ends.data_ptr(), starts.shape[0], out.data_ptr(), _lib.stream_handle(volume.device))
+        return out
+
+    def _from_source(self, volume: Tensor, grid: Grid, source, points: Optional[Tensor] = None,
+                     point_grid: Optional[Grid] = None) -> Tensor:
+        vol = _voxel_major(volume, grid)
+        host = HostArgs()
+        box, dims = _grid_args(host, grid)
+        device = volume.device
+        C = volume.shape[0]
+        if points is not None:
+            pts = points.to(device=device, dtype=torch.float64).reshape(-1, 3).contiguous()
+            P = pts.shape[0]
+            out = torch.empty(C, P, device=device, dtype=torch.float32)
+            _lib.call("citrus_trace_from_source", vol.data_ptr(), C, box, dims, host.doubles(source), pts.data_ptr(),
+                      None, None, None, None, P, out.data_ptr(), _lib.stream_handle(device))
+            return out
+        ax = [a.to(device) for a in point_grid.axis_coordinates(dtype=torch.float64)]
+        P = point_grid.num_voxels
+        out = torch.empty(C, P, device=device, dtype=torch.float32)
+        _lib.call("citrus_trace_from_source", vol.data_ptr(), C, box, dims, host.doubles(source), None,
+                  ax[0].data_ptr(), ax[1].data_ptr(), ax[2].data_ptr(), host.int64s(point_grid.shape), P,
+                  out.data_ptr(), _lib.stream_handle(device))
+        return out
+
+    # ---- (a) upstream -------------------------------------------------------------------------------------------
+    def upstream_cumulative(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float) -> Tensor:
+        """[C, R, Cc, S] optical depth from the focal spot to every voxel centre."""
+        return self._from_source(mu, grid, geometry.source_position(angle), point_grid=grid).reshape(mu.shape)
+
+    def upstream_to_points(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                           points) -> Tensor:
+        """[C, N] from the focal spot to each point; ``points`` is a float [N, 3] tensor or a point ``Grid``."""
+        if isinstance(points, Grid):
+            return self._from_source(mu, grid, geometry.source_position(angle), point_grid=points)
+        return self._from_source(mu, grid, geometry.source_position(angle), points=points)
+
+    # ---- (b) primary --------------------------------------------------------------------------------------------
+    def primary_project(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                        samples_per_pixel_axis: Optional[int] = None) -> Tensor:
+        """[C, Rd, Cd] from the focal spot to every pixel centre, or ``-log(mean(exp(-tau)))`` over n x n sub-rays."""
+        n = self.samples_per_pixel_axis if samples_per_pixel_axis is None else int(samples_per_pixel_axis)
+        Rd, Cd = geometry.image_shape
+        if n == 1:
+            pts = torch.as_tensor(geometry.pixel_centers_np(angle).reshape(-1, 3))
+            return self._from_source(mu, grid, geometry.source_position(angle), points=pts).reshape(-1, Rd, Cd)
+        pts = torch.as_tensor(subpixel_points(geometry, angle, n).reshape(-1, 3))
+        tau = self._from_source(mu, grid, geometry.source_position(angle), points=pts).reshape(-1, Rd, Cd, n * n)
+        return -(torch.logsumexp(-tau, dim=-1) - math.log(n * n))
+
+    # ---- (c) downstream -----------------------------------------------------------------------------------------
+    def downstream_cumulative(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                              omegas: Tensor, out: Optional[Tensor] = None) -> Tensor:
+        """[K, C, R, Cc, S] from every voxel centre along each direction to the panel; +inf where the direction does
+        not face the panel (``omega . (-n_hat) <= 0``), 0 beyond the panel."""
+        vol = _voxel_major(mu, grid)
+        device = mu.device
+        omegas = omegas.to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
+        K = omegas.shape[0]
+        n_hat = torch.tensor(geometry.panel_axes(angle)[2], dtype=torch.float32, device=device)
+        toward = ((omegas * (-n_hat)).sum(-1) > 0).to(torch.uint8).contiguous()
+        if out is None:
+            out = torch.empty(K, *mu.shape, device=device, dtype=torch.float32)
+        host = HostArgs()
+        box, dims = _grid_args(host, grid)
+        diagonal = math.sqrt(sum(e * e for e in grid.extent)) * (1 + 1e-9) + 1e-9
+        _lib.call("citrus_downstream_cumulative", vol.data_ptr(), mu.shape[0], box, dims, omegas.data_ptr(),
+                  toward.data_ptr(), K, panel_args(host, geometry, angle), diagonal, out.data_ptr(),
+                  _lib.stream_handle(device))
+        return out
+
+    # ---- (d) oblique --------------------------------------------------------------------------------------------
+    def oblique_project(self, field: Tensor, grid: Grid, geometry: ConeGeometry, angle: float, omegas: Tensor,
+                        out: Optional[Tensor] = None, voxel_major: bool = False) -> Tensor:
+        """[K, C, Rd, Cd] line integrals through every pixel centre along each direction (``out`` any strides).
+
+        ``field`` is [K, C, R, Cc, S] or [C, R, Cc, S] (shared), or with ``voxel_major`` already [K, V, C]."""
+        device = field.device
+        omegas = omegas.to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
+        K = omegas.shape[0]
+        if voxel_major:
+            if field.dim() != 3 or field.shape[1] != grid.num_voxels or not field.is_contiguous():
+                raise ValueError("a voxel-major field must be contiguous [K, V, C]")
+            vol, C, stride = field, int(field.shape[2]), int(field.shape[1] * field.shape[2])
+        elif field.dim() == 4:
+            vol, C, stride = _voxel_major(field, grid), int(field.shape[0]), 0
+        elif field.dim() == 5 and field.shape[0] == K:
+            if tuple(field.shape[2:]) != tuple(grid.shape):
+                raise ValueError(f"field spatial shape {tuple(field.shape[2:])} != grid shape {grid.shape}")
+            C = int(field.shape[1])
+            vol = field.reshape(K, C, -1).permute(0, 2, 1).contiguous()
+            stride = grid.num_voxels * C
+        else:
+            raise ValueError(f"field must be [C, ...] or [K={K}, C, ...], got {tuple(field.shape)}")
+        Rd, Cd = geometry.image_shape
+        pixels = torch.as_tensor(geometry.pixel_centers_np(angle).reshape(-1, 3), dtype=torch.float32).to(device)
+        if out is None:
+            out = torch.empty(K, C, Rd, Cd, device=device, dtype=torch.float32)
+        if tuple(out.shape) != (K, C, Rd, Cd):
+            raise ValueError(f"out must be [K, C, Rd, Cd] = {(K, C, Rd, Cd)}, got {tuple(out.shape)}")
+        host = HostArgs()
+        box, dims = _grid_args(host, grid)
+        _lib.call("citrus_oblique_project", vol.data_ptr(), C, stride, box, dims, omegas.data_ptr(), K,
+                  pixels.data_ptr(), Rd, Cd, out.data_ptr(), out.stride(0), out.stride(1), out.stride(2),
+                  out.stride(3), _lib.stream_handle(device))
+        return out

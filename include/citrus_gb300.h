@@ -82,6 +82,45 @@ int citrus_scattering_moments(const float* transfer, const float* phi, float* ou
                               int64_t ps_g, int64_t ps_n, int64_t ps_k, int64_t ps_x, int64_t os_g, int64_t os_n,
                               int64_t os_k, int64_t os_x, void* stream);
 
+/* ------------------------------------------------------------------------------------------------------------------
+ * Siddon line integrals (exact for voxel-wise constant fields, zero outside the grid box).
+ * Replaces the Projectors protocol operations of citrus/scatter_solver/ray_tracing.py:27-115 and their Triton kernels
+ * in kernels/ray_tracing_kernels.py:215-1063.
+ *
+ * volume [V, C] voxel-major (the C channels of a voxel contiguous), V = dims[0] * dims[1] * dims[2] in the flat order
+ * (row * cols + col) * slices + slice. box (host) = lower corner (x, y, z) and voxel sizes (dx, dy, dz) in cm; dims
+ * (host) = (cols, rows, slices). Outputs are channel-major [C, rays] unless stated.
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* Generic segments starts[r] -> ends[r] ([R, 3] float32); replaces ray_tracing.line_integrals (ray_tracing.py:205-284). */
+int citrus_line_integrals(const float* volume, int64_t channels, const double* box, const int64_t* dims,
+                          const float* starts, const float* ends, int64_t num_rays, float* out, void* stream);
+
+/* From the focal spot (host double [3]) to points: explicit float64 points [P, 3] (device), or, with points NULL, the
+ * centres of a point grid given by its float64 axes x [cols], y [rows], z [slices] (device) and point_dims (host:
+ * rows, cols, slices). Replaces upstream_cumulative / upstream_to_points / primary_project (ray_tracing.py:405-498). */
+int citrus_trace_from_source(const float* volume, int64_t channels, const double* box, const int64_t* dims,
+                             const double* source, const double* points, const double* axis_x, const double* axis_y,
+                             const double* axis_z, const int64_t* point_dims, int64_t num_points, float* out,
+                             void* stream);
+
+/* From every voxel centre along each direction omegas[k] ([K, 3]) to the panel, out [K, C, V]; +inf for directions
+ * with toward[k] == 0 (uint8 [K], NULL: all toward), 0 beyond the panel. panel (host double [11]) = curved flag,
+ * flat-panel centre [3], normal [3], focal spot [3], cylinder radius; diagonal clamps the distance.
+ * Replaces downstream_cumulative (ray_tracing.py:501-545, ray_tracing_kernels.py:516-639). */
+int citrus_downstream_cumulative(const float* volume, int64_t channels, const double* box, const int64_t* dims,
+                                 const float* omegas, const uint8_t* toward, int64_t num_directions,
+                                 const double* panel, double diagonal, float* out, void* stream);
+
+/* Line through every pixel centre (pixels [rows, cols, 3]) along each direction, clipped to the box on both sides;
+ * field [K or 1, V, C] with field_stride elements between directions (0: shared); out element (k, c, row, col) at
+ * k * os_k + c * os_c + row * os_r + col * os_col (any layout, e.g. rows-outer [K, rows, C, cols]).
+ * Replaces oblique_project (ray_tracing.py:548-620). */
+int citrus_oblique_project(const float* field, int64_t channels, int64_t field_stride, const double* box,
+                           const int64_t* dims, const float* omegas, int64_t num_directions, const float* pixels,
+                           int64_t num_rows, int64_t num_cols, float* out, int64_t os_k, int64_t os_c, int64_t os_r,
+                           int64_t os_col, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,36 @@ def scatter_moments_small():
          T4=scatter_source_moments(transfer, phi4), T1=scatter_source_moments(transfer, phi1))
 
 
+@case
+def siddon_small():
+    """The five Siddon ray operations of the reference (PyTorch path, float64) on a small anisotropic grid, with a flat
+    and a curved panel."""
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+
+    g = torch.Generator().manual_seed(99)
+    grid = Grid((6, 7, 5), 1.1, 0.9, 1.3, recon_slice_offset=0.4)
+    vol = torch.rand(2, *grid.shape, generator=g, dtype=F64)
+    proj = SiddonProjectors(backend="torch")
+    arrays = dict(volume=vol)
+    omegas = torch.nn.functional.normalize(torch.randn(5, 3, generator=g, dtype=F64), dim=-1)
+    points = (torch.rand(20, 3, generator=g, dtype=F64) - 0.5) * 14.0
+    arrays.update(omegas=omegas, points=points)
+    for name, curved in (("flat", False), ("curved", True)):
+        geo = ConeGeometry(30.0, 45.0, 5, 7, 1.7, 1.9, det_row_offset=0.3, det_channel_offset=-0.2,
+                           use_curved_detector=curved)
+        angle = 0.7
+        arrays[f"{name}_upstream"] = proj.upstream_cumulative(vol, grid, geo, angle)
+        arrays[f"{name}_to_points"] = proj.upstream_to_points(vol, grid, geo, angle, points)
+        arrays[f"{name}_primary"] = proj.primary_project(vol, grid, geo, angle)
+        arrays[f"{name}_primary_n2"] = proj.primary_project(vol, grid, geo, angle, samples_per_pixel_axis=2)
+        down = proj.downstream_cumulative(vol, grid, geo, angle, omegas)
+        arrays[f"{name}_downstream"] = down
+        arrays[f"{name}_oblique"] = proj.oblique_project(vol, grid, geo, angle, omegas)
+        arrays[f"{name}_pixels"] = geo.pixel_centers(angle, dtype=F64)
+    save("siddon_small", **arrays)
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)
     for n in names:

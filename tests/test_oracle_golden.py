@@ -106,3 +106,48 @@ def test_oracle_slab_against_one_dimensional_solution(axis, sign):
             psi_in = a0 + a1
         np.testing.assert_allclose(psi[code, g, 0], along(p0[None].repeat(G, 0))[g], atol=1e-12)
         np.testing.assert_allclose(psi[code, g, 1 + axis], along(p1[None].repeat(G, 0))[g], atol=1e-12)
+
+
+def _siddon_setup():
+    from citrus_gb300.geometry import ConeGeometry
+    grid = Grid((6, 7, 5), 1.1, 0.9, 1.3, recon_slice_offset=0.4)
+    geos = {name: ConeGeometry(30.0, 45.0, 5, 7, 1.7, 1.9, det_row_offset=0.3, det_channel_offset=-0.2,
+                               use_curved_detector=curved) for name, curved in (("flat", False), ("curved", True))}
+    return grid, geos
+
+
+def finite_rel_err(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    assert np.array_equal(np.isinf(a), np.isinf(b))
+    m = np.isfinite(b)
+    return rel_err(a[m], b[m])
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_oracle_siddon_matches_reference(name):
+    from oracle import siddon
+    g = golden("siddon_small")
+    grid, geos = _siddon_setup()
+    geo, angle, vol = geos[name], 0.7, g["volume"]
+    np.testing.assert_allclose(geo.pixel_centers_np(angle), g[f"{name}_pixels"], atol=1e-12)
+    src = geo.source_position(angle)
+    assert rel_err(siddon.upstream_to_points(vol, grid, src, siddon.centers(grid).reshape(-1, 3)).reshape(vol.shape),
+                   g[f"{name}_upstream"]) < 1e-12
+    assert rel_err(siddon.upstream_to_points(vol, grid, src, g["points"]), g[f"{name}_to_points"]) < 1e-12
+    assert rel_err(siddon.primary_project(vol, grid, geo, angle), g[f"{name}_primary"]) < 1e-12
+    assert finite_rel_err(siddon.downstream_cumulative(vol, grid, geo, angle, g["omegas"]),
+                          g[f"{name}_downstream"]) < 1e-12
+    assert rel_err(siddon.oblique_project(vol, grid, geo, angle, g["omegas"]), g[f"{name}_oblique"]) < 1e-12
+
+
+def test_c_oracle_sweep_matches_numpy_oracle():
+    from oracle import native
+    rng = np.random.default_rng(4)
+    shape, G, Dc = (4, 5, 3), 3, 2
+    N = int(np.prod(shape))
+    c = rng.random((8, Dc, 3)) + 0.1
+    mu = rng.random((N, G)) + 0.2
+    src = rng.standard_normal((8, Dc, N, G, 4))
+    expected = osweep.sweep_chunk(shape, c, mu, src)
+    got = native.sweep_chunk(osweep.plan(shape), c, mu, src)
+    assert rel_err(got, expected) < 1e-14

@@ -1,0 +1,83 @@
+"""Parity of the sm_103a Siddon kernels with the reference fixtures and the float64 oracle."""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden, rel_err
+from citrus_gb300.geometry import ConeGeometry, Grid
+from citrus_gb300.ray_tracing import GB300Projectors
+from oracle import siddon
+from test_oracle_golden import _siddon_setup, finite_rel_err
+
+pytestmark = pytest.mark.gpu
+PATH_REL = 1e-6  # path lengths of the upstream and primary traces, relative to the largest
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_projectors_match_reference_fixture(cuda_device, name):
+    g = golden("siddon_small")
+    grid, geos = _siddon_setup()
+    geo, angle = geos[name], 0.7
+    vol = torch.as_tensor(g["volume"], dtype=torch.float32, device=cuda_device)
+    p = GB300Projectors()
+    assert rel_err(p.upstream_cumulative(vol, grid, geo, angle), g[f"{name}_upstream"]) < 2e-6
+    pts = torch.as_tensor(g["points"], device=cuda_device)
+    assert rel_err(p.upstream_to_points(vol, grid, geo, angle, pts), g[f"{name}_to_points"]) < 2e-6
+    assert rel_err(p.primary_project(vol, grid, geo, angle), g[f"{name}_primary"]) < 2e-6
+    assert rel_err(p.primary_project(vol, grid, geo, angle, samples_per_pixel_axis=2), g[f"{name}_primary_n2"]) < 2e-6
+    om = torch.as_tensor(g["omegas"], dtype=torch.float32, device=cuda_device)
+    down = p.downstream_cumulative(vol, grid, geo, angle, om).cpu().numpy()
+    assert finite_rel_err(down, g[f"{name}_downstream"]) < 1e-5
+    assert rel_err(p.oblique_project(vol, grid, geo, angle, om), g[f"{name}_oblique"]) < 1e-5
+    # a rows-outer output buffer, as the scatter image writes it
+    K, C = om.shape[0], vol.shape[0]
+    Rd, Cd = geo.image_shape
+    rows_outer = torch.empty(K, Rd, C, Cd, device=cuda_device)
+    p.oblique_project(vol, grid, geo, angle, om, out=rows_outer.permute(0, 2, 1, 3))
+    assert rel_err(rows_outer.permute(0, 2, 1, 3), g[f"{name}_oblique"]) < 1e-5
+
+
+def _cylinder_phantom(grid):
+    c = siddon.centers(grid)
+    r = np.hypot(c[..., 0], c[..., 1])
+    water = (r < 7.0).astype(np.float64)
+    bone = (np.hypot(c[..., 0] - 3.0, c[..., 1] + 1.5) < 1.0).astype(np.float64)
+    return np.stack([water * (1 - bone) + 0.0012 * (1 - water), 1.85 * bone])
+
+
+@pytest.mark.parametrize("curved", [False, True])
+def test_path_lengths_within_one_part_per_million(cuda_device, curved):
+    """The 32^3 water-cylinder phantom: upstream traces to every voxel centre and primary traces to every pixel of a
+    64 x 64 panel against the float64 oracle, within 1e-6 of the largest path."""
+    grid = Grid((32, 32, 32), 0.5)
+    geo = ConeGeometry(100.0, 150.0, 64, 64, 0.4, 0.4, use_curved_detector=curved)
+    rho = _cylinder_phantom(grid)
+    vol = torch.as_tensor(rho, dtype=torch.float32, device=cuda_device)
+    p = GB300Projectors()
+    for angle in (0.0, 0.37, 2.2):
+        up = p.upstream_cumulative(vol, grid, geo, angle)
+        ref = siddon.upstream_to_points(rho, grid, geo.source_position(angle), siddon.centers(grid).reshape(-1, 3))
+        assert rel_err(up.reshape(2, -1), ref) < PATH_REL
+        prim = p.primary_project(vol, grid, geo, angle)
+        assert rel_err(prim, siddon.primary_project(rho, grid, geo, angle)) < PATH_REL
+
+
+def test_random_segments_and_edge_cases(cuda_device):
+    rng = np.random.default_rng(3)
+    grid = Grid((5, 9, 4), 0.8, 1.2, 0.7)
+    vol = rng.random((3, *grid.shape))
+    ext = np.asarray(grid.extent)
+    starts = (rng.random((500, 3)) - 0.5) * ext * 3
+    ends = (rng.random((500, 3)) - 0.5) * ext * 3
+    # axis-aligned rays along grid planes, zero-length rays, rays missing the box and rays inside one voxel
+    starts[:4] = [[-10, 0.0, 0.1], [0.4, -10, 0.35], [0.2, 0.3, 0.0], [50, 50, 50]]
+    ends[:4] = [[10, 0.0, 0.1], [0.4, 10, 0.35], [0.2, 0.3, 0.0], [60, 50, 50]]
+    starts[4], ends[4] = [0.1, 0.1, 0.1], [0.2, 0.15, 0.12]
+    got = GB300Projectors().line_integrals(torch.as_tensor(vol, dtype=torch.float32, device=cuda_device),
+                                           torch.as_tensor(starts), torch.as_tensor(ends), grid)
+    assert rel_err(got, siddon.line_integrals(vol, starts, ends, grid)) < 1e-5
