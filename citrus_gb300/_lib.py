@@ -31,6 +31,18 @@ SIGNATURES = {
     "citrus_trace_from_source": [P, I64, P, P, P, P, P, P, P, P, I64, P, P],
     "citrus_downstream_cumulative": [P, I64, P, P, P, P, I64, P, F64, P, P],
     "citrus_oblique_project": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P],
+    "citrus_group_transmission": [P, I64, I64, P, P, P, I64, I64, P, P, P, P, P],
+    "citrus_source_weight": [P, P, P, P, P, P, I64, I32, P, P],
+    "citrus_first_collision_source": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, I64, P, P],
+    "citrus_first_collision_moments": [P, I64, P, I64, P, P, I64, P, P, I64, F64, F64, P, I64, P, P, P, I64, P],
+    "citrus_first_collision_correction": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, P, I64, P, P, P, P, P],
+    "citrus_attenuated_emission": [P, I64, P, I64, P, P, I64, P, P, P, I64, F64, F64, P, I64, P, P, P, P, P, P, P,
+                                   I64, P, P],
+    "citrus_box_blur": [P, P, I64, I64, I64, I64, I64, I64, I64, I64, I64, P, P, P, I32, F64, F64, P],
+    "citrus_box_matrix": [P, I64, I64, P, P],
+    "citrus_weighted_group_sum": [P, P, I64, I64, I64, I64, I64, P, P],
+    "citrus_sum_directions": [P, I64, I64, I64, P, I32, P],
+    "citrus_weighted_direction_sum": [P, I64, I64, I64, I64, I64, I64, I64, I64, P, I64, I64, P, I32, P],
 }
 
 _LIBRARY: Optional[ctypes.CDLL] = None

@@ -1,0 +1,308 @@
+"""Collapsed-cone scatter image and primary image of one view (mirrors ``citrus/scatter_solver/scatter_image.py``).
+
+Per chunk of panel-facing cone directions the image runs: the downstream optical depth of the transport cells
+(``Projectors.downstream_cumulative``), the multiple-collision source ``Y_k @ T`` (``kernels.small_k_gemm``), the
+attenuated total emission at the quadrature points with its height sums (``citrus_attenuated_emission``; with
+direction-only signal weights the groups are summed there), the projection through every pixel centre
+(``Projectors.oblique_project``, written rows-outer), the finite-cone footprint blur (``citrus_box_blur``, widths from
+the height sums on the device) and the weighted accumulation (``citrus_weighted_group_sum``,
+``citrus_sum_directions``, ``citrus_weighted_direction_sum``).
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import torch
+from torch import Tensor
+
+from . import _lib, kernels
+from .cross_sections import MultigroupLibrary
+from .geometry import ConeGeometry, Grid
+from .quadrature import Quadrature, hemisphere_quadrature, real_spherical_harmonics, to_device
+from .ray_tracing import HostArgs
+from .responses import DetectorResponse, GridResponse, SourceModel, detector_angle
+from .uncollided import _FCArgs, group_transmission, present_materials
+
+IMAGE_CHUNK_MAX_DIRECTIONS = 32
+IMAGE_CHUNK_BUDGET_BYTES = 256 * 2 ** 20
+
+
+def covering_polar_angle(grid: Grid, geometry: ConeGeometry, angle: float, margin: float = 1e-6) -> float:
+    """Smallest cone half-angle about the inward panel normal containing every box-to-panel direction
+    (reference ``scatter_image.py:59-95``)."""
+    lower, extent = grid.lower_corner(), grid.extent
+    corners = np.array([[lower[0] + i * extent[0], lower[1] + j * extent[1], lower[2] + k * extent[2]]
+                        for i in (0, 1) for j in (0, 1) for k in (0, 1)])
+    u_hat, v_hat, n_hat = (np.asarray(a) for a in geometry.panel_axes(angle))
+    pc = np.asarray(geometry.panel_center(angle))
+    half_u, half_v = geometry.panel_half_extent()
+    cu, cv = -geometry.det_channel_offset, -geometry.det_row_offset
+    if geometry.use_curved_detector:
+        eu = cu + np.linspace(-half_u, half_u, 4 * geometry.num_det_channels + 1)
+        ev = cv + np.array([-half_v, half_v])
+        panel = geometry.panel_points_np(eu[:, None], ev[None, :], angle).reshape(-1, 3)
+    else:
+        panel = np.stack([pc + (cu + su * half_u) * u_hat + (cv + sv * half_v) * v_hat
+                          for su in (-1, 1) for sv in (-1, 1)])
+    d = panel[:, None, :] - corners[None, :, :]
+    normal = (d * (-n_hat)).sum(-1)
+    if np.any(normal <= 0):
+        return math.pi / 2
+    lateral = np.linalg.norm(d - normal[..., None] * (-n_hat), axis=-1)
+    return float(min(math.pi / 2, float(np.arctan2(lateral, normal).max()) + margin))
+
+
+def panel_direction_set(geometry: ConeGeometry, angle: float, counts: tuple, max_polar_angle=math.pi / 2) -> Quadrature:
+    """Cone product set about the inward panel normal with gnomonic cell widths (reference ``:98-130``)."""
+    if isinstance(max_polar_angle, Grid):
+        max_polar_angle = covering_polar_angle(max_polar_angle, geometry, angle)
+    u_hat, v_hat, n_hat = geometry.panel_axes(angle)
+    return hemisphere_quadrature([-c for c in n_hat], int(counts[0]), int(counts[1]), max_polar_angle,
+                                 tangent_axes=(u_hat, v_hat))
+
+
+@dataclass(eq=False)
+class DirectionSetContext:
+    """The emission-independent part of one view's image (reference ``scatter_image.py:137-405``, for detector
+    responses that depend on energy and incidence and grid responses that do not depend on the angles).
+
+    Device tensors (float32): omega [K, 3], weight [K], cos_theta0 [K], cell_width [K, 2]; ``signal_group_weight``
+    [K, G] when the signal weights are the same at every pixel (flat panel), else ``signal_channel_weight``
+    [K, G, Cd] (curved panel: incidence per channel); ``planar_weight`` [K, 1 | Cd].
+    """
+
+    quadrature: Quadrature
+    geometry: ConeGeometry
+    angle: float
+    group_energy: np.ndarray
+    omega: Tensor
+    weight: Tensor
+    cos_theta0: Tensor
+    cell_width: Tensor
+    signal_group_weight: Optional[Tensor]
+    signal_channel_weight: Optional[Tensor]
+    planar_weight: Tensor
+    chunk_bounds: tuple
+    image_shape: tuple
+    _cache: dict = field(default_factory=dict, repr=False)
+
+    @property
+    def num_directions(self) -> int:
+        return int(self.omega.shape[0])
+
+    @property
+    def device(self) -> torch.device:
+        return self.omega.device
+
+    def harmonics(self, L: int) -> Tensor:
+        key = ("Y", int(L))
+        if key not in self._cache:
+            self._cache[key] = to_device(real_spherical_harmonics(L, self._omega64), self.device)
+        return self._cache[key]
+
+    def footprint(self, grid: Grid) -> tuple:
+        """(heights [V] of the point centres above the panel, height of the box centre) (reference ``:1033-1077``)."""
+        key = ("footprint", grid)
+        if key not in self._cache:
+            _, _, n_hat = self.geometry.panel_axes(self.angle)
+            pc = np.asarray(self.geometry.panel_center(self.angle))
+            x, y, z = (a.double().numpy() for a in grid.axis_coordinates(dtype=torch.float64))
+            h = ((x[None, :, None] - pc[0]) * n_hat[0] + (y[:, None, None] - pc[1]) * n_hat[1]
+                 + (z[None, None, :] - pc[2]) * n_hat[2])
+            lower, extent = grid.lower_corner(), grid.extent
+            corner = [sum((lower[a] + c[a] * extent[a] - pc[a]) * n_hat[a] for a in range(3))
+                      for c in [(i, j, k) for i in (0, 1) for j in (0, 1) for k in (0, 1)]]
+            self._cache[key] = (to_device(np.broadcast_to(h, grid.shape).reshape(-1), self.device),
+                                0.5 * (min(corner) + max(corner)))
+        return self._cache[key]
+
+
+def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle: float, detector: DetectorResponse,
+                           grid_response: GridResponse, library: MultigroupLibrary, device,
+                           chunk: int = 8) -> DirectionSetContext:
+    """Keep the panel-facing directions and precompute their weights (reference ``scatter_image.py:542-696``)."""
+    energy = np.asarray(library.group_energy, dtype=np.float64)
+    G = energy.size
+    _, _, n_hat = geometry.panel_axes(angle)
+    n_hat = np.asarray(n_hat)
+    # the selection in the images' float32, as the projectors see a grazing direction
+    cos32 = (quadrature.omega.astype(np.float32) * (-n_hat).astype(np.float32)).sum(-1)
+    kept = np.nonzero(cos32 > 0)[0]
+    omega = quadrature.omega[kept]
+    weight = quadrature.weight[kept]
+    cos64 = (omega * (-n_hat)).sum(-1)
+    K = kept.size
+    Rd, Cd = geometry.image_shape
+    grid_t = grid_response.at_energy(energy)                                    # [G]
+    if geometry.use_curved_detector:
+        pixels = geometry.pixel_centers_np(angle)
+        normals = geometry.local_normals_np(pixels[0], angle)                   # [Cd, 3]
+        cos_channel = np.clip(omega @ (-normals).T, 0.0, 1.0)                   # [K, Cd]
+        planar = weight[:, None] * cos_channel
+        channel = planar[None] * detector.at(energy, np.arccos(cos_channel)) * grid_t[:, None, None]  # [G, K, Cd]
+        signal_group, signal_channel = None, to_device(channel.transpose(1, 0, 2), device)
+        planar_weight = to_device(planar, device)
+    else:
+        response = detector.at(energy, detector_angle(omega, geometry, angle)) if K else np.zeros((G, 0))
+        direction = (weight * cos64)[None] * response * grid_t[:, None]          # [G, K]
+        signal_group, signal_channel = to_device(direction.T, device), None
+        planar_weight = to_device((weight * cos64)[:, None], device)
+    chunk = max(1, int(chunk))
+    ctx = DirectionSetContext(
+        quadrature=quadrature, geometry=geometry, angle=float(angle), group_energy=energy, omega=to_device(omega, device),
+        weight=to_device(weight, device), cos_theta0=to_device(cos64, device),
+        cell_width=to_device(quadrature.cell_width[kept], device), signal_group_weight=signal_group,
+        signal_channel_weight=signal_channel, planar_weight=planar_weight,
+        chunk_bounds=tuple((s, min(s + chunk, K)) for s in range(0, K, chunk)), image_shape=(Rd, Cd))
+    ctx._omega64 = omega
+    return ctx
+
+
+def _blur(src: Tensor, dst: Tensor, lines: int, length: int, strides_in: tuple, strides_out: tuple, k: int,
+          height_sums: Tensor, cell_width: Tensor, axis: int, pitch: float, center_height: float) -> None:
+    _lib.call("citrus_box_blur", src.data_ptr(), dst.data_ptr(), k, lines, length, *strides_in, *strides_out, None,
+              height_sums.data_ptr(), cell_width.data_ptr(), axis, float(pitch), float(center_height),
+              _lib.stream_handle(src.device))
+
+
+def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, phi_uncollided: Tensor,
+                           grid_quadrature: Grid, q: int, scatter_source_moments: Tensor, L: int,
+                           geometry: ConeGeometry, angle: float, mu_t_coarse: Tensor, projectors,
+                           context: DirectionSetContext, grid_coarse: Optional[Grid] = None,
+                           signal_only: bool = False, footprint: bool = True) -> dict:
+    """Total scatter image of one view, first order plus multiple collision (reference ``scatter_image.py:1141-1323``).
+
+    Returns ``{"signal": [Rd, Cd]}`` with ``signal_only``, else fluence, planar_fluence and signal_per_group
+    [G, Rd, Cd] and signal [Rd, Cd].
+    """
+    device = phi_uncollided.device
+    f = int(q)
+    grid_coarse = grid_quadrature.coarsen(f) if grid_coarse is None else grid_coarse
+    G = int(mu_t_coarse.shape[0])
+    NC = grid_coarse.num_voxels
+    V = grid_quadrature.num_voxels
+    if scatter_source_moments.dim() == 6:
+        scatter_source_moments = scatter_source_moments[:, :, 0]
+    N_sh = (L + 1) ** 2
+    if tuple(scatter_source_moments.shape) != (G, N_sh, *grid_coarse.shape):
+        raise ValueError(f"scatter_source_moments must be [{G}, {N_sh}, {grid_coarse.shape}]")
+    # [N_sh, G * cells]: a view of moment-major storage, else one copy
+    T = scatter_source_moments.transpose(0, 1).reshape(N_sh, G * NC).contiguous()
+    Y = context.harmonics(L)
+    Rd, Cd = context.image_shape
+    heights, center_height = context.footprint(grid_quadrature)
+    fc = _FCArgs(library, rho_quadrature, phi_uncollided, grid_quadrature, geometry, angle)
+    host = HostArgs()
+    deltas = host.doubles(grid_quadrature.deltas)
+    mu = mu_t_coarse.to(torch.float32).reshape(G, NC).contiguous()
+    flat_signal = signal_only and context.signal_group_weight is not None
+    C = 1 if flat_signal else G
+    acc = torch.zeros(Rd, Cd, device=device) if signal_only else torch.zeros(3, G, Rd, Cd, device=device)
+    K_max = max((e - s for s, e in context.chunk_bounds), default=0)
+    nblocks = -(-V // 32)
+    partial = torch.empty(K_max * nblocks * 2, device=device)
+    sums = torch.empty(K_max, 2, device=device)
+    stream = _lib.stream_handle(device)
+    for s, e in context.chunk_bounds:
+        k = e - s
+        dirs = context.omega[s:e]
+        tau = projectors.downstream_cumulative(mu_t_coarse, grid_coarse, geometry, angle, dirs)  # [k, G, cells]
+        multiple = torch.empty(k, G * NC, device=device)
+        kernels.small_k_gemm(Y[s:e].contiguous(), T, multiple)
+        emission = torch.empty(k, V, C, device=device)
+        _lib.call("citrus_attenuated_emission", *fc.common(), f, deltas, fc.focal, fc.table.data_ptr(), fc.num_eta,
+                  fc.eta_lo, fc.eta_hi, dirs.data_ptr(), k, tau.data_ptr(), mu.data_ptr(), multiple.data_ptr(),
+                  heights.data_ptr(), context.signal_group_weight[s:e].contiguous().data_ptr() if flat_signal else None,
+                  emission.data_ptr(), partial.data_ptr(), partial.numel(), sums.data_ptr(), stream)
+        del tau, multiple
+        rows_outer = torch.empty(k, Rd, C, Cd, device=device)
+        projectors.oblique_project(emission, grid_quadrature, geometry, angle, dirs,
+                                   out=rows_outer.permute(0, 2, 1, 3), voxel_major=True)
+        del emission
+        cw = context.cell_width[s:e].contiguous()
+        if not footprint:
+            blurred = rows_outer
+        else:
+            blurred = torch.empty_like(rows_outer)  # channels: lines (row, channel-group) of Cd contiguous pixels
+            _blur(rows_outer, blurred, Rd * C, Cd, (Rd * C * Cd, Cd, 1), (Rd * C * Cd, Cd, 1), k, sums, cw, 0,
+                  geometry.delta_det_channel, center_height)
+        if signal_only and not flat_signal:
+            single = torch.empty(k, Rd, Cd, device=device)
+            _lib.call("citrus_weighted_group_sum", blurred.data_ptr(),
+                      context.signal_channel_weight[s:e].contiguous().data_ptr(), k, Rd, G, Cd, Cd,
+                      single.data_ptr(), stream)
+            image, C_img = single, 1
+        else:
+            image, C_img = blurred, C
+        if footprint:  # rows: lines (channel-group, channel) of Rd pixels with stride C_img * Cd
+            rows = torch.empty_like(image)
+            _blur(image, rows, C_img * Cd, Rd, (Rd * C_img * Cd, 1, C_img * Cd), (Rd * C_img * Cd, 1, C_img * Cd), k,
+                  sums, cw, 1, geometry.delta_det_row, center_height)
+            image = rows
+        if signal_only:
+            _lib.call("citrus_sum_directions", image.data_ptr(), k, Rd * Cd, Rd * Cd, acc.data_ptr(), 1, stream)
+            continue
+        img = image.view(k, Rd, G, Cd)  # rows-outer [k, Rd, G, Cd] seen as [k, G, Rd, Cd] through strides
+        strides = (Rd * G * Cd, Cd, G * Cd, 1)
+        ones = context.weight[s:e].reshape(k, 1, 1, 1).expand(k, G, 1, 1).contiguous()
+        planar = context.planar_weight[s:e]
+        planar = planar.reshape(k, 1, 1, -1).expand(k, G, 1, planar.shape[-1]).contiguous()
+        signal = (context.signal_group_weight[s:e].reshape(k, G, 1, 1).contiguous()
+                  if context.signal_group_weight is not None
+                  else context.signal_channel_weight[s:e].reshape(k, G, 1, Cd).contiguous())
+        for j, w in enumerate((ones, planar, signal)):
+            _lib.call("citrus_weighted_direction_sum", img.data_ptr(), k, G, Rd, Cd, *strides, w.data_ptr(), 1,
+                      w.shape[-1], acc[j].data_ptr(), 1, stream)
+    if signal_only:
+        return {"signal": acc}
+    return {"fluence": acc[0], "planar_fluence": acc[1], "signal_per_group": acc[2], "signal": acc[2].sum(0)}
+
+
+# ---- primary ---------------------------------------------------------------------------------------------------------
+
+def primary_path_lengths(projectors, rho: Tensor, grid: Grid, geometry: ConeGeometry, angle: float) -> Tensor:
+    """[M', Rd, Cd] density line integrals to the pixel centres (reference ``scatter_image.py:1368-1392``)."""
+    return projectors.primary_project(rho, grid, geometry, angle)
+
+
+def primary_from_path_lengths(library: MultigroupLibrary, path: Tensor, materials, geometry: ConeGeometry,
+                              angle: float, source: SourceModel, detector: DetectorResponse,
+                              grid_response: GridResponse) -> dict:
+    """Primary image from per-material line integrals, exact in energy (reference ``scatter_image.py:1419-1471``)."""
+    device = path.device
+    T = group_transmission(library, path, materials)                          # [G, Rd, Cd]
+    pixels = geometry.pixel_centers_np(angle)
+    d = pixels - np.asarray(geometry.source_position(angle))
+    dist2 = (d * d).sum(-1)
+    b = source.angular_weight_np(d, geometry, angle)
+    omega_p = d / np.sqrt(dist2)[..., None]
+    energy = library.group_energy
+    theta0 = detector_angle(omega_p, geometry, angle, pixels)
+    fluence_factor = to_device(b / dist2, device)
+    planar_factor = to_device(b / dist2 * np.cos(theta0), device)
+    signal_factor = to_device((b / dist2 * np.cos(theta0))[None] * detector.at(energy, theta0)
+                              * grid_response.at_energy(energy)[:, None, None], device)
+    fluence = T * fluence_factor
+    signal_per_group = T * signal_factor
+    return {"fluence": fluence, "planar_fluence": T * planar_factor, "signal_per_group": signal_per_group,
+            "signal": signal_per_group.sum(0)}
+
+
+def primary_image(library: MultigroupLibrary, rho: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                  source: SourceModel, projectors, detector: DetectorResponse, grid_response: GridResponse) -> dict:
+    """Primary image of one view from the density maps (reference ``scatter_image.py:1474-1506``)."""
+    present = present_materials(rho)
+    traced = rho if present is None else rho[present]
+    path = primary_path_lengths(projectors, traced.contiguous(), grid, geometry, angle)
+    return primary_from_path_lengths(library, path, present, geometry, angle, source, detector, grid_response)
+
+
+def scatter_fraction(scatter_signal: Tensor, primary_signal: Tensor) -> Tensor:
+    """S / (P + S), 0 where P + S = 0 (reference ``scatter_image.py:1509-1521``)."""
+    den = primary_signal + scatter_signal
+    return torch.where(den > 0, scatter_signal / torch.where(den > 0, den, torch.ones_like(den)),
+                       torch.zeros_like(den))

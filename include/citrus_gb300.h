@@ -121,6 +121,103 @@ int citrus_oblique_project(const float* field, int64_t channels, int64_t field_s
                            int64_t num_rows, int64_t num_cols, float* out, int64_t os_k, int64_t os_c, int64_t os_r,
                            int64_t os_col, void* stream);
 
+/* ------------------------------------------------------------------------------------------------------------------
+ * Uncollided fluence and first-collision source.
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* T[g, p] = factor[p] * sum_{e: fine_group[e] = g} fine_weight[e] exp(-sum_m fine_mu[m, e] path[m, p]
+ *           - filter_mu[e] filter_path[p]); path [M', P], fine_mu [M', E]; filter and factor optional (NULL).
+ * Replaces cross_sections.group_transmission (cross_sections.py:797-883, transmission_kernels.py:187-275). */
+int citrus_group_transmission(const float* path, int64_t num_materials, int64_t num_points, const float* fine_mu,
+                              const float* fine_weight, const int32_t* fine_group, int64_t num_fine,
+                              int64_t num_groups, const float* filter_path, const float* filter_mu,
+                              const float* factor, float* out, void* stream);
+
+/* Focal-spot weight b(Omega) (1 where the ray from the focal spot meets the collimated field), divided by |r - r0|^2
+ * when asked, at explicit float64 points [P, 3] or at the centres of a point grid (float64 axes, point_dims host).
+ * field (host double [23]) = curved flag, focal spot [3], panel centre [3], u_hat [3], v_hat [3], n_hat [3],
+ * source-detector distance, channel and row offsets, panel half widths (u, v), field margins (u, v).
+ * Replaces SourceModel.angular_weight (source.py:289-382) and the 1 / |r - r0|^2 of uncollided.py:193-197. */
+int citrus_source_weight(const double* field, const double* points, const double* axis_x, const double* axis_y,
+                         const double* axis_z, const int64_t* point_dims, int64_t num_points,
+                         int32_t divide_by_distance_squared, float* out, void* stream);
+
+/* Shared arguments of the first-collision kernels: rho [M, V] densities on the point grid, phi [G, V] uncollided
+ * fluence, axes = float32 point coordinates x [cols], y [rows], z [slices] back to back, point_dims (host) = rows,
+ * cols, slices, focal_spot (host double [3]), table [M, N_eta, G_out, G_in] per-steradian transfer (zero for
+ * G_in > G_out) on the uniform cosine nodes eta_lo .. eta_hi, omegas [K, 3].
+ *
+ * S_FC [K, G, V] at the points (uncollided.py:200-308, uncollided_kernels.py:488-550). */
+int citrus_first_collision_source(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
+                                  const float* axes, const int64_t* point_dims, const double* focal_spot,
+                                  const float* table, int64_t num_eta, double eta_lo, double eta_hi,
+                                  const float* omegas, int64_t num_directions, float* out, void* stream);
+
+/* LD moments (mean, x, y, z slopes) of the corrected source scale (1 + beta cos) S_FC over the points_per_cell^3
+ * points of each transport cell, cell-major into out [K, NC, G, 4] with out_direction_stride floats between
+ * directions (the sweep's store). Replaces first_collision_moments_at_directions (uncollided.py:464-511,
+ * uncollided_kernels.py:552-634). */
+int citrus_first_collision_moments(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
+                                   const float* axes, const int64_t* point_dims, int64_t points_per_cell,
+                                   const double* focal_spot, const float* table, int64_t num_eta, double eta_lo,
+                                   double eta_hi, const float* omegas, int64_t num_directions, const float* scale,
+                                   const float* beta, float* out, int64_t out_direction_stride, void* stream);
+
+/* Sampling correction: quadrature sums I0, I1, I2 over the K sweep directions (weights [K]) and exact moments E0, E1
+ * from moments [M, 2, G_out, G_in] (Legendre l = 0, 1), optionally stored in sums [5, G, V], and the float64 factors
+ * scale, beta [G, V] (uncollided.py:357-461, 538-636, uncollided_kernels.py:636-710). */
+int citrus_first_collision_correction(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
+                                      const float* axes, const int64_t* point_dims, const double* focal_spot,
+                                      const float* table, int64_t num_eta, double eta_lo, double eta_hi,
+                                      const float* omegas, const float* weights, int64_t num_directions,
+                                      const float* moments, float* sums, float* scale, float* beta, void* stream);
+
+/* Attenuated total emission of the collapsed-cone image: (S_FC + multiple[k, g, cell]) exp(-max(0, tau[k, g, cell]
+ * - mu[g, cell] omega . (r - r_cell))) written voxel-major out [K, V, G], or with signal_weight [K, G] its weighted
+ * group sum [K, V]; height_sums [K, 2] = (sum e, sum e h) with the panel heights h [V] (NULL: 0), summed in a fixed
+ * order through partial [K, ceil(V / 32), 2] (device scratch of partial_capacity floats).
+ * Replaces attenuated_emission (uncollided_kernels.py:712-795, 1138-1205) and supervoxel_subpoint_emission
+ * (scatter_image.py:829-874). */
+int citrus_attenuated_emission(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
+                               const float* axes, const int64_t* point_dims, int64_t points_per_cell,
+                               const double* point_deltas, const double* focal_spot, const float* table,
+                               int64_t num_eta, double eta_lo, double eta_hi, const float* omegas,
+                               int64_t num_directions, const float* tau, const float* mu, const float* multiple,
+                               const float* heights, const float* signal_weight, float* out, float* partial,
+                               int64_t partial_capacity, float* height_sums, void* stream);
+
+/* ------------------------------------------------------------------------------------------------------------------
+ * Finite-cone footprint and accumulation of the collapsed-cone image (scatter_image.py:897-1135, 1234-1323).
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* Box blur along one axis of length N: out[k, line, c] = sum_j B_k[c, j] in[k, line, j] with the overlap weights of
+ * scatter_image.box_matrix (scatter_image.py:952-1007), element strides for directions, lines and pixels. The width
+ * in pixels is widths[k], or, with widths NULL, hbar_k cell_width[k, axis] / pitch with the mean height
+ * hbar_k = height_sums[k, 1] / height_sums[k, 0] (center_height where the sum vanishes) (scatter_image.py:1079-1135). */
+int citrus_box_blur(const float* in, float* out, int64_t num_directions, int64_t lines, int64_t length, int64_t is_k,
+                    int64_t is_l, int64_t is_p, int64_t os_k, int64_t os_l, int64_t os_p, const float* widths,
+                    const float* height_sums, const float* cell_width, int32_t axis, double pitch,
+                    double center_height, void* stream);
+
+/* Dense overlap matrices [K, N, N] of the footprint filter (scatter_image.box_matrix, scatter_image.py:952-1007). */
+int citrus_box_matrix(const float* widths, int64_t num_directions, int64_t length, float* out, void* stream);
+
+/* out[k, r, c] = sum_g image[k, r, g, c] weights[k, g, c] of rows-outer images (weight_cols 1: one weight per
+ * (k, g)) (the signal weighting of scatter_image.py:1290-1310). */
+int citrus_weighted_group_sum(const float* image, const float* weights, int64_t num_directions, int64_t rows,
+                              int64_t groups, int64_t cols, int64_t weight_cols, float* out, void* stream);
+
+/* accumulator[g, r, c] (+)= sum_k weights[k, g, r | 0, c | 0] image[k, g, r, c] with image element strides (the
+ * accumulation of the full images, DirectionSetContext.accumulate, scatter_image.py:340-371). */
+int citrus_weighted_direction_sum(const float* image, int64_t num_directions, int64_t groups, int64_t rows,
+                                  int64_t cols, int64_t is_k, int64_t is_g, int64_t is_r, int64_t is_c,
+                                  const float* weights, int64_t weight_rows, int64_t weight_cols, float* accumulator,
+                                  int32_t accumulate, void* stream);
+
+/* accumulator[p] (+)= sum_k image[k * stride_k + p], directions in order (scatter_image.py:1289-1319). */
+int citrus_sum_directions(const float* image, int64_t num_directions, int64_t pixels, int64_t stride_k,
+                          float* accumulator, int32_t accumulate, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -125,6 +125,118 @@ def siddon_small():
     save("siddon_small", **arrays)
 
 
+def small_spectral_library():
+    """A three-group Klein-Nishina library from citrus_gb300 (its fields are plain arrays; the reference reads them)."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from citrus_gb300.cross_sections import BONE, WATER, spectral_library
+    from citrus_gb300.workloads import bremsstrahlung_spectrum
+    return spectral_library(np.linspace(120.0, 40.0, 4), bremsstrahlung_spectrum(seed=3), [WATER, BONE], 3,
+                            num_eta=101, fine_per_group=4)
+
+
+def reference_library(lib):
+    """The reference's MultigroupLibrary holding the same float64 tables."""
+    from citrus.scatter_solver.cross_sections import MultigroupLibrary
+    t = lambda a: torch.as_tensor(np.asarray(a), dtype=F64)  # noqa: E731
+    return MultigroupLibrary(group_edges=t(lib.group_edges), group_energy=t(lib.group_energy),
+                             spectrum_fraction=t(lib.spectrum_fraction), mu_t=t(lib.mu_t), mu_pe=t(lib.mu_pe),
+                             mu_s_l=t(lib.mu_s_l), eta_grid=t(lib.eta_grid), mu_s_eta=t(lib.mu_s_eta),
+                             fine_energy=t(lib.fine_energy), fine_mu_t=t(lib.fine_mu_t),
+                             fine_weight=t(lib.fine_weight), fine_group=torch.as_tensor(lib.fine_group),
+                             materials=tuple(lib.materials), nominal_density=t(lib.nominal_density))
+
+
+@case
+def uncollided_small():
+    """Uncollided fluence, first-collision source, sampling correction and LD moments (q = 2) of the reference on a
+    small grid with the synthetic two-material library, flat and curved panels."""
+    from citrus.scatter_solver.angular_quadrature import product_quadrature
+    from citrus.scatter_solver.cross_sections import synthetic_library
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.source import SourceModel
+    from citrus.scatter_solver.uncollided import (DENSE, first_collision_moments_at_directions,
+                                                  first_collision_sampling_correction,
+                                                  first_collision_source_at_directions, uncollided_fluence)
+
+    g = torch.Generator().manual_seed(5)
+    library = reference_library(small_spectral_library())
+    grid = Grid((4, 4, 6), 1.5)
+    rho = torch.rand(2, *grid.shape, generator=g, dtype=F64) * torch.tensor([1.0, 1.8], dtype=F64)[:, None, None, None]
+    q = product_quadrature(4, 8, dtype=F64)
+    arrays = dict(rho=rho, omega=q.omega, weight=q.weight)
+    for name, curved in (("flat", False), ("curved", True)):
+        geo = ConeGeometry(40.0, 60.0, 30, 40, 1.0, 1.0, use_curved_detector=curved)
+        angle = 0.3
+        phi = uncollided_fluence(library, rho, grid, geo, angle, SourceModel(), SiddonProjectors(backend="torch"))
+        src = first_collision_source_at_directions(library, rho, phi, grid, geo, angle, q.omega[::4], pairs=DENSE)
+        corr = first_collision_sampling_correction(library, rho, phi, grid, geo, angle, q.omega, q.weight, pairs=DENSE)
+        mom = first_collision_moments_at_directions(library, rho, phi, grid, geo, angle, q.omega[::4], corr, 2,
+                                                    pairs=DENSE)
+        arrays.update({f"{name}_phi": phi, f"{name}_source": src, f"{name}_scale": corr.scale,
+                       f"{name}_beta": corr.beta, f"{name}_moments": mom})
+    save("uncollided_small", **arrays)
+
+
+def scintillator_table():
+    """A synthetic energy-integrating detector table D(E, theta) = E (1 - exp(-mu(E) t / cos theta))."""
+    e = np.linspace(10.0, 150.0, 57)
+    th = np.radians(np.linspace(0.0, 89.5, 46))
+    mu = 0.9 * (e / 60.0) ** -2.5 + 0.1
+    return e, th, e[:, None] * (-np.expm1(-mu[:, None] * 4.51 * 0.06 / np.cos(th)[None, :]))
+
+
+@case
+def image_small():
+    """The reference's collapsed-cone image (full and signal-only) and primary of one view, flat and curved panels,
+    with the three-group Klein-Nishina library and a synthetic scintillator response."""
+    from citrus.scatter_solver.angular_quadrature import scatter_source_moments
+    from citrus.scatter_solver.cross_sections import mu_t_volume, transfer_moments_volume
+    from citrus.scatter_solver.detector import DetectorResponse, no_grid
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.scatter_image import (combined_scatter_image, make_direction_context,
+                                                     panel_direction_set, primary_image)
+    from citrus.scatter_solver.source import SourceModel
+    from citrus.scatter_solver.uncollided import DENSE, uncollided_fluence
+
+    g = torch.Generator().manual_seed(21)
+    library = reference_library(small_spectral_library())
+    L = 2
+    grid_q = Grid((6, 6, 4), 2.0)
+    q = 2
+    grid_c = grid_q.coarsen(q)
+    rho = torch.rand(2, *grid_q.shape, generator=g, dtype=F64) * torch.tensor([1.0, 0.5], dtype=F64)[:, None, None,
+                                                                                                         None]
+    rho_c = rho.reshape(2, 3, 2, 3, 2, 2, 2).mean(dim=(2, 4, 6))
+    mu_c = mu_t_volume(library, rho_c)
+    phi_coll = torch.rand(library.num_groups, (L + 1) ** 2, *grid_c.shape, generator=g, dtype=F64) * 1e-4
+    T = scatter_source_moments(transfer_moments_volume(library, rho_c)[:, :, :L + 1], phi_coll)
+    e, th, table = scintillator_table()
+    det = DetectorResponse(torch.as_tensor(e), torch.as_tensor(th), torch.as_tensor(table))
+    arrays = dict(rho=rho, T=T, det_e=e, det_theta=th, det_table=table)
+    for name, curved in (("flat", False), ("curved", True)):
+        geo = ConeGeometry(50.0, 80.0, 10, 14, 1.5, 1.5, det_channel_offset=0.4, use_curved_detector=curved)
+        angle = 0.8
+        proj = SiddonProjectors(backend="torch")
+        phi = uncollided_fluence(library, rho, grid_q, geo, angle, SourceModel(), proj)
+        cone = panel_direction_set(geo, angle, (3, 6), max_polar_angle=grid_c, dtype=F64)
+        grid_response = no_grid()
+        ctx = make_direction_context(cone, geo, angle, det, grid_response, library, "cpu", F64, chunk=5)
+        full = combined_scatter_image(library, rho, phi, grid_q, q, T, L, geo, angle, cone, mu_c, proj, det,
+                                      grid_response, ctx, pairs=DENSE, grid_coarse=grid_c)
+        sig = combined_scatter_image(library, rho, phi, grid_q, q, T, L, geo, angle, cone, mu_c, proj, det,
+                                     grid_response, ctx, pairs=DENSE, grid_coarse=grid_c,
+                                     signal_only=True)["signal"]
+        prim = primary_image(library, rho, grid_q, geo, angle, SourceModel(), proj, det, grid_response)
+        arrays.update({f"{name}_phi": phi, f"{name}_cone_omega": cone.omega, f"{name}_cone_weight": cone.weight,
+                       f"{name}_cone_width": cone.cell_width, f"{name}_fluence": full["fluence"],
+                       f"{name}_planar": full["planar_fluence"], f"{name}_signal_pg": full["signal_per_group"],
+                       f"{name}_signal": full["signal"], f"{name}_signal_only": sig,
+                       f"{name}_primary_signal": prim["signal"], f"{name}_primary_fluence": prim["fluence"]})
+    save("image_small", **arrays)
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)
     for n in names:

@@ -151,3 +151,33 @@ def test_c_oracle_sweep_matches_numpy_oracle():
     expected = osweep.sweep_chunk(shape, c, mu, src)
     got = native.sweep_chunk(osweep.plan(shape), c, mu, src)
     assert rel_err(got, expected) < 1e-14
+
+
+def _uncollided_setup():
+    from citrus_gb300.cross_sections import BONE, WATER, spectral_library
+    from citrus_gb300.geometry import ConeGeometry
+    from citrus_gb300.workloads import bremsstrahlung_spectrum
+    library = spectral_library(np.linspace(120.0, 40.0, 4), bremsstrahlung_spectrum(seed=3), [WATER, BONE], 3,
+                               num_eta=101, fine_per_group=4)
+    grid = Grid((4, 4, 6), 1.5)
+    geos = {name: ConeGeometry(40.0, 60.0, 30, 40, 1.0, 1.0, use_curved_detector=curved)
+            for name, curved in (("flat", False), ("curved", True))}
+    return library, grid, geos
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_oracle_uncollided_and_first_collision_match_reference(name):
+    from oracle import physics
+    g = golden("uncollided_small")
+    library, grid, geos = _uncollided_setup()
+    geo, angle, rho = geos[name], 0.3, g["rho"]
+    phi = physics.uncollided_fluence(library, rho, grid, geo, angle)
+    assert rel_err(phi, g[f"{name}_phi"]) < 1e-12
+    om = g["omega"]
+    assert rel_err(physics.first_collision_source(library, rho, phi, grid, geo, angle, om[::4]),
+                   g[f"{name}_source"]) < 1e-12
+    scale, beta, _, _ = physics.correction(library, rho, phi, grid, geo, angle, om, g["weight"])
+    assert rel_err(scale, g[f"{name}_scale"]) < 1e-11 and rel_err(beta, g[f"{name}_beta"]) < 1e-10
+    assert np.abs(g[f"{name}_beta"]).max() > 1e-3  # a non-trivial correction (Klein-Nishina kernel)
+    assert rel_err(physics.first_collision_moments(library, rho, phi, grid, geo, angle, om[::4], scale, beta, 2),
+                   g[f"{name}_moments"]) < 1e-12

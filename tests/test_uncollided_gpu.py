@@ -1,0 +1,74 @@
+"""Parity of the uncollided-fluence and first-collision kernels with the reference fixtures and the oracle."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden, rel_err
+from citrus_gb300.ray_tracing import GB300Projectors
+from citrus_gb300.responses import SourceModel
+from citrus_gb300.uncollided import (first_collision_moments_at_directions, first_collision_sampling_correction,
+                                     first_collision_source_at_directions, group_transmission, uncollided_fluence)
+from oracle import physics
+from test_oracle_golden import _uncollided_setup
+
+pytestmark = pytest.mark.gpu
+F32_REL = 1e-5
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_uncollided_and_first_collision_match_reference(cuda_device, name):
+    g = golden("uncollided_small")
+    library, grid, geos = _uncollided_setup()
+    geo, angle = geos[name], 0.3
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    rho = dev(g["rho"])
+    phi = uncollided_fluence(library, rho, grid, geo, angle, SourceModel(), GB300Projectors())
+    assert rel_err(phi, g[f"{name}_phi"]) < 2e-6
+    om, w = dev(g["omega"]), dev(g["weight"])
+    src = first_collision_source_at_directions(library, rho, phi, grid, geo, angle, om[::4])
+    assert rel_err(src, g[f"{name}_source"]) < F32_REL
+    corr = first_collision_sampling_correction(library, rho, phi, grid, geo, angle, om, w)
+    assert rel_err(corr.scale, g[f"{name}_scale"]) < F32_REL
+    assert rel_err(corr.beta, g[f"{name}_beta"]) < 1e-4
+    mom = first_collision_moments_at_directions(library, rho, phi, grid, geo, angle, om[::4], corr, 2,
+                                                cell_major=False)
+    assert rel_err(mom, g[f"{name}_moments"]) < F32_REL
+
+
+def test_group_transmission_matches_oracle(cuda_device):
+    library, _, _ = _uncollided_setup()
+    rng = np.random.default_rng(2)
+    path = rng.random((2, 7, 9)) * 20.0
+    got = group_transmission(library, torch.as_tensor(path, dtype=torch.float32, device=cuda_device))
+    assert rel_err(got, physics.group_transmission(library, path)) < 2e-6
+    # a subset of materials, as the uncollided fluence traces only the present ones
+    got = group_transmission(library, torch.as_tensor(path[1:], dtype=torch.float32, device=cuda_device), [1])
+    assert rel_err(got, physics.group_transmission(library, path[1:], [1])) < 2e-6
+
+
+def test_config_library_first_collision_on_refined_grid(cuda_device):
+    """The eight-group Klein-Nishina library of the batched-views workload on a q = 3 quadrature grid."""
+    from citrus_gb300.geometry import ConeGeometry, Grid
+    from citrus_gb300.quadrature import product_quadrature
+    from citrus_gb300.workloads import batched_views
+    w = batched_views()
+    library = w.library
+    grid = Grid((6, 9, 6), 0.5)
+    geo = ConeGeometry(100.0, 150.0, 192, 256, 0.16, 0.16, use_curved_detector=True)
+    rng = np.random.default_rng(9)
+    rho = rng.random((2, *grid.shape)) * np.array([1.0, 1.85])[:, None, None, None]
+    phi = physics.uncollided_fluence(library, rho, grid, geo, 1.1)
+    q = product_quadrature(6, 20)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    scale, beta, _, _ = physics.correction(library, rho, phi, grid, geo, 1.1, q.omega, q.weight)
+    corr = first_collision_sampling_correction(library, dev(rho), dev(phi), grid, geo, 1.1, dev(q.omega),
+                                               dev(q.weight))
+    assert rel_err(corr.scale, scale) < 1e-5
+    assert np.abs(corr.beta.cpu().numpy() - beta).max() < 1e-4
+    ref = physics.first_collision_moments(library, rho, phi, grid, geo, 1.1, q.omega[:16], scale, beta, 3)
+    got = first_collision_moments_at_directions(library, dev(rho), dev(phi), grid, geo, 1.1, dev(q.omega[:16]), corr,
+                                                3, cell_major=False)
+    assert rel_err(got, ref) < 2e-5
