@@ -35,7 +35,8 @@ def _parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="sweep", choices=["sweep"])
+    p.add_argument("--workload", default="step", choices=["step", "sweep"])
+    p.add_argument("--views", type=int, default=0, help="views per step (0: the workload's 60)")
     p.add_argument("--method", default="persistent", choices=["persistent", "planes"])
     p.add_argument("--dc", type=int, default=0, help="directions per octant per sweep chunk (0: all)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
@@ -257,9 +258,118 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# =====================================================================================================================
+# the scatter step of every view
+# =====================================================================================================================
+
+def make_step_solver(device, views: int = 0):
+    """The batched-views workload: solver, fields input, view angles (64^3, G = 8, P5, 120 directions, curved 256 x 192
+    panel, cone 16 x 32, ideal counting detector, no grid)."""
+    from citrus_gb300.responses import ideal_counting_response, no_grid
+    from citrus_gb300.scatter_solver import ScatterSolver, SolverConfig
+    from citrus_gb300.workloads import batched_views
+
+    w = batched_views()
+    config = SolverConfig(num_groups=w.library.num_groups, legendre_order=w.legendre_order, num_polar=w.num_polar,
+                          num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
+                          quadrature_point_spacing_cm=0.5, cone_num_polar=w.cone_num_polar,
+                          cone_num_azimuthal=w.cone_num_azimuthal)
+    solver = ScatterSolver(w.library, config, w.geometry, detector=ideal_counting_response(), grid_response=no_grid(),
+                           device=device)
+    angles = w.angles()
+    if views:
+        angles = angles[:views]
+    return w, solver, angles
+
+
+def run_step(args):
+    import torch
+
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+    w, solver, angles = make_step_solver(device, args.views)
+    # weak scaling: every rank runs its own set of views (offset by the rank) of the same phantom
+    angles = angles + rank * (2 * math.pi / len(angles)) / max(1, world)
+    V = len(angles)
+    rho_host = torch.as_tensor(w.rho, dtype=torch.float32).pin_memory()
+    rho_dev = rho_host.to(device)
+    states = [CitrusState() for _ in angles]
+    stream = torch.cuda.current_stream(device)
+
+    def one_step(rho, signals=None):
+        fields = solver.material_fields(rho, w.grid)
+        for v, angle in enumerate(angles):
+            scatter, _, states[v] = citrus_view_step(solver, states[v], fields, float(angle), primary=False)
+            if signals is not None:
+                signals[v].copy_(scatter, non_blocking=True)
+
+    for _ in range(args.warmup):
+        one_step(rho_dev)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with sampler:
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            one_step(rho_dev)
+        end.record(stream)
+        torch.cuda.synchronize()
+    elapsed = start.elapsed_time(end) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t)
+    # e2e: the densities in from pinned host memory, every view's scatter signal out to pinned host memory
+    Rd, Cd = w.geometry.image_shape
+    host_signals = torch.empty(V, Rd, Cd, dtype=torch.float32).pin_memory()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        one_step(rho_host.to(device, non_blocking=True), host_signals)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e = e0.elapsed_time(e1) / 1e3
+    ms_per_view = elapsed * 1e3 / (args.steps * V)
+    N = w.grid.num_voxels
+    updates = 8 * (w.num_polar * w.num_azimuthal // 8) * N * w.library.num_groups
+    line = {
+        "metric": "scatter-step ms/view (all views of one outer iteration; cell*dir*group updates/s alongside)",
+        "value": ms_per_view / max(1, world), "unit": "ms/view", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom and library)",
+        "config": {"workload": f"batched_views: 64^3 cells x 0.4 cm, G=8 (30-120 keV), P5, 120 sweep directions, "
+                               f"cone 16x32, curved 256x192 panel, {V} views per rank per step, one accumulator "
+                               f"sweep per view (citrus_view_step, signal only)",
+                   "l2": "inputs larger than L2 (4 GB sweep store per view)"},
+        "updates_per_s": updates * V * args.steps * world / elapsed,
+        "e2e": {"value": e2e * 1e3 / (args.steps * V) / max(1, world), "unit": "ms/view",
+                "h2d_bytes_per_step": rho_host.numel() * 4, "d2h_bytes_per_step": host_signals.numel() * 4},
+        "clocks": sampler.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 if __name__ == "__main__":
     a = _parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "step":
+        run_step(a)
     else:
         run_gb300(a)

@@ -237,6 +237,56 @@ def image_small():
     save("image_small", **arrays)
 
 
+STEP_CONFIG = dict(num_groups=3, legendre_order=2, num_polar=4, num_azimuthal=8, transport_cell_cm=2.0,
+                   quadrature_point_spacing_cm=1.0, cone_num_polar=3, cone_num_azimuthal=6, direction_chunk=4,
+                   source_iteration_tolerance=1e-4, max_source_iterations=40)
+
+
+@case
+def citrus_step_small():
+    """Two CITRUS scatter steps of one view (citrus_view_step with the primary) and a converged solve_view of the
+    reference's ScatterSolver, float64 CPU, flat and curved panels."""
+    from citrus.citrus import CitrusState, citrus_view_step
+    from citrus.scatter_solver.config import SolverConfig
+    from citrus.scatter_solver.detector import DetectorResponse, no_grid
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.scatter_solver import ScatterSolver
+
+    g = torch.Generator().manual_seed(31)
+    library = reference_library(small_spectral_library())
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.zeros(2, *grid.shape, dtype=F64)
+    rho[0] = 0.9 + 0.2 * torch.rand(*grid.shape, generator=g, dtype=F64)
+    rho[1, 2:5, 3:6, 1:4] = 1.85
+    rho[0, 2:5, 3:6, 1:4] = 0.0
+    e, th, table = scintillator_table()
+    det = DetectorResponse(torch.as_tensor(e), torch.as_tensor(th), torch.as_tensor(table))
+    config = SolverConfig(**STEP_CONFIG)
+    arrays = dict(rho=rho, det_e=e, det_theta=th, det_table=table)
+    for name, curved in (("flat", False), ("curved", True)):
+        geo = ConeGeometry(40.0, 60.0, 12, 16, 1.2, 1.2, use_curved_detector=curved)
+        solver = ScatterSolver(library, config, geo, SiddonProjectors(backend="torch"), det, no_grid(),
+                               device="cpu", dtype=F64)
+        fields = solver.material_fields(rho, grid)
+        angle = 0.6
+        state = CitrusState()
+        for step in (1, 2):
+            scatter, primary, state = citrus_view_step(solver, state, fields, angle, primary=True)
+            arrays[f"{name}_step{step}_scatter"] = scatter
+            arrays[f"{name}_step{step}_collided"] = state.collided_moments
+            arrays[f"{name}_step{step}_change"] = np.asarray(state.history[-1])
+        arrays[f"{name}_primary"] = primary
+        result = solver.solve_view(rho, grid, angle, signal_only=True)
+        arrays[f"{name}_solve_scatter"] = result.scatter_signal
+        arrays[f"{name}_solve_primary"] = result.primary["signal"]
+        arrays[f"{name}_solve_iterations"] = np.asarray(result.source_iteration_result.num_iterations)
+        arrays[f"{name}_solve_history"] = np.asarray(result.source_iteration_result.history)
+        arrays[f"{name}_mu_t_coarse"] = fields.mu_t_coarse
+        arrays[f"{name}_rho_coarse"] = fields.rho_coarse
+    save("citrus_step_small", **arrays)
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)
     for n in names:

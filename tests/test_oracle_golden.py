@@ -181,3 +181,42 @@ def test_oracle_uncollided_and_first_collision_match_reference(name):
     assert np.abs(g[f"{name}_beta"]).max() > 1e-3  # a non-trivial correction (Klein-Nishina kernel)
     assert rel_err(physics.first_collision_moments(library, rho, phi, grid, geo, angle, om[::4], scale, beta, 2),
                    g[f"{name}_moments"]) < 1e-12
+
+
+def _image_setup():
+    from citrus_gb300.geometry import ConeGeometry
+    from citrus_gb300.responses import DetectorResponse
+    g = golden("image_small")
+    library, _, _ = _uncollided_setup()
+    grid_q = Grid((6, 6, 4), 2.0)
+    det = DetectorResponse(g["det_e"], g["det_theta"], g["det_table"])
+    geos = {name: ConeGeometry(50.0, 80.0, 10, 14, 1.5, 1.5, det_channel_offset=0.4, use_curved_detector=curved)
+            for name, curved in (("flat", False), ("curved", True))}
+    return g, library, grid_q, det, geos
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_oracle_image_and_primary_match_reference(name):
+    from citrus_gb300.scatter_image import panel_direction_set
+    from oracle import image as oimage
+    from oracle import physics
+    g, library, grid_q, det, geos = _image_setup()
+    geo, angle = geos[name], 0.8
+    grid_c = grid_q.coarsen(2)
+    rho = g["rho"]
+    rho_c = rho.reshape(2, 3, 2, 3, 2, 2, 2).mean(axis=(2, 4, 6))
+    mu_c = np.einsum("mg,mijk->gijk", library.mu_t, rho_c)
+    phi = physics.uncollided_fluence(library, rho, grid_q, geo, angle)
+    assert rel_err(phi, g[f"{name}_phi"]) < 1e-12
+    cone = panel_direction_set(geo, angle, (3, 6), max_polar_angle=grid_c)
+    np.testing.assert_allclose(cone.omega, g[f"{name}_cone_omega"], atol=1e-13)
+    np.testing.assert_allclose(cone.cell_width, g[f"{name}_cone_width"], rtol=1e-10, atol=1e-13)
+    img = oimage.combined_image(library, rho, phi, grid_q, 2, g["T"], 2, geo, angle, cone.omega, cone.weight,
+                                cone.cell_width, mu_c, det)
+    assert rel_err(img["fluence"], g[f"{name}_fluence"]) < 1e-11
+    assert rel_err(img["planar_fluence"], g[f"{name}_planar"]) < 1e-11
+    assert rel_err(img["signal_per_group"], g[f"{name}_signal_pg"]) < 1e-11
+    assert rel_err(img["signal"], g[f"{name}_signal_only"]) < 1e-11
+    prim = oimage.primary(library, rho, grid_q, geo, angle, det)
+    assert rel_err(prim["signal"], g[f"{name}_primary_signal"]) < 1e-12
+    assert rel_err(prim["fluence"], g[f"{name}_primary_fluence"]) < 1e-12
