@@ -14,7 +14,7 @@ constexpr int kThreads = 256;  // 8 warps; warp w owns rows w, w + 8, ... of the
 constexpr int kCols = 128;     // columns per block: 32 lanes x float4
 constexpr int kChunk = 32;     // rows of B per shared-memory chunk
 
-template <int R>
+template <int R, bool kAligned>
 __global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __restrict__ A, int64_t lda,
                                                                 const float* __restrict__ B, int64_t ldb,
                                                                 float* __restrict__ C, int64_t ldc, int M, int K,
@@ -44,7 +44,15 @@ __global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __r
       const int r = i / (kCols / 4), c4 = i % (kCols / 4);
       const int64_t gc = col0 + 4 * c4;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gc < J) v = *reinterpret_cast<const float4*>(B + (int64_t)(k0 + r) * ldb + gc);
+      const float* row = B + (int64_t)(k0 + r) * ldb;
+      if (kAligned) {
+        if (gc < J) v = *reinterpret_cast<const float4*>(row + gc);
+      } else {
+        if (gc < J) v.x = row[gc];
+        if (gc + 1 < J) v.y = row[gc + 1];
+        if (gc + 2 < J) v.z = row[gc + 2];
+        if (gc + 3 < J) v.w = row[gc + 3];
+      }
       *reinterpret_cast<float4*>(Bs + r * kCols + 4 * c4) = v;
     }
     __syncthreads();
@@ -65,32 +73,49 @@ __global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __r
   for (int i = 0; i < R; ++i) {
     const int row = row0 + warp + 8 * i;
     if (row >= M) break;
-    float4* out = reinterpret_cast<float4*>(C + (int64_t)row * ldc + col);
     float4 v = acc[i];
-    if (accumulate) {
-      const float4 o = *out;
-      v.x += o.x;
-      v.y += o.y;
-      v.z += o.z;
-      v.w += o.w;
+    if (kAligned) {
+      float4* out = reinterpret_cast<float4*>(C + (int64_t)row * ldc + col);
+      if (accumulate) {
+        const float4 o = *out;
+        v.x += o.x;
+        v.y += o.y;
+        v.z += o.z;
+        v.w += o.w;
+      }
+      *out = v;
+    } else {
+      float* out = C + (int64_t)row * ldc + col;
+      const float vals[4] = {v.x, v.y, v.z, v.w};
+      for (int q = 0; q < 4; ++q)
+        if (col + q < J) out[q] = accumulate ? out[q] + vals[q] : vals[q];
     }
-    *out = v;
   }
+}
+
+template <int R, bool kAligned>
+int launch_variant(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
+                   int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t stream) {
+  const size_t smem = ((size_t)8 * R * K + (size_t)kChunk * kCols) * sizeof(float);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(small_k_gemm_kernel<R, kAligned>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
+  }
+  dim3 grid((unsigned)cdiv(J, kCols), (unsigned)cdiv(M, 8 * R), (unsigned)batch);
+  small_k_gemm_kernel<R, kAligned><<<grid, kThreads, smem, stream>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
+                                                                     stride_c, accumulate);
+  return launch_status("citrus_small_k_gemm");
 }
 
 template <int R>
 int launch(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K, int64_t J,
            int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t stream) {
-  const size_t smem = ((size_t)8 * R * K + (size_t)kChunk * kCols) * sizeof(float);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(small_k_gemm_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
-  }
-  dim3 grid((unsigned)cdiv(J, kCols), (unsigned)cdiv(M, 8 * R), (unsigned)batch);
-  small_k_gemm_kernel<R><<<grid, kThreads, smem, stream>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b, stride_c,
-                                                           accumulate);
-  return launch_status("citrus_small_k_gemm");
+  const bool aligned = J % 4 == 0 && ldb % 4 == 0 && ldc % 4 == 0 && stride_b % 4 == 0 && stride_c % 4 == 0 &&
+                       ((uintptr_t)B % 16) == 0 && ((uintptr_t)C % 16) == 0;
+  if (aligned) return launch_variant<R, true>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate,
+                                              stream);
+  return launch_variant<R, false>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, stream);
 }
 
 }  // namespace
@@ -107,10 +132,6 @@ extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, 
                  (long long)J, (long long)batch);
   CITRUS_REQUIRE(K <= 1024 && M <= (1 << 20), "citrus_small_k_gemm: K %lld or M %lld too large", (long long)K,
                  (long long)M);
-  CITRUS_REQUIRE(J % 4 == 0 && ldb % 4 == 0 && ldc % 4 == 0 && stride_b % 4 == 0 && stride_c % 4 == 0,
-                 "citrus_small_k_gemm: J, ldb, ldc and the batch strides must be multiples of 4");
-  CITRUS_REQUIRE(((uintptr_t)B % 16) == 0 && ((uintptr_t)C % 16) == 0, "citrus_small_k_gemm: B and C must be "
-                 "16-byte aligned");
   CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "citrus_small_k_gemm: leading dimensions too small");
   if (J == 0) return CITRUS_OK;
   const int m = (int)M, k = (int)K;

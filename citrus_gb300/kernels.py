@@ -179,7 +179,8 @@ def _merged_stride(t: Tensor, first: int) -> Optional[int]:
     return kept[-1][1]
 
 
-def scattering_moments(transfer: Tensor, phi: Tensor, layout: str = "contiguous") -> Tensor:
+def scattering_moments(transfer: Tensor, phi: Tensor, layout: str = "contiguous",
+                       out: Optional[Tensor] = None) -> Tensor:
     """Scattering-source moments ``T[g, n] = sum_g' transfer[g', g, l(n)] phi[g', n]`` (reference
     ``scattering_kernels.py:206-252``), in a new tensor of the requested storage.
 
@@ -188,6 +189,8 @@ def scattering_moments(transfer: Tensor, phi: Tensor, layout: str = "contiguous"
         phi: [G_in, N, *rest] moments, rest = spatial or (4, *spatial), any strides.
         layout: "contiguous" ([G_out, N, *rest]), "moment_major" ([N, G_out, *rest]) or "cell_major"
             ([N, *spatial, G_out, (4)], the sweep's storage).
+        out: storage of the requested layout to write into (``[N, *spatial, G_out, (4)]`` for "cell_major"), or
+            None to allocate it.
 
     Returns:
         [G_out, N, *rest] view of the requested storage.
@@ -214,13 +217,20 @@ def scattering_moments(transfer: Tensor, phi: Tensor, layout: str = "contiguous"
     if ps_x is None:
         phi = phi.contiguous()
         ps_x = 1
+    if layout != "cell_major" and out is not None:
+        raise ValueError("out is supported for the cell_major layout")
     if layout == "contiguous":
         out = torch.empty((G_out, N) + rest, device=phi.device, dtype=phi.dtype)
     elif layout == "moment_major":
         out = torch.empty((N, G_out) + rest, device=phi.device, dtype=phi.dtype).movedim(0, 1)
     else:
-        storage = torch.empty((N,) + spatial + (G_out,) + ((4,) if has_k else ()), device=phi.device,
-                              dtype=phi.dtype)
+        shape = (N,) + spatial + (G_out,) + ((4,) if has_k else ())
+        if out is not None:
+            if tuple(out.shape) != shape or not out.is_contiguous() or out.dtype != torch.float32:
+                raise ValueError(f"out must be contiguous float32 cell-major storage {shape}")
+            storage = out
+        else:
+            storage = torch.empty(shape, device=phi.device, dtype=phi.dtype)
         out = cell_major_view(storage, len(spatial))
     os_x = _merged_stride(out, out.dim() - len(spatial))
     if X == 0:

@@ -65,7 +65,8 @@ int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c,
  * C[b] (=|+=) A @ B[b] with A [M, K] row-major (lda), B[b] [K, J] row-major (ldb), C[b] [M, J] row-major (ldc),
  * batch b with element strides stride_b, stride_c. Replaces the torch.mm/addmm_ calls of
  * citrus/scatter_solver/transport_sweep.py:524-528 (moment accumulation), source_iteration.py:94-103 (scattering
- * source) and scatter_image.py:1246 (multiple-collision source). Requires J % 4 == 0 and 16-byte aligned rows.
+ * source) and scatter_image.py:1246 (multiple-collision source). Rows that are 16-byte aligned with J % 4 == 0 move
+ * as float4; any other shape takes the element-wise path.
  * ------------------------------------------------------------------------------------------------------------------ */
 int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t M,
                         int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int32_t accumulate,
