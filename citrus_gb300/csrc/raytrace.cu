@@ -6,8 +6,9 @@
 // The walk keeps the ray's position as integer voxel indices plus a fractional position inside the current voxel, so
 // every segment length is computed from quantities of voxel size (relative error ~ float epsilon per segment), and the
 // travelled distance is summed with a compensated (Kahan) sum, so the end of the ray is placed to float epsilon of its
-// total length. Rays that must meet 1e-6 relative path lengths (upstream to points, primary) do their set-up in
-// float64; the dense image rays (downstream, oblique) do it in float32.
+// total length, and it crosses along each axis only as many planes as lie between the entry and exit voxels. Rays that
+// must meet 1e-6 relative path lengths (upstream to points, primary) and the oblique rays through the pixel centres,
+// some of which run along a face of the box, do their set-up in float64; the downstream rays do it in float32.
 //
 // Volumes are read voxel-major, [V, C] with the C channels (groups or materials) of a voxel contiguous, so one voxel
 // visit is one or two 16-byte loads for every channel at once.
@@ -44,7 +45,15 @@ struct Setup {
   float v[3];       // direction in voxel units per cm
   int idx[3];       // voxel index at the entry point
   float f[3];       // fractional position inside that voxel, in [0, 1]
+  int cross[3];     // plane crossings along each axis between the entry and exit voxels
 };
+
+// Rounded add and multiply that the compiler may not fuse, for the set-up steps whose rounding decides which voxels a
+// line touches (the reference evaluates them as separate float64 tensor operations).
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 
 // Clip p0 -> p1 to the box and locate the entry voxel. T is the arithmetic type of the set-up (double or float).
 template <typename T>
@@ -54,7 +63,7 @@ __device__ __forceinline__ Setup<T> ray_setup(const Box& b, const T p0[3], const
   T a_lo = 0, a_hi = 1;
   for (int a = 0; a < 3; ++a) {
     d[a] = p1[a] - p0[a];
-    const T lo = (T)b.lo[a], hi = (T)b.lo[a] + (T)b.delta[a] * (T)b.n[a];
+    const T lo = (T)b.lo[a], hi = add_rn(lo, mul_rn((T)b.delta[a], (T)b.n[a]));
     if (d[a] != 0) {
       const T inv = (T)1 / d[a];
       const T t1 = (lo - p0[a]) * inv, t2 = (hi - p0[a]) * inv;
@@ -84,6 +93,13 @@ __device__ __forceinline__ Setup<T> ray_setup(const Box& b, const T p0[3], const
     if (fr > 1) fr = 1;
     s.idx[a] = i;
     s.f[a] = (float)fr;
+    // exit voxel along this axis, clamped like the entry one: a line that runs along a face of the box (within
+    // rounding) stays in the boundary layer for its whole clipped length, as the segment midpoints of
+    // ray_tracing.py:186-192 place it, instead of stepping out through that face at once
+    int ie = (int)floor((p0[a] + a_hi * d[a] - (T)b.lo[a]) / (T)b.delta[a]);
+    if (ie < 0) ie = 0;
+    if (ie > b.n[a] - 1) ie = b.n[a] - 1;
+    s.cross[a] = ie > i ? ie - i : i - ie;
   }
   return s;
 }
@@ -103,12 +119,13 @@ __device__ __forceinline__ void ray_walk(const Box& b, const Setup<float>& s, co
   const float ivy = vy != 0.f ? 1.f / fabsf(vy) : INFINITY;
   const float ivz = vz != 0.f ? 1.f / fabsf(vz) : INFINITY;
   const int stx = vx > 0.f ? 1 : -1, sty = vy > 0.f ? 1 : -1, stz = vz > 0.f ? 1 : -1;
+  int cx = s.cross[0], cy = s.cross[1], cz = s.cross[2];  // crossings left along each axis
   float t = 0.f, t_comp = 0.f;  // travelled distance, Kahan-compensated
   const int max_steps = b.n[0] + b.n[1] + b.n[2] + 3;
   for (int step = 0; step < max_steps; ++step) {
-    const float dx = (vx > 0.f ? 1.f - fx : fx) * ivx;
-    const float dy = (vy > 0.f ? 1.f - fy : fy) * ivy;
-    const float dz = (vz > 0.f ? 1.f - fz : fz) * ivz;
+    const float dx = cx > 0 ? (vx > 0.f ? 1.f - fx : fx) * ivx : INFINITY;
+    const float dy = cy > 0 ? (vy > 0.f ? 1.f - fy : fy) * ivy : INFINITY;
+    const float dz = cz > 0 ? (vz > 0.f ? 1.f - fz : fz) * ivz : INFINITY;
     int axis = 0;
     float dt = dx;
     if (dy < dt) { dt = dy; axis = 1; }
@@ -162,14 +179,17 @@ __device__ __forceinline__ void ray_walk(const Box& b, const Setup<float>& s, co
     fz = fminf(fmaxf(fmaf(dt, vz, fz), 0.f), 1.f);
     if (axis == 0) {
       ix += stx;
+      --cx;
       fx = stx > 0 ? 0.f : 1.f;
       if (ix < 0 || ix >= b.n[0]) break;
     } else if (axis == 1) {
       iy += sty;
+      --cy;
       fy = sty > 0 ? 0.f : 1.f;
       if (iy < 0 || iy >= b.n[1]) break;
     } else {
       iz += stz;
+      --cz;
       fz = stz > 0 ? 0.f : 1.f;
       if (iz < 0 || iz >= b.n[2]) break;
     }
@@ -188,6 +208,7 @@ __device__ __forceinline__ void integrate(const Box& b, const T p0[3], const T p
     s.v[a] = st.v[a];
     s.idx[a] = st.idx[a];
     s.f[a] = st.f[a];
+    s.cross[a] = st.cross[a];
   }
   ray_walk<kC, kCompensated>(b, s, vol, C, acc);
 }
@@ -302,27 +323,33 @@ __global__ void __launch_bounds__(kThreads) downstream_kernel(Box b, const float
 }
 
 // ---- oblique: through every pixel centre along each direction, clipped to the box on both sides --------------
+// The set-up is float64 from float64 pixel centres, as the reference forms these lines: a line that grazes a face of
+// the box is inside or outside exactly as in float64, where a float32 rounding of the pixel centre could move it onto
+// the face and integrate a whole slice.
 template <int kC>
 __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* __restrict__ vol, int C,
                                                            int64_t field_stride, const float* __restrict__ omegas,
-                                                           const float* __restrict__ pixels, int64_t P, float cx,
-                                                           float cy, float cz, float half,
+                                                           const double* __restrict__ pixels, int64_t P, double cx,
+                                                           double cy, double cz, double half,
                                                            float* __restrict__ out, int64_t os_k, int64_t os_c,
                                                            int64_t os_r, int64_t os_col, int64_t cols) {
   const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int k = blockIdx.y;
   if (p >= P) return;
-  const float w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
-  const float px = pixels[3 * p], py = pixels[3 * p + 1], pz = pixels[3 * p + 2];
-  const float w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
-  const float cp = ((cx - px) * w[0] + (cy - py) * w[1] + (cz - pz) * w[2]) / w2;
-  const float h = half / sqrtf(w2);
-  const float a[3] = {px + (cp - h) * w[0], py + (cp - h) * w[1], pz + (cp - h) * w[2]};
-  const float e[3] = {px + (cp + h) * w[0], py + (cp + h) * w[1], pz + (cp + h) * w[2]};
+  const double w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
+  const double px = pixels[3 * p], py = pixels[3 * p + 1], pz = pixels[3 * p + 2];
+  // the endpoints of ray_tracing.py:588-595, operation by operation
+  const double w2 = add_rn(add_rn(mul_rn(w[0], w[0]), mul_rn(w[1], w[1])), mul_rn(w[2], w[2]));
+  const double dot = add_rn(add_rn(mul_rn(cx - px, w[0]), mul_rn(cy - py, w[1])), mul_rn(cz - pz, w[2]));
+  const double cp = dot / w2;
+  const double h = half / sqrt(w2);
+  const double tm = cp - h, tp = cp + h;
+  const double a[3] = {add_rn(px, mul_rn(tm, w[0])), add_rn(py, mul_rn(tm, w[1])), add_rn(pz, mul_rn(tm, w[2]))};
+  const double e[3] = {add_rn(px, mul_rn(tp, w[0])), add_rn(py, mul_rn(tp, w[1])), add_rn(pz, mul_rn(tp, w[2]))};
   const int nC = kC > 0 ? kC : C;
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
-  integrate<kC, false, float>(b, a, e, vol + (int64_t)k * field_stride, C, acc);
+  integrate<kC, false, double>(b, a, e, vol + (int64_t)k * field_stride, C, acc);
   const int64_t row = p / cols;
   float* o = out + (int64_t)k * os_k + row * os_r + (p - row * cols) * os_col;
   for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = acc[c];
@@ -420,7 +447,7 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
 
 extern "C" int citrus_oblique_project(const float* field, int64_t channels, int64_t field_stride, const double* box,
                                       const int64_t* dims, const float* omegas, int64_t num_directions,
-                                      const float* pixels, int64_t num_rows, int64_t num_cols, float* out,
+                                      const double* pixels, int64_t num_rows, int64_t num_cols, float* out,
                                       int64_t os_k, int64_t os_c, int64_t os_r, int64_t os_col, void* stream) {
   int status = check_common(field, channels, box, dims, out);
   if (status) return status;
@@ -440,7 +467,7 @@ extern "C" int citrus_oblique_project(const float* field, int64_t channels, int6
   const int C = (int)channels;
   dim3 grid((unsigned)cdiv(num_pixels, kThreads), (unsigned)num_directions);
   CITRUS_CHANNEL_DISPATCH(C, oblique_kernel, grid, as_stream(stream), b, field, C, field_stride, omegas, pixels,
-                          num_pixels, (float)center[0], (float)center[1], (float)center[2], (float)half, out, os_k,
-                          os_c, os_r, os_col, num_cols)
+                          num_pixels, center[0], center[1], center[2], half, out, os_k, os_c, os_r, os_col,
+                          num_cols)
   return launch_status("citrus_oblique_project");
 }

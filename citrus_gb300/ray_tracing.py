@@ -202,7 +202,8 @@ class GB300Projectors:
         else:
             raise ValueError(f"field must be [C, ...] or [K={K}, C, ...], got {tuple(field.shape)}")
         Rd, Cd = geometry.image_shape
-        pixels = torch.as_tensor(geometry.pixel_centers_np(angle).reshape(-1, 3), dtype=torch.float32).to(device)
+        pixels = torch.as_tensor(np.ascontiguousarray(geometry.pixel_centers_np(angle).reshape(-1, 3)),
+                                 dtype=torch.float64).to(device)
         if out is None:
             out = torch.empty(K, C, Rd, Cd, device=device, dtype=torch.float32)
         if tuple(out.shape) != (K, C, Rd, Cd):

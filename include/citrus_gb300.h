@@ -113,12 +113,13 @@ int citrus_downstream_cumulative(const float* volume, int64_t channels, const do
                                  const float* omegas, const uint8_t* toward, int64_t num_directions,
                                  const double* panel, double diagonal, float* out, void* stream);
 
-/* Line through every pixel centre (pixels [rows, cols, 3]) along each direction, clipped to the box on both sides;
+/* Line through every pixel centre (float64 pixels [rows, cols, 3]) along each direction, clipped to the box on both
+ * sides (float64 set-up);
  * field [K or 1, V, C] with field_stride elements between directions (0: shared); out element (k, c, row, col) at
  * k * os_k + c * os_c + row * os_r + col * os_col (any layout, e.g. rows-outer [K, rows, C, cols]).
  * Replaces oblique_project (ray_tracing.py:548-620). */
 int citrus_oblique_project(const float* field, int64_t channels, int64_t field_stride, const double* box,
-                           const int64_t* dims, const float* omegas, int64_t num_directions, const float* pixels,
+                           const int64_t* dims, const float* omegas, int64_t num_directions, const double* pixels,
                            int64_t num_rows, int64_t num_cols, float* out, int64_t os_k, int64_t os_c, int64_t os_r,
                            int64_t os_col, void* stream);
 

@@ -110,9 +110,12 @@ def oblique_project(field, grid, geometry, angle, omegas):
     center = lo + 0.5 * np.asarray(grid.extent)
     half = 0.5 * math.sqrt(sum(e * e for e in grid.extent)) * (1 + 1e-6) + 1e-6
     out = []
+    q = center - p
     for k, w in enumerate(omegas):
-        w2 = float(w @ w)
-        cp = ((center - p) @ w) / w2
+        # elementwise, in the reference's order of operations (ray_tracing.py:588-595): the rounding of these
+        # endpoints decides whether a line along a face of the box meets it
+        w2 = float((w[0] * w[0] + w[1] * w[1]) + w[2] * w[2])
+        cp = ((q[:, 0] * w[0] + q[:, 1] * w[1]) + q[:, 2] * w[2]) / w2
         h = half / math.sqrt(w2)
         a = p + (cp - h)[:, None] * w
         b = p + (cp + h)[:, None] * w

@@ -81,3 +81,21 @@ def test_random_segments_and_edge_cases(cuda_device):
     got = GB300Projectors().line_integrals(torch.as_tensor(vol, dtype=torch.float32, device=cuda_device),
                                            torch.as_tensor(starts), torch.as_tensor(ends), grid)
     assert rel_err(got, siddon.line_integrals(vol, starts, ends, grid)) < 1e-5
+
+
+def test_oblique_line_grazing_a_box_face(cuda_device):
+    """Pixel centres whose float64 z lies just outside a face of the box, with cone directions whose z component is
+    ~1e-17: the lines miss the box in float64 (the reference) and must not integrate the face slice after a float32
+    rounding of the pixel centre."""
+    from citrus_gb300.scatter_image import panel_direction_set
+    grid = Grid((8, 8, 6), 1.0)
+    rng = np.random.default_rng(0)
+    field = rng.random((3, *grid.shape))
+    geo = ConeGeometry(40.0, 60.0, 12, 16, 1.2, 1.2)
+    cone = panel_direction_set(geo, 0.6, (3, 6), max_polar_angle=Grid.covering(grid, 2.0))
+    om = cone.omega[:6]
+    assert np.abs(om[:, 2]).min() < 1e-15
+    ref = siddon.oblique_project(field, grid, geo, 0.6, om)
+    got = GB300Projectors().oblique_project(torch.as_tensor(field, dtype=torch.float32, device=cuda_device), grid,
+                                            geo, 0.6, torch.as_tensor(om, dtype=torch.float32, device=cuda_device))
+    assert rel_err(got, ref) < 1e-5
