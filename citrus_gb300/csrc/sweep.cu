@@ -7,6 +7,7 @@
 // sweep_kernels.py:265-290) and one persistent cooperative launch that walks all planes with a bounded grid barrier
 // between them, so a whole chunk is a single launch.
 #include "common.cuh"
+#include <mutex>
 
 namespace citrus {
 namespace {
@@ -211,4 +212,94 @@ extern "C" int citrus_sweep_persistent(float* store, const float* mu_cells, cons
     default: return launch_persistent<0>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
                                          G, dc, views, sy, max_blocks, t, skip, s);
   }
+}
+
+// ---- allocation-free persistent sweep ----------------------------------------------------------------------------
+//
+// The same persistent launch with its scratch in a file-scope device array instead of caller-provided device memory:
+// the barrier words at [0, 4) and the int32 plane offsets from word 64 (byte 256) on. The call makes no device
+// allocation of any kind; it only clears the barrier words and copies the offsets into the array, both on the stream.
+namespace citrus {
+namespace {
+
+constexpr int64_t kStaticMaxPlanes = 8191;  // R + C + S - 2 <= 8191: every grid up to 2730^3 cells
+constexpr int kStaticOffsetsWord = 64;
+constexpr int kStaticWords = kStaticOffsetsWord + (int)kStaticMaxPlanes + 1;  // 8256 words, 33 KB per device
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) uint32_t g_static_sweep_scratch[kStaticWords];
+
+std::mutex g_static_mutex;
+uint32_t* g_static_address[kStaticMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once per device.
+int static_scratch(uint32_t** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent_static: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kStaticMaxDevices)
+    return set_error(CITRUS_EINVAL, "citrus_sweep_persistent_static: device %d beyond the %d supported", dev,
+                     kStaticMaxDevices);
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (g_static_address[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_sweep_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      return set_error(CITRUS_ECUDA, "citrus_sweep_persistent_static: scratch address on device %d: %s", dev,
+                       cudaGetErrorString(e));
+    g_static_address[dev] = static_cast<uint32_t*>(p);
+  }
+  *out = g_static_address[dev];
+  return CITRUS_OK;
+}
+
+}  // namespace
+}  // namespace citrus
+
+extern "C" int citrus_sweep_persistent_static(float* store, const float* mu_cells, const float* c,
+                                              const int32_t* octant, const int32_t* cell, const int32_t* upstream,
+                                              const int32_t* plane_offsets_host, int64_t num_planes,
+                                              int64_t num_cells, int64_t num_groups, int64_t dc, int64_t views,
+                                              uint32_t* timeout_word, int64_t timeout_ns, void* stream) {
+  int status = check_sweep_args(store, mu_cells, c, octant, cell, upstream, num_planes, num_cells, num_groups, dc,
+                                views);
+  if (status) return status;
+  CITRUS_REQUIRE(plane_offsets_host != nullptr, "citrus_sweep_persistent_static: null plane offsets");
+  CITRUS_REQUIRE(num_planes <= kStaticMaxPlanes,
+                 "citrus_sweep_persistent_static: %lld planes exceed the static scratch (at most %lld planes, "
+                 "R + C + S - 2 <= %lld); use citrus_sweep_persistent with caller scratch",
+                 (long long)num_planes, (long long)kStaticMaxPlanes, (long long)kStaticMaxPlanes);
+  CITRUS_REQUIRE(timeout_ns > 0, "citrus_sweep_persistent_static: timeout_ns must be positive");
+  uint32_t* scratch = nullptr;
+  status = static_scratch(&scratch);
+  if (status) return status;
+  cudaStream_t s = as_stream(stream);
+  int32_t* offsets = reinterpret_cast<int32_t*>(scratch + kStaticOffsetsWord);
+  cudaError_t e = cudaMemcpyAsync(offsets, plane_offsets_host, (size_t)(num_planes + 1) * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess)
+    return set_error(CITRUS_ECUDA, "citrus_sweep_persistent_static: offsets copy: %s", cudaGetErrorString(e));
+  // the barrier words are cleared by the launch below (cudaMemsetAsync on the stream)
+  const int G = (int)num_groups, P = (int)num_planes;
+  const uint64_t t = (uint64_t)timeout_ns;
+  unsigned* sy = reinterpret_cast<unsigned*>(scratch);
+  switch (G) {
+    case 1: status = launch_persistent<1>(store, mu_cells, c, octant, cell, upstream, offsets, P, num_cells, G, dc,
+                                          views, sy, 0, t, -1, s); break;
+    case 2: status = launch_persistent<2>(store, mu_cells, c, octant, cell, upstream, offsets, P, num_cells, G, dc,
+                                          views, sy, 0, t, -1, s); break;
+    case 4: status = launch_persistent<4>(store, mu_cells, c, octant, cell, upstream, offsets, P, num_cells, G, dc,
+                                          views, sy, 0, t, -1, s); break;
+    case 8: status = launch_persistent<8>(store, mu_cells, c, octant, cell, upstream, offsets, P, num_cells, G, dc,
+                                          views, sy, 0, t, -1, s); break;
+    case 16: status = launch_persistent<16>(store, mu_cells, c, octant, cell, upstream, offsets, P, num_cells, G, dc,
+                                            views, sy, 0, t, -1, s); break;
+    default: status = launch_persistent<0>(store, mu_cells, c, octant, cell, upstream, offsets, P, num_cells, G, dc,
+                                           views, sy, 0, t, -1, s); break;
+  }
+  if (status || timeout_word == nullptr) return status;
+  e = cudaMemcpyAsync(timeout_word, scratch + 2, sizeof(uint32_t), cudaMemcpyDefault, s);
+  if (e != cudaSuccess)
+    return set_error(CITRUS_ECUDA, "citrus_sweep_persistent_static: timeout word copy: %s", cudaGetErrorString(e));
+  return CITRUS_OK;
 }

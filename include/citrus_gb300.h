@@ -60,6 +60,20 @@ int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c,
                             int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc, int64_t views,
                             uint32_t* sync, int64_t max_blocks, int64_t timeout_ns, int64_t skip_block, void* stream);
 
+/* The persistent sweep without any allocation: no counterpart in the reference, which always runs the sweep through
+ * torch's allocator. The barrier words and the plane offsets live in a static device array of this library (33 KB
+ * per device, at most 8191 planes, i.e. R + C + S - 2 <= 8191; more planes return CITRUS_EINVAL). The call clears
+ * the barrier words and copies plane_offsets_host [num_planes + 1] (int32, host memory; a pinned buffer must stay
+ * unchanged until the stream reaches the copy) into the array on the stream, then launches. The first call on each
+ * device looks the array's address up (that device must be current); make it before any stream capture. Calls on
+ * one device share the array, so calls that overlap in time (two streams, two host threads) race and must not be
+ * made. timeout_word, when not NULL, receives the barrier error word on the stream (non-zero: a wait ran out and
+ * the store is invalid); a pageable host word makes the call wait for the sweep. */
+int citrus_sweep_persistent_static(float* store, const float* mu_cells, const float* c, const int32_t* octant,
+                                   const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_host,
+                                   int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
+                                   int64_t views, uint32_t* timeout_word, int64_t timeout_ns, void* stream);
+
 /* ------------------------------------------------------------------------------------------------------------------
  * Small-K matrix products of the sweep and of the image.
  * C[b] (=|+=) A @ B[b] with A [M, K] row-major (lda), B[b] [K, J] row-major (ldb), C[b] [M, J] row-major (ldc),
