@@ -40,6 +40,8 @@ def _parse():
     p.add_argument("--method", default="persistent", choices=["persistent", "planes"])
     p.add_argument("--dc", type=int, default=0, help="directions per octant per sweep chunk (0: all)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    p.add_argument("--cells", type=int, default=64, help="cells per axis of the step workload (64; smaller for "
+                                                         "profiling captures)")
     return p.parse_args()
 
 
@@ -53,6 +55,7 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.samples = []
+        self.window = (0.0, float("inf"))
         self._stop = threading.Event()
         self._thread = None
 
@@ -63,7 +66,7 @@ class ClockSampler:
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
                 vals = [v.strip() for v in out.stdout.strip().split(",")]
                 if len(vals) >= 7:
-                    self.samples.append(vals)
+                    self.samples.append([time.monotonic()] + vals)
             except Exception:  # noqa: BLE001
                 pass
             self._stop.wait(0.2)
@@ -77,13 +80,19 @@ class ClockSampler:
         self._stop.set()
         self._thread.join(timeout=10)
 
+    def mark(self, start: float, end: float) -> None:
+        """The timed region, in time.monotonic() seconds: the summary uses the samples inside it."""
+        self.window = (start, end)
+
     def summary(self) -> dict:
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        lo, hi = self.window
+        inside = [s[1:] for s in self.samples if lo <= s[0] <= hi] or [s[1:] for s in self.samples]
+        sm = [float(s[0]) for s in inside if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in inside if s[1].replace(".", "").isdigit()]
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        reasons = sorted({n for s in self.samples for n, v in zip(names, s[3:7]) if v.lower() == "active"})
+        reasons = sorted({n for s in inside for n, v in zip(names, s[3:7]) if v.lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(inside)}
 
 
 def _peaks() -> dict:
@@ -248,6 +257,20 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.workload == "step":
+        cpu_baseline_step(cells=args.cells, image_directions=1, fc_directions=1, sweep_chunks=1, points=1024,
+                          slices=1)  # warm-up (imports, pages, OpenMP threads)
+        runs = [cpu_baseline_step(cells=args.cells, seed=i) for i in range(args.steps)]
+        value = statistics.median(r["value"] for r in runs)
+        base = dict(runs[0], value=value)
+        base["sample"] = f"median of {args.steps} samples; " + base["sample"]
+        line = {"metric": STEP_METRIC, "value": value, "unit": "ms/view", "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+                "dtype": "f64", "data": "synthetic (seeded phantom and library)",
+                "config": {"workload": step_workload_name(args.cells, 60)}, "cpu_baseline": base,
+                "e2e": {"value": value, "unit": "ms/view", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     base = cpu_baseline_sweep(budget_s=max(5.0, 60.0 / max(1, args.steps + args.warmup)))
     line = {"metric": "accumulator sweep cell*dir*group updates/s (scatter-step sweep stage)", "value": base["value"],
             "unit": "updates/s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -258,18 +281,113 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def cpu_baseline_step(cells: int = 64, image_directions: int = 1, fc_directions: int = 1, sweep_chunks: int = 1,
+                      points: int = 4096, slices: int = 2, seed: int = 0) -> dict:
+    """ms/view of the float64 restatement of one view's scatter step, each stage timed on a bounded sample and scaled
+    linearly by its unit count to the whole view: the uncollided fluence (rays to ``points`` of the V quadrature
+    points), the first-collision sampling correction and LD moments (``fc_directions`` of the sweep directions), the
+    accumulator sweep (``sweep_chunks`` of the 15 eight-direction chunks, C with OpenMP, with the numpy source
+    expansion and moment accumulation of those chunks), the two scattering-moment contractions (``slices`` of the
+    z slices) and the collapsed-cone image (``image_directions`` of the panel-facing cone directions). The work does
+    not depend on the values, so the fields between the stages are seeded stand-ins of the right shapes."""
+    import numpy as np
+
+    from citrus_gb300.quadrature import product_quadrature, real_spherical_harmonics
+    from citrus_gb300.responses import ideal_counting_response
+    from citrus_gb300.scatter_image import panel_direction_set
+    from citrus_gb300.workloads import batched_views
+    from oracle import image as oimage, native, physics, siddon, sweep as osweep
+
+    w = batched_views(cells=cells)
+    lib, geo, grid, rho = w.library, w.geometry, w.grid, w.rho
+    G, L, angle = lib.num_groups, w.legendre_order, 0.0
+    N_sh = (L + 1) ** 2
+    V, shape = grid.num_voxels, grid.shape
+    rng = np.random.default_rng(seed)
+    stages = {}
+
+    def timed(name, scale, fn):
+        t0 = time.perf_counter()
+        fn()
+        stages[name] = (time.perf_counter() - t0) * scale
+
+    src = np.asarray(geo.source_position(angle))
+    pts = siddon.centers(grid).reshape(-1, 3)[rng.choice(V, points, replace=False)]
+
+    def uncollided():
+        path = siddon.upstream_to_points(rho, grid, src, pts)
+        d = pts - src
+        return physics.group_transmission(lib, path) * (physics.source_weight(geo, angle, pts) / (d * d).sum(-1))
+
+    timed("uncollided", V / points, uncollided)
+    phi_uc = 1e-4 * (1.0 + rng.random((G, *shape)))
+    q = product_quadrature(w.num_polar, w.num_azimuthal)
+    q = q.reordered(q.by_octant())
+    K_s = q.omega.shape[0]
+    om, wt = q.omega[:fc_directions], q.weight[:fc_directions]
+
+    def first_collision():
+        scale, beta, _, _ = physics.correction(lib, rho, phi_uc, grid, geo, angle, om, wt)
+        physics.first_collision_moments(lib, rho, phi_uc, grid, geo, angle, om, scale, beta, 1)
+
+    timed("first collision", K_s / fc_directions, first_collision)
+    lib_t = lib.truncated(L)
+    transfer = np.einsum("mabl,mijk->ablijk", lib_t.mu_s_l, rho[:, :, :, :slices])
+    acc = 1e-3 * rng.random((G, N_sh, 4, shape[0], shape[1], slices))
+    timed("scattering moments", 2 * shape[2] / slices,
+          lambda: (osweep.scatter_moments(transfer, acc), osweep.scatter_moments(transfer, acc[:, :, 0])))
+    del transfer, acc
+    N = V
+    plan = osweep.plan(shape)
+    mu_cells = np.ascontiguousarray(np.einsum("mg,mijk->gijk", lib.mu_t, rho).reshape(G, N).T)
+    c = (np.abs(q.omega) / np.asarray(grid.deltas)).reshape(8, -1, 3)
+    Y = real_spherical_harmonics(L, q.omega).reshape(8, -1, N_sh)
+    T_cells = 1e-3 * rng.random((N_sh, N * G * 4))
+    moments = np.zeros((N_sh, N * G * 4))
+    Dc = c.shape[1]
+
+    def sweep():
+        for j in range(sweep_chunks):
+            Yc = Y[:, j]                                                   # one direction per octant
+            source = (Yc @ T_cells).reshape(8, 1, N, G, 4)
+            psi = native.sweep_chunk(plan, c[:, j:j + 1], mu_cells, source)
+            moments[...] += Yc.T @ psi.reshape(8, -1)
+
+    timed("sweep", Dc / sweep_chunks, sweep)
+    del T_cells, moments
+    cone = panel_direction_set(geo, angle, (w.cone_num_polar, w.cone_num_azimuthal), max_polar_angle=grid)
+    keep, *_ = oimage.direction_weights(cone.omega, cone.weight, geo, angle, ideal_counting_response(),
+                                        lib.group_energy)
+    kept = np.flatnonzero(keep)
+    pick = kept[:image_directions]
+    T_img = 1e-3 * rng.random((G, N_sh, *shape))
+    mu_t_coarse = np.einsum("mg,mijk->gijk", lib.mu_t, rho)
+    timed("image", kept.size / image_directions,
+          lambda: oimage.combined_image(lib, rho, phi_uc, grid, 1, T_img, L, geo, angle, cone.omega[pick],
+                                        cone.weight[pick], cone.cell_width[pick], mu_t_coarse,
+                                        ideal_counting_response()))
+    total_ms = 1e3 * sum(stages.values())
+    return {"value": total_ms, "unit": "ms/view", "cores": os.cpu_count(), "kind": "port",
+            "stages_ms": {k: round(1e3 * v, 1) for k, v in stages.items()},
+            "sample": (f"one view of batched_views at {cells}^3, float64 oracle: uncollided rays to {points} of {V} "
+                       f"points, first collision at {fc_directions} of {K_s} sweep directions, sweep {sweep_chunks} of "
+                       f"{Dc} chunks (C, OpenMP), moments on {slices} of {shape[2]} slices, image at "
+                       f"{image_directions} of {kept.size} cone directions; each stage scaled linearly to the view "
+                       f"(BLAS and OpenMP stages use every core, numpy elementwise stages one)")}
+
+
 # =====================================================================================================================
 # the scatter step of every view
 # =====================================================================================================================
 
-def make_step_solver(device, views: int = 0):
+def make_step_solver(device, views: int = 0, cells: int = 64):
     """The batched-views workload: solver, fields input, view angles (64^3, G = 8, P5, 120 directions, curved 256 x 192
     panel, cone 16 x 32, ideal counting detector, no grid)."""
     from citrus_gb300.responses import ideal_counting_response, no_grid
     from citrus_gb300.scatter_solver import ScatterSolver, SolverConfig
     from citrus_gb300.workloads import batched_views
 
-    w = batched_views()
+    w = batched_views(cells=cells)
     config = SolverConfig(num_groups=w.library.num_groups, legendre_order=w.legendre_order, num_polar=w.num_polar,
                           num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
                           quadrature_point_spacing_cm=0.5, cone_num_polar=w.cone_num_polar,
@@ -282,9 +400,82 @@ def make_step_solver(device, views: int = 0):
     return w, solver, angles
 
 
+STEP_METRIC = "scatter-step ms/view (all views of one outer iteration; cell*dir*group updates/s alongside)"
+
+
+def step_workload_name(cells: int, views: int) -> str:
+    return (f"batched_views: {cells}^3 cells x {25.6 / cells:g} cm, G=8 (30-120 keV), P5, 120 sweep directions, cone "
+            f"16x32, curved 256x192 panel, {views} views per rank per step, one accumulator sweep per view "
+            f"(citrus_view_step, signal only)")
+
+
+def _dims(address) -> tuple:
+    """The three int64 sizes behind a host-array address handed to the library."""
+    import ctypes
+    arr = ctypes.cast(address, ctypes.POINTER(ctypes.c_int64))
+    return int(arr[0]), int(arr[1]), int(arr[2])
+
+
+def emission_bytes(args) -> int:
+    """Algorithmic bytes of one citrus_attenuated_emission_moments call: every input read once (the densities and
+    fluence of the points, the cells' attenuation, optical depths and scattering-source moments, the harmonics), the
+    emission written once."""
+    M, G, dims, f, k, NS = int(args[1]), int(args[3]), _dims(args[5]), int(args[6]), int(args[14]), int(args[19])
+    V = dims[0] * dims[1] * dims[2]
+    NC = V // (f ** 3)
+    C = 1 if args[21] is not None else G
+    floats = (M + G + 1) * V + G * NC + k * G * NC + NS * G * NC + k * NS + k * G + k * V * C + 2 * k * (-(-V // 32))
+    return 4 * floats
+
+
+def product_emission_bytes(args) -> int:
+    """Algorithmic bytes of one citrus_attenuated_emission call: as the fused form, with the multiple-collision
+    source [K, NC, G] read in place of the moments and harmonics."""
+    M, G, dims, f, k = int(args[1]), int(args[3]), _dims(args[5]), int(args[6]), int(args[14])
+    V = dims[0] * dims[1] * dims[2]
+    NC = V // (f ** 3)
+    C = 1 if args[19] is not None else G
+    floats = (M + G + 1) * V + G * NC + 2 * k * G * NC + k * G + k * V * C + 2 * k * (-(-V // 32))
+    return 4 * floats
+
+
+def downstream_bytes(args) -> int:
+    """citrus_downstream_cumulative: the cell volume read once, the optical depths [K, C, V] written once."""
+    C, dims, K = int(args[1]), _dims(args[3]), int(args[6])
+    V = dims[0] * dims[1] * dims[2]
+    return 4 * (C * V + K * C * V)
+
+
+def sweep_bytes(args) -> int:
+    """citrus_sweep_persistent: 32 B per cell x direction x group update (source moments in, fluence moments out)."""
+    N, G, Dc, views = int(args[8]), int(args[9]), int(args[10]), int(args[11])
+    return 32 * views * 8 * Dc * N * G
+
+
+STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_attenuated_emission": product_emission_bytes,
+              "citrus_downstream_cumulative": downstream_bytes,
+              "citrus_sweep_persistent": sweep_bytes, "citrus_oblique_project": None, "citrus_box_blur": None,
+              "citrus_small_k_gemm": None, "citrus_first_collision_moments": None,
+              "citrus_first_collision_correction": None, "citrus_scattering_moments": None}
+
+
+def count_launches(fn) -> dict:
+    """Kernels launched by ``fn()`` (one untimed step): this library's, from its own launch counter."""
+    import torch
+
+    from citrus_gb300 import _lib
+
+    torch.cuda.synchronize()
+    before = _lib.launch_count()
+    fn()
+    torch.cuda.synchronize()
+    return {"citrus": _lib.launch_count() - before}
+
+
 def run_step(args):
     import torch
 
+    from citrus_gb300 import _lib
     from citrus_gb300.citrus_step import CitrusState, citrus_view_step
 
     rank = int(os.environ.get("RANK", "0"))
@@ -296,7 +487,7 @@ def run_step(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=device)
-    w, solver, angles = make_step_solver(device, args.views)
+    w, solver, angles = make_step_solver(device, args.views, args.cells)
     # weak scaling: every rank runs its own set of views (offset by the rank) of the same phantom
     angles = angles + rank * (2 * math.pi / len(angles)) / max(1, world)
     V = len(angles)
@@ -312,25 +503,37 @@ def run_step(args):
             if signals is not None:
                 signals[v].copy_(scatter, non_blocking=True)
 
-    for _ in range(args.warmup):
-        one_step(rho_dev)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(local)  # started before the warm-up: its first nvidia-smi call is slow
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with sampler:
-        torch.cuda.synchronize()
-        start.record(stream)
-        for _ in range(args.steps):
+        for _ in range(args.warmup):
             one_step(rho_dev)
-        end.record(stream)
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t_start = time.monotonic()
+        with _lib.timed_calls(*STEP_TIMED, capture={n: f for n, f in STEP_TIMED.items() if f}) as calls:
+            start.record(stream)
+            for _ in range(args.steps):
+                one_step(rho_dev)
+            end.record(stream)
+            torch.cuda.synchronize()
+        sampler.mark(t_start, time.monotonic())
     elapsed = start.elapsed_time(end) / 1e3
     if dist:
         t = torch.tensor([elapsed], device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t)
+    # entry points timed inside the timed region (CUDA events on the launch stream); the roofline is reported for
+    # the one with the largest share among those with an algorithmic byte count
+    per_entry = {}
+    for name, recs in calls.items():
+        if recs:
+            per_entry[name] = [a.elapsed_time(b) / 1e3 for _, a, b in recs]
+    ranked = sorted((n for n in per_entry if STEP_TIMED[n] is not None), key=lambda n: -sum(per_entry[n]))
+    top = ranked[0] if ranked else None
+    top_s = per_entry[top] if top else []
+    top_bytes = [info for info, _, _ in calls[top]] if top else []
     # e2e: the densities in from pinned host memory, every view's scatter signal out to pinned host memory
     Rd, Cd = w.geometry.image_shape
     host_signals = torch.empty(V, Rd, Cd, dtype=torch.float32).pin_memory()
@@ -342,24 +545,35 @@ def run_step(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e = e0.elapsed_time(e1) / 1e3
+    launches = count_launches(lambda: one_step(rho_dev))
     ms_per_view = elapsed * 1e3 / (args.steps * V)
     N = w.grid.num_voxels
     updates = 8 * (w.num_polar * w.num_azimuthal // 8) * N * w.library.num_groups
+    peaks = _peaks()
+    achieved = sum(top_bytes) / sum(top_s) / 1e9 if top_s else None
     line = {
-        "metric": "scatter-step ms/view (all views of one outer iteration; cell*dir*group updates/s alongside)",
+        "metric": STEP_METRIC,
         "value": ms_per_view / max(1, world), "unit": "ms/view", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom and library)",
-        "config": {"workload": f"batched_views: 64^3 cells x 0.4 cm, G=8 (30-120 keV), P5, 120 sweep directions, "
-                               f"cone 16x32, curved 256x192 panel, {V} views per rank per step, one accumulator "
-                               f"sweep per view (citrus_view_step, signal only)",
+        "config": {"workload": step_workload_name(args.cells, V),
                    "l2": "inputs larger than L2 (4 GB sweep store per view)"},
         "updates_per_s": updates * V * args.steps * world / elapsed,
         "e2e": {"value": e2e * 1e3 / (args.steps * V) / max(1, world), "unit": "ms/view",
                 "h2d_bytes_per_step": rho_host.numel() * 4, "d2h_bytes_per_step": host_signals.numel() * 4},
+        "gpu_launches": launches["citrus"] * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": None if achieved is None else achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peaks["source"],
+                     "entry_point": top, "launches": len(top_s),
+                     "kernel_ms_mean": 1e3 * statistics.mean(top_s) if top_s else None,
+                     "algorithmic_bytes_per_launch": statistics.mean(top_bytes) if top_bytes else None},
+        "entry_point_ms_per_view": {n: round(1e3 * sum(t) / (args.steps * V), 3)
+                                    for n, t in sorted(per_entry.items(), key=lambda x: -sum(x[1]))},
         "clocks": sampler.summary(),
     }
     if rank == 0:
+        line["cpu_baseline"] = None if args.no_cpu else cpu_baseline_step(cells=args.cells)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -23,6 +23,7 @@ F64 = ctypes.c_double
 # name -> argument types (every entry point returns int status)
 SIGNATURES = {
     "citrus_abi_version": [],
+    "citrus_launch_count": [],
     "citrus_sweep_planes": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P],
     "citrus_sweep_persistent": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, I64, I64, P],
     "citrus_sweep_persistent_static": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, P],
@@ -30,15 +31,18 @@ SIGNATURES = {
     "citrus_scattering_moments": [P, P, P] + [I64] * 14 + [P],
     "citrus_line_integrals": [P, I64, P, P, P, P, I64, P, P],
     "citrus_trace_from_source": [P, I64, P, P, P, P, P, P, P, P, I64, P, P],
-    "citrus_downstream_cumulative": [P, I64, P, P, P, P, I64, P, F64, P, P],
+    "citrus_downstream_cumulative": [P, I64, P, P, P, P, I64, P, F64, P, I64, I64, I64, P, I64, P],
     "citrus_oblique_project": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P],
     "citrus_group_transmission": [P, I64, I64, P, P, P, I64, I64, P, P, P, P, P],
     "citrus_source_weight": [P, P, P, P, P, P, I64, I32, P, P],
     "citrus_first_collision_source": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, I64, P, P],
-    "citrus_first_collision_moments": [P, I64, P, I64, P, P, I64, P, P, I64, F64, F64, P, I64, P, P, P, I64, P],
-    "citrus_first_collision_correction": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, P, I64, P, P, P, P, P],
-    "citrus_attenuated_emission": [P, I64, P, I64, P, P, I64, P, P, P, I64, F64, F64, P, I64, P, P, P, P, P, P, P,
-                                   I64, P, P],
+    "citrus_first_collision_moments": [P, I64, P, I64, P, P, I64, P, P, I64, F64, F64, P, I64, P, P, P, P, P, I64,
+                                       P],
+    "citrus_first_collision_correction": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, P, I64, P, P, P, P, P, P],
+    "citrus_attenuated_emission": [P, I64, P, I64, P, P, I64, P, P, P, I64, F64, F64, P, I64, P, P, I64, P, P, P, P,
+                                   P, P, I64, P, P],
+    "citrus_attenuated_emission_moments": [P, I64, P, I64, P, P, I64, P, P, P, I64, F64, F64, P, I64, P, P, I64, P, P,
+                                           P, I64, P, P, P, P, I64, P, P],
     "citrus_box_blur": [P, P, I64, I64, I64, I64, I64, I64, I64, I64, I64, P, P, P, I32, F64, F64, P],
     "citrus_box_matrix": [P, I64, I64, P, P],
     "citrus_weighted_group_sum": [P, P, I64, I64, I64, I64, I64, P, P],
@@ -67,14 +71,46 @@ def library() -> ctypes.CDLL:
             fn.restype = ctypes.c_int
         lib.citrus_last_error_string.argtypes = []
         lib.citrus_last_error_string.restype = ctypes.c_char_p
+        lib.citrus_launch_count.restype = ctypes.c_int64
         _LIBRARY = lib
     return _LIBRARY
+
+
+_TIMED: Optional[dict] = None
+
+
+class timed_calls:
+    """Context manager that records CUDA events on the current stream around every call of the named entry points:
+    ``records[name]`` is a list of (info, start event, end event), info = ``capture[name](args)`` evaluated during the
+    call (while host arrays behind address arguments are alive), else None. A measurement aid for the benchmark."""
+
+    def __init__(self, *names: str, capture: Optional[dict] = None):
+        self.records = {n: [] for n in names}
+        self.capture = dict(capture or {})
+
+    def __enter__(self):
+        global _TIMED
+        _TIMED = self
+        return self.records
+
+    def __exit__(self, *exc):
+        global _TIMED
+        _TIMED = None
 
 
 def call(name: str, *args) -> None:
     """Call an entry point and raise ``CitrusKernelError`` with the library's message on a non-zero status."""
     lib = library()
-    status = getattr(lib, name)(*args)
+    if _TIMED is not None and name in _TIMED.records:
+        stream = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        status = getattr(lib, name)(*args)
+        e1.record(stream)
+        fn = _TIMED.capture.get(name)
+        _TIMED.records[name].append((fn(args) if fn is not None else None, e0, e1))
+    else:
+        status = getattr(lib, name)(*args)
     if status != 0:
         message = lib.citrus_last_error_string().decode(errors="replace")
         raise CitrusKernelError(f"{name} failed with status {status}: {message}")
@@ -88,3 +124,8 @@ def ptr(t: Optional[torch.Tensor]) -> Optional[int]:
 def stream_handle(device: torch.device) -> int:
     """Raw handle of the current torch stream of ``device``."""
     return torch.cuda.current_stream(device).cuda_stream
+
+
+def launch_count() -> int:
+    """Kernels the library has launched in this process so far."""
+    return int(library().citrus_launch_count())

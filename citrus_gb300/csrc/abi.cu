@@ -1,6 +1,7 @@
 // Status plumbing of the C ABI: the per-thread error message, launch checks and device queries.
 #include <stdarg.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -24,6 +25,10 @@ int launch_status(const char* what) {
   return CITRUS_OK;
 }
 
+static std::atomic<long long> g_launches{0};
+
+void note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 int num_sms() {
   static std::mutex mutex;
   static std::vector<int> cache;
@@ -44,3 +49,5 @@ int num_sms() {
 extern "C" int citrus_abi_version(void) { return CITRUS_GB300_ABI_VERSION; }
 
 extern "C" const char* citrus_last_error_string(void) { return citrus::g_last_error; }
+
+extern "C" int64_t citrus_launch_count(void) { return (int64_t)citrus::g_launches.load(std::memory_order_relaxed); }

@@ -55,12 +55,22 @@ struct Table {
   const float* t;    // [M, N, G, G] transfer by (node, g_out, g_in)
   int M, N, G;
   float eta_lo, eta_hi;
+  float inv_span;    // 1 / (eta_hi - eta_lo) when the span is a power of two (the product is then the quotient), else 0
 };
+
+Table make_table(const float* t, int64_t M, int64_t N, int64_t G, double eta_lo, double eta_hi) {
+  Table tb{t, (int)M, (int)N, (int)G, (float)eta_lo, (float)eta_hi, 0.f};
+  const float span = tb.eta_hi - tb.eta_lo;
+  int e = 0;
+  if (span > 0.f && frexpf(span, &e) == 0.5f) tb.inv_span = ldexpf(1.f, 1 - e);
+  return tb;
+}
 
 // table position of a cosine (cross_sections.py:905-938, uniform table)
 __device__ __forceinline__ void table_position(const Table& tb, float cosine, int& i0, float& w) {
   const float eta = fminf(fmaxf(cosine, tb.eta_lo), tb.eta_hi);
-  const float pos = __fdiv_rn(eta - tb.eta_lo, tb.eta_hi - tb.eta_lo) * (float)(tb.N - 1);
+  const float q = tb.inv_span != 0.f ? (eta - tb.eta_lo) * tb.inv_span : __fdiv_rn(eta - tb.eta_lo, tb.eta_hi - tb.eta_lo);
+  const float pos = q * (float)(tb.N - 1);
   float f0 = floorf(pos);
   f0 = fminf(fmaxf(f0, 0.f), (float)(tb.N - 2));
   i0 = (int)f0;
@@ -354,27 +364,180 @@ __global__ void fc_sums_kernel(FCInputs in, Table tb, PointGrid pg, const float*
 // ---- attenuated total emission of the image ---------------------------------------------------------------------
 // e = (S_FC + S_MC,cell) exp(-max(0, tau_cell - mu_cell omega . (r - r_cell))), written voxel-major [k, V, G] (or the
 // weighted group sum [k, V] with signal weights), and per block the sums of e and e h (h = panel height of the point).
-template <int kG>
-__global__ void emission_kernel(FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, int K,
-                                const float* __restrict__ tau /*[K, G, NC]*/, const float* __restrict__ mu /*[G, NC]*/,
-                                const float* __restrict__ multiple /*[K, G, NC]*/, const float* __restrict__ heights,
-                                const float* __restrict__ signal_weight /*[K, G] or null*/, float dx, float dy,
-                                float dz, float* __restrict__ out, float* __restrict__ partial /*[K, nblocks, 2]*/) {
-  __shared__ float tile[kPoints * kMaxG];
-  __shared__ float red[2][kMaxG][kPoints + 1];
-  const int64_t v = (int64_t)blockIdx.x * kPoints + threadIdx.x;
-  const int go = threadIdx.y;
-  const int G = kG > 0 ? kG : tb.G;
+//
+// A block is 32 points (threadIdx.x) by the G groups (threadIdx.y) by kEmitDirs directions: a warp reads 32
+// consecutive cells of one group (coalesced [K, G, NC] loads), the point's inputs are loaded once for all of the
+// block's directions, and the transfer rows of the eta nodes that the block's points and directions touch are staged
+// in shared memory (the window). S_MC is either read ([K, G, NC], the reference's interface) or formed from the
+// scattering-source moments of the point's cell held in registers, T[n, g, cell] for n < N_sh, and the harmonics of
+// the block's directions in shared memory. The per-block sums are a fixed-order warp butterfly and a fixed-order sum
+// over the groups: deterministic.
+constexpr int kEmitPoints = 32;
+constexpr int kEmitDirs = 16;
+constexpr int kMaxMoments = 64;
+constexpr int kRegMoments = 36;  // scattering-source moments held in registers (P5); more are read per direction
+
+// row . phi over the incoming groups (upscatter entries of the table are zero); the row in global memory (read-only
+// path) or in shared memory
+template <int kGP, bool kShared>
+__device__ __forceinline__ float row_dot(const float* __restrict__ row, const float* phi, int G) {
+  float a = 0.f;
+  if (kGP % 4 == 0 && G == kGP) {
+#pragma unroll
+    for (int q = 0; q < kGP / 4; ++q) {
+      const float4 t = kShared ? reinterpret_cast<const float4*>(row)[q] : __ldg(reinterpret_cast<const float4*>(row) + q);
+      a = fmaf(t.x, phi[4 * q], a);
+      a = fmaf(t.y, phi[4 * q + 1], a);
+      a = fmaf(t.z, phi[4 * q + 2], a);
+      a = fmaf(t.w, phi[4 * q + 3], a);
+    }
+  } else {
+#pragma unroll
+    for (int gi = 0; gi < kGP; ++gi)
+      if (gi < G) a = fmaf(kShared ? row[gi] : __ldg(row + gi), phi[gi], a);
+  }
+  return a;
+}
+
+// The window of table nodes a block needs: its points' cosines with its directions span a few dozen of the eta nodes,
+// so the rows of those nodes ([node][m][g][g'], each (node, m) block padded by 4 floats against bank conflicts) are
+// staged in shared memory once and every interpolation of the block reads them there.
+constexpr int kWindowBytes = 32 * 1024;
+
+__host__ __device__ inline int window_row_stride(int G) { return G * G + 4; }
+__host__ __device__ inline int window_nodes(int M, int G) {
+  const int n = kWindowBytes / (4 * M * window_row_stride(G));
+  return n < 64 ? n : 64;
+}
+
+
+// Stages the table window of a block for the directions s_om[0..n): the eta nodes [lo, hi + 1] that its valid points
+// touch, if they fit, else s_window[0] = -1 (rows read from global memory). Each thread evaluates the directions
+// first_dir, first_dir + dir_step, ... for its point; s_range holds one (lo, hi) per warp. Ends with a block barrier;
+// every thread of the block must call it.
+__device__ void stage_window(const Table& tb, bool valid, float ux, float uy, float uz, const float (*s_om)[3], int n,
+                             int first_dir, int dir_step, int warp, int nwarps, int tid, int nthreads,
+                             int (*s_range)[32], int* s_window, float* s_tab) {
+  const int G = tb.G;
+  int lo = 1 << 30, hi = -1;
+  if (valid) {
+    for (int dd = first_dir; dd < n; dd += dir_step) {
+      int i0;
+      float w;
+      table_position(tb, ux * s_om[dd][0] + uy * s_om[dd][1] + uz * s_om[dd][2], i0, w);
+      lo = min(lo, i0);
+      hi = max(hi, i0);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+  }
+  if ((tid & 31) == 0) {
+    s_range[0][warp] = lo;
+    s_range[1][warp] = hi;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int q = 1; q < nwarps; ++q) {
+      lo = min(lo, s_range[0][q]);
+      hi = max(hi, s_range[1][q]);
+    }
+    const bool fits = hi >= lo && hi + 2 - lo <= window_nodes(tb.M, G);
+    s_window[0] = fits ? lo : -1;
+    s_window[1] = fits ? hi + 2 - lo : 0;
+  }
+  __syncthreads();
+  const int win_lo = s_window[0], win_n = s_window[1];
+  if (win_lo >= 0) {
+    const int RS = window_row_stride(G);
+    const int per = tb.M * G * G;
+    for (int q = tid; q < win_n * per; q += nthreads) {
+      const int node = q / per, rem = q - node * per;
+      const int m = rem / (G * G), r = rem - m * G * G;
+      s_tab[(node * tb.M + m) * RS + r] = __ldg(tb.t + ((int64_t)m * tb.N + win_lo + node) * G * G + r);
+    }
+  }
+  __syncthreads();
+}
+
+// S_FC of group g at one point for one direction, rows from the window (win_lo >= 0) or from global memory
+template <int kGP, int kMM>
+__device__ __forceinline__ float fc_group(const Table& tb, const float* s_tab, int win_lo, int i0, float w, int g,
+                                          const float* rho, const float* phi) {
+  const int G = tb.G, RS = window_row_stride(G);
+  float src = 0.f;
+#pragma unroll
+  for (int m = 0; m < kMM; ++m) {
+    const float r = rho[m];
+    if (m >= tb.M || r == 0.f) continue;
+    float a0, a1;
+    if (win_lo >= 0) {
+      const float* row0 = s_tab + ((i0 - win_lo) * tb.M + m) * RS + g * G;
+      a0 = row_dot<kGP, true>(row0, phi, G);
+      a1 = row_dot<kGP, true>(row0 + tb.M * RS, phi, G);
+    } else {
+      const float* row0 = tb.t + (((int64_t)m * tb.N + i0) * G + g) * G;
+      a0 = row_dot<kGP, false>(row0, phi, G);
+      a1 = row_dot<kGP, false>(row0 + (int64_t)G * G, phi, G);
+    }
+    src = fmaf(r, a0 + (a1 - a0) * w, src);
+  }
+  return src;
+}
+
+template <int kGP, int kMM, bool kFused>
+__global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
+    FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, int K,
+    const float* __restrict__ tau /*[K, NC, G], or [K, NC, TM] path lengths with tau_mu*/,
+    const float* __restrict__ tau_mu /*[TM, G] or null*/, int TM, const float* __restrict__ mu /*[G, NC]*/,
+    const float* __restrict__ multiple /*[K, NC, G], read when not fused*/,
+    const float* __restrict__ harmonics /*[K, NS], fused*/, const float* __restrict__ moments /*[NS, NC, G], fused*/,
+    int NS, const float* __restrict__ heights, const float* __restrict__ signal_weight /*[K, G] or null*/, float dx,
+    float dy, float dz, float* __restrict__ out, float* __restrict__ partial /*[K, nblocks, 2]*/) {
+  constexpr int kPW = 32 / kGP;                 // points per warp
+  constexpr int kWarps = kEmitPoints / kPW;     // = kGP
+  extern __shared__ float4 s_dyn4[];
+  float* s_tab = reinterpret_cast<float*>(s_dyn4);  // the table window (dynamic, kWindowBytes)
+  __shared__ float s_om[kEmitDirs][3];
+  __shared__ __align__(16) float s_y[kFused ? kEmitDirs : 1][kFused ? kMaxMoments : 4];
+  __shared__ float s_sum[kEmitDirs][kWarps][2];   // per-direction, per-warp sums of e and e h
+  __shared__ int s_range[2][32];
+  __shared__ int s_window[2];
+  const int G = tb.G;
+  const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+  const int g = lane % kGP, p = warp * kPW + lane / kGP;   // the thread's group and point of the block
+  const bool gvalid = g < G;
+  const int d0 = blockIdx.y * kEmitDirs;
+  const int nd = min(kEmitDirs, K - d0);
+  constexpr int nthreads = kEmitPoints * kGP;
+  for (int i = tid; i < kEmitDirs * 3; i += nthreads) s_om[i / 3][i % 3] = i < nd * 3 ? omegas[3 * d0 + i] : 0.f;
+  if (kFused)
+    for (int i = tid; i < kEmitDirs * NS; i += nthreads)
+      s_y[i / NS][i % NS] = i < nd * NS ? harmonics[(int64_t)d0 * NS + i] : 0.f;
+
+  const int64_t v = (int64_t)blockIdx.x * kEmitPoints + p;
   const bool valid = v < in.V;
   const int64_t NC = (int64_t)pg.Rc * pg.Cc * pg.Sc;
-  float rho[kMaxM], phi[kG > 0 ? kG : kMaxG];
-  float ux = 0.f, uy = 0.f, uz = 0.f, h = 0.f, muc = 0.f, offx = 0.f, offy = 0.f, offz = 0.f;
+  float rho[kMM], phi[kGP];
+  float ux = 0.f, uy = 0.f, uz = 0.f, h = 0.f, offx = 0.f, offy = 0.f, offz = 0.f, muc = 0.f;
   int64_t cell = 0;
+#pragma unroll
+  for (int q = 0; q < kGP; ++q) phi[q] = 0.f;
+#pragma unroll
+  for (int m = 0; m < kMM; ++m) rho[m] = 0.f;
+  float tmom[kFused ? kRegMoments : 1];
   if (valid) {
     int i, j, k;
     point_rcs(v, pg, i, j, k);
     primary_direction(__ldg(in.ax_x + j), __ldg(in.ax_y + i), __ldg(in.ax_z + k), in.r0x, in.r0y, in.r0z, ux, uy, uz);
-    load_point<kG>(in, tb, v, rho, phi);
+#pragma unroll
+    for (int m = 0; m < kMM; ++m)
+      if (m < tb.M) rho[m] = __ldg(in.rho + (int64_t)m * in.V + v);
+#pragma unroll
+    for (int q = 0; q < kGP; ++q)
+      if (q < G) phi[q] = __ldg(in.phi + (int64_t)q * in.V + v);
     const int F = pg.f, ic = i / F, jc = j / F, kc = k / F;
     cell = ((int64_t)ic * pg.Cc + jc) * pg.Sc + kc;
     const float half = (F - 1) * 0.5f;
@@ -382,48 +545,290 @@ __global__ void emission_kernel(FCInputs in, Table tb, PointGrid pg, const float
     offx = dx * ((float)(j - jc * F) - half);
     offz = dz * ((float)(k - kc * F) - half);
     h = heights ? __ldg(heights + v) : 0.f;
-    muc = __ldg(mu + (int64_t)go * NC + cell);
+    if (gvalid) muc = __ldg(mu + (int64_t)g * NC + cell);
   }
-  const int64_t base_v = (int64_t)blockIdx.x * kPoints;
-  const int npts = (int)min((int64_t)kPoints, in.V - base_v);
-  const int KB = (K + gridDim.y - 1) / gridDim.y;
-  for (int kb = 0; kb < KB; ++kb) {
-    const int d = blockIdx.y * KB + kb;
-    if (d >= K) break;
+  float tmu[kMM];  // the group's attenuation per traced material, when tau holds material path lengths
+#pragma unroll
+  for (int m = 0; m < kMM; ++m) tmu[m] = (tau_mu != nullptr && m < TM && gvalid) ? __ldg(tau_mu + m * G + g) : 0.f;
+  if (kFused) {
+#pragma unroll
+    for (int n = 0; n < (kFused ? kRegMoments : 1); ++n)
+      tmom[n] = (valid && gvalid && n < NS) ? __ldg(moments + ((int64_t)n * NC + cell) * G + g) : 0.f;
+  }
+  __syncthreads();  // s_om and s_y are complete
+  stage_window(tb, valid, ux, uy, uz, s_om, nd, g, kGP, warp, kWarps, tid, nthreads, s_range, s_window, s_tab);
+  const int win_lo = s_window[0];
+
+  for (int dd = 0; dd < nd; ++dd) {
+    const int d = d0 + dd;
     float e = 0.f;
-    if (valid) {
-      const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+    if (valid && gvalid) {
+      const float ox = s_om[dd][0], oy = s_om[dd][1], oz = s_om[dd][2];
       const float cosine = ux * ox + uy * oy + uz * oz;
       int i0;
       float w;
       table_position(tb, cosine, i0, w);
-      const float src = fc_value<kG>(tb, i0, w, go, rho, phi);
-      const int64_t kc = ((int64_t)d * G + go) * NC + cell;
       const float offset = oy * offy + ox * offx + oz * offz;
-      const float depth = fmaxf(__ldg(tau + kc) - muc * offset, 0.f);
-      e = (src + __ldg(multiple + kc)) * expf(-depth);
+      const float src = fc_group<kGP, kMM>(tb, s_tab, win_lo, i0, w, g, rho, phi);
+      const int64_t kc = ((int64_t)d * NC + cell) * G + g;
+      float smc = 0.f;
+      if (kFused) {
+#pragma unroll
+        for (int n = 0; n < (kFused ? kRegMoments : 1); n += 4) {
+          const float4 y = *reinterpret_cast<const float4*>(&s_y[kFused ? dd : 0][n]);
+          smc = fmaf(y.x, tmom[n], smc);
+          if (n + 1 < kRegMoments) smc = fmaf(y.y, tmom[n + 1], smc);
+          if (n + 2 < kRegMoments) smc = fmaf(y.z, tmom[n + 2], smc);
+          if (n + 3 < kRegMoments) smc = fmaf(y.w, tmom[n + 3], smc);
+        }
+        for (int n = kRegMoments; n < NS; ++n)
+          smc = fmaf(s_y[kFused ? dd : 0][n], __ldg(moments + ((int64_t)n * NC + cell) * G + g), smc);
+      } else {
+        smc = __ldg(multiple + kc);
+      }
+      float t;
+      if (tau_mu != nullptr) {  // sum_m mu[m, g] P_m, in material order
+        const float* pm = tau + ((int64_t)d * NC + cell) * TM;
+        t = 0.f;
+#pragma unroll
+        for (int m = 0; m < kMM; ++m)
+          if (m < TM) t = fmaf(tmu[m], __ldg(pm + m), t);
+      } else {
+        t = __ldg(tau + kc);
+      }
+      const float depth = fmaxf(t - muc * offset, 0.f);
+      e = (src + smc) * expf(-depth);
+    }
+    // group sums over the kGP lanes of the point (in group order), then the warp's points
+    float tot = e, sgl = signal_weight != nullptr && valid && gvalid ? __ldg(signal_weight + (int64_t)d * G + g) * e : 0.f;
+#pragma unroll
+    for (int off = 1; off < kGP; off <<= 1) {
+      tot += __shfl_xor_sync(0xffffffffu, tot, off);
+      sgl += __shfl_xor_sync(0xffffffffu, sgl, off);
+    }
+    if (signal_weight != nullptr) {
+      if (g == 0 && valid) out[(int64_t)d * in.V + v] = sgl;
+    } else if (valid && gvalid) {
+      out[((int64_t)d * in.V + v) * G + g] = e;
+    }
+    float a = (g == 0) ? tot : 0.f, b = (g == 0) ? tot * h : 0.f;
+#pragma unroll
+    for (int off = kGP; off < 32; off <<= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, off);
+      b += __shfl_xor_sync(0xffffffffu, b, off);
+    }
+    if (lane == 0) {
+      s_sum[dd][warp][0] = a;
+      s_sum[dd][warp][1] = b;
+    }
+  }
+  __syncthreads();
+  if (tid < 2 * nd) {
+    const int dd = tid / 2, which = tid % 2;
+    float acc = 0.f;
+    for (int q = 0; q < kWarps; ++q) acc += s_sum[dd][q][which];
+    partial[((int64_t)(d0 + dd) * gridDim.x + blockIdx.x) * 2 + which] = acc;
+  }
+}
+
+// ---- sampling correction over the sweep directions, with the source values kept -----------------------------------
+// A block is 32 points by the G groups and walks all K sweep directions, in the order of their cosine with the
+// block's first point so that each batch of kFcBatch directions touches few table nodes (the window); it sums
+// I0, I1, I2 per (point, group), stores S_FC(direction, group, point) in cache [K, G, V] when given (the LD moments
+// of the sweep's source read it back instead of evaluating the table again), and forms E0, E1 and the float64
+// factors as the reference does.
+constexpr int kFcBatch = 16;
+constexpr int kMaxSorted = 1024;
+
+template <int kGP, int kMM>
+__global__ void __launch_bounds__(kEmitPoints * kGP) fc_correction_kernel(
+    FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, const float* __restrict__ weights, int K,
+    const float* __restrict__ moments /*[M, 2, G, G]*/, float* __restrict__ sums /*[5, G, V] or null*/,
+    float* __restrict__ scale, float* __restrict__ beta, float* __restrict__ cache /*[K, G, V] or null*/) {
+  extern __shared__ float4 s_dyn4[];
+  float* s_tab = reinterpret_cast<float*>(s_dyn4);
+  __shared__ float s_key[kMaxSorted];
+  __shared__ int s_order[kMaxSorted];
+  __shared__ float s_om[kFcBatch][3];
+  __shared__ float s_w[kFcBatch];
+  __shared__ int s_d[kFcBatch];
+  __shared__ int s_range[2][32];
+  __shared__ int s_window[2];
+  __shared__ float s_u0[3];
+  const int G = tb.G;
+  const int g = threadIdx.y, lane = threadIdx.x;
+  const int nthreads = kEmitPoints * G, tid = g * kEmitPoints + lane;
+  const int64_t v = (int64_t)blockIdx.x * kEmitPoints + lane;
+  const bool valid = v < in.V;
+  float rho[kMM], phi[kGP];
+  float ux = 0.f, uy = 0.f, uz = 0.f;
+#pragma unroll
+  for (int q = 0; q < kGP; ++q) phi[q] = 0.f;
+#pragma unroll
+  for (int m = 0; m < kMM; ++m) rho[m] = 0.f;
+  if (valid) {
+    int i, j, k;
+    point_rcs(v, pg, i, j, k);
+    primary_direction(__ldg(in.ax_x + j), __ldg(in.ax_y + i), __ldg(in.ax_z + k), in.r0x, in.r0y, in.r0z, ux, uy, uz);
+#pragma unroll
+    for (int m = 0; m < kMM; ++m)
+      if (m < tb.M) rho[m] = __ldg(in.rho + (int64_t)m * in.V + v);
+#pragma unroll
+    for (int q = 0; q < kGP; ++q)
+      if (q < G) phi[q] = __ldg(in.phi + (int64_t)q * in.V + v);
+  }
+  // exact l = 0, 1 moments of the source (downscatter rows of the moment table)
+  float E0 = 0.f, E1 = 0.f;
+  for (int m = 0; m < tb.M; ++m) {
+    const float* r0 = moments + (((int64_t)m * 2 + 0) * G + g) * G;
+    const float* r1 = moments + (((int64_t)m * 2 + 1) * G + g) * G;
+    float a0 = 0.f, a1 = 0.f;
+    for (int gi = 0; gi <= g; ++gi) {
+      a0 = fmaf(__ldg(r0 + gi), phi[gi < kGP ? gi : 0], a0);
+      a1 = fmaf(__ldg(r1 + gi), phi[gi < kGP ? gi : 0], a1);
+    }
+    E0 = fmaf(rho[m], a0, E0);
+    E1 = fmaf(rho[m], a1, E1);
+  }
+  // directions in the order of their cosine with the block's first point
+  if (tid == 0) {
+    s_u0[0] = ux;
+    s_u0[1] = uy;
+    s_u0[2] = uz;
+  }
+  __syncthreads();
+  const bool sorted = K <= kMaxSorted;
+  if (sorted) {
+    for (int d = tid; d < K; d += nthreads)
+      s_key[d] = s_u0[0] * __ldg(omegas + 3 * d) + s_u0[1] * __ldg(omegas + 3 * d + 1) +
+                 s_u0[2] * __ldg(omegas + 3 * d + 2);
+    __syncthreads();
+    for (int d = tid; d < K; d += nthreads) {
+      const float key = s_key[d];
+      int rank = 0;
+      for (int q = 0; q < K; ++q) {
+        const float other = s_key[q];
+        rank += (other < key) || (other == key && q < d);
+      }
+      s_order[rank] = d;
     }
     __syncthreads();
-    red[0][go][threadIdx.x] = e;
-    red[1][go][threadIdx.x] = e * h;
-    if (signal_weight == nullptr) tile[threadIdx.x * G + go] = e;
+  }
+  float I0 = 0.f, I1 = 0.f, I2 = 0.f;
+  for (int b0 = 0; b0 < K; b0 += kFcBatch) {
+    const int nb = min(kFcBatch, K - b0);
+    if (tid < nb) {
+      const int d = sorted ? s_order[b0 + tid] : b0 + tid;
+      s_d[tid] = d;
+      s_om[tid][0] = __ldg(omegas + 3 * d);
+      s_om[tid][1] = __ldg(omegas + 3 * d + 1);
+      s_om[tid][2] = __ldg(omegas + 3 * d + 2);
+      s_w[tid] = __ldg(weights + d);
+    }
     __syncthreads();
-    if (signal_weight == nullptr) {
-      // the block's [points, G] tile is contiguous in the voxel-major output
-      float* o = out + ((int64_t)d * in.V + base_v) * G;
-      for (int q = threadIdx.y * kPoints + threadIdx.x; q < npts * G; q += kPoints * G) o[q] = tile[q];
-    } else if (threadIdx.y == 0 && valid) {
-      float s = 0.f;
-      for (int g = 0; g < G; ++g) s = fmaf(__ldg(signal_weight + (int64_t)d * G + g), red[0][g][threadIdx.x], s);
-      out[(int64_t)d * in.V + v] = s;
+    stage_window(tb, valid, ux, uy, uz, s_om, nb, g, G, g, G, tid, nthreads, s_range, s_window, s_tab);
+    const int win_lo = s_window[0];
+    if (valid) {
+      for (int i = 0; i < nb; ++i) {
+        const float cosine = ux * s_om[i][0] + uy * s_om[i][1] + uz * s_om[i][2];
+        int i0;
+        float w;
+        table_position(tb, cosine, i0, w);
+        const float S = fc_group<kGP, kMM>(tb, s_tab, win_lo, i0, w, g, rho, phi);
+        const float ws = S * s_w[i];
+        I0 += ws;
+        I1 += ws * cosine;
+        I2 += ws * (cosine * cosine);
+        if (cache != nullptr) cache[((int64_t)s_d[i] * G + g) * in.V + v] = S;
+      }
     }
-    if (threadIdx.y == 0 && threadIdx.x < 2) {  // fixed-order block sums: deterministic
-      const int which = threadIdx.x;
-      float s = 0.f;
-      for (int g = 0; g < G; ++g)
-        for (int p = 0; p < kPoints; ++p) s += red[which][g][p];
-      partial[((int64_t)d * gridDim.x + blockIdx.x) * 2 + which] = s;
+    __syncthreads();  // the batch's directions and window are replaced next
+  }
+  if (!valid) return;
+  const int64_t gv = (int64_t)g * in.V + v;
+  if (sums) {
+    const int64_t GV = (int64_t)G * in.V;
+    sums[gv] = I0;
+    sums[GV + gv] = I1;
+    sums[2 * GV + gv] = I2;
+    sums[3 * GV + gv] = E0;
+    sums[4 * GV + gv] = E1;
+  }
+  // factors in float64 (uncollided.py:611-636)
+  const double i0d = I0, i1d = I1, i2d = I2, e0 = E0, e1 = E1;
+  const bool pos = e0 > 0;
+  const double c = pos ? e1 / e0 : 0.0;
+  const double den = i2d - c * i1d;
+  const bool ok = pos && fabs(den) > 1e-12 * fabs(i0d);
+  double b = ok ? (c * i0d - i1d) / den : 0.0;
+  b = fmin(fmax(b, -1.0), 1.0);
+  const double d0 = i0d + b * i1d;
+  scale[gv] = (float)(d0 > 0 ? e0 / d0 : 1.0);
+  beta[gv] = (float)b;
+}
+
+// ---- LD moments of the corrected source from the kept source values ---------------------------------------------
+// A block is 32 cells by the G groups by kFcBatch directions of the chunk: S_FC read from cache [K, G, V] at the
+// chunk direction's cache_index, corrected (scale (1 + beta cos)) and restricted to the cell's LD moments; the
+// block's [cells, G, 4] tile goes out through shared memory as contiguous float4 rows.
+template <int kGP>
+__global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
+    FCInputs in, PointGrid pg, const float* __restrict__ omegas, int K, const float* __restrict__ cache,
+    const int32_t* __restrict__ cache_index, const float* __restrict__ scale, const float* __restrict__ beta,
+    float slope_scale, float* __restrict__ out, int64_t out_k_stride) {
+  __shared__ float4 s_tile[kEmitPoints * kGP];
+  const int G = (int)(blockDim.y);
+  const int g = threadIdx.y, lane = threadIdx.x;
+  const int nthreads = kEmitPoints * G, tid = g * kEmitPoints + lane;
+  const int64_t NC = (int64_t)pg.Rc * pg.Cc * pg.Sc;
+  const int64_t c0 = (int64_t)blockIdx.x * kEmitPoints;
+  const int64_t c = c0 + lane;
+  const int ncells = (int)min((int64_t)kEmitPoints, NC - c0);
+  const bool valid = c < NC;
+  const int F = pg.f;
+  int ic = 0, jc = 0, kc = 0;
+  if (valid) {
+    const int64_t csc = (int64_t)pg.Cc * pg.Sc;
+    ic = (int)(c / csc);
+    jc = (int)((c - (int64_t)ic * csc) / pg.Sc);
+    kc = (int)(c - (int64_t)ic * csc - (int64_t)jc * pg.Sc);
+  }
+  const float inv = 1.f / (float)(F * F * F);
+  const int dlast = min(K, (int)(blockIdx.y + 1) * kFcBatch);
+  for (int d = blockIdx.y * kFcBatch; d < dlast; ++d) {
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+      const float* src = cache + (int64_t)__ldg(cache_index + d) * G * in.V + (int64_t)g * in.V;
+      float m0 = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+      for (int a = 0; a < F; ++a) {      // rows (y)
+        for (int b = 0; b < F; ++b) {    // cols (x)
+          for (int e = 0; e < F; ++e) {  // slices (z)
+            const int i = ic * F + a, j = jc * F + b, k = kc * F + e;
+            const int64_t v = ((int64_t)i * pg.C + j) * pg.S + k;
+            float ux, uy, uz;
+            primary_direction(__ldg(in.ax_x + j), __ldg(in.ax_y + i), __ldg(in.ax_z + k), in.r0x, in.r0y, in.r0z,
+                              ux, uy, uz);
+            const float cosine = ux * ox + uy * oy + uz * oz;
+            const int64_t gv = (int64_t)g * in.V + v;
+            const float s = __ldg(src + v) * __ldg(scale + gv) * (1.f + __ldg(beta + gv) * cosine);
+            m0 += s;
+            mx += s * ((2.f * b + 1.f) / F - 1.f);
+            my += s * ((2.f * a + 1.f) / F - 1.f);
+            mz += s * ((2.f * e + 1.f) / F - 1.f);
+          }
+        }
+      }
+      r.x = m0 * inv;
+      r.y = mx * (inv * slope_scale);
+      r.z = my * (inv * slope_scale);
+      r.w = mz * (inv * slope_scale);
     }
+    s_tile[lane * G + g] = r;
+    __syncthreads();
+    float4* o = reinterpret_cast<float4*>(out + d * out_k_stride + c0 * G * 4);
+    for (int q = tid; q < ncells * G; q += nthreads) o[q] = s_tile[q];
+    __syncthreads();
   }
 }
 
@@ -486,7 +891,8 @@ PointGrid make_grid(const int64_t* pdims, int64_t f) {
     case 8: KERNEL<8><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;                    \
     case 16: KERNEL<16><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;                  \
     default: KERNEL<0><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;                   \
-  }
+  }                                                                                           \
+  note_launches();
 
 }  // namespace
 }  // namespace citrus
@@ -512,6 +918,7 @@ extern "C" int citrus_group_transmission(const float* path, int64_t num_material
   transmission_kernel<<<(unsigned)cdiv(num_points, 128), 128, smem, as_stream(stream)>>>(
       path, (int)num_materials, num_points, fine_mu, fine_weight, fine_group, (int)num_fine, (int)num_groups,
       filter_path, filter_mu, factor, out);
+  note_launches();
   return launch_status("citrus_group_transmission");
 }
 
@@ -544,6 +951,7 @@ extern "C" int citrus_source_weight(const double* field, const double* points, c
   if (num_points == 0) return CITRUS_OK;
   source_weight_kernel<<<(unsigned)cdiv(num_points, 128), 128, 0, as_stream(stream)>>>(
       fd, points, axis_x, axis_y, axis_z, gc, gs, num_points, divide_by_distance_squared, out);
+  note_launches();
   return launch_status("citrus_source_weight");
 }
 
@@ -559,7 +967,7 @@ extern "C" int citrus_first_collision_source(const float* rho, int64_t num_mater
   const int64_t V = point_dims[0] * point_dims[1] * point_dims[2];
   if (V == 0 || num_directions == 0) return CITRUS_OK;
   const FCInputs in = make_inputs(rho, phi, axes, V, focal_spot, point_dims);
-  const Table tb{table, (int)num_materials, (int)num_eta, (int)num_groups, (float)eta_lo, (float)eta_hi};
+  const Table tb = make_table(table, num_materials, num_eta, num_groups, eta_lo, eta_hi);
   const PointGrid pg = make_grid(point_dims, 1);
   const int G = (int)num_groups, K = (int)num_directions, KB = 4;
   dim3 grid((unsigned)cdiv(V, kPoints), (unsigned)cdiv(K, KB)), block(kPoints, G);
@@ -567,16 +975,64 @@ extern "C" int citrus_first_collision_source(const float* rho, int64_t num_mater
   return launch_status("citrus_first_collision_source");
 }
 
+namespace citrus {
+namespace {
+
+template <int kGP, int kMM>
+int launch_fc_correction_m(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const Table& tb,
+                           const PointGrid& pg, const float* omegas, const float* weights, int K,
+                           const float* moments, float* sums, float* scale, float* beta, float* cache) {
+  cudaError_t e = cudaFuncSetAttribute(fc_correction_kernel<kGP, kMM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kWindowBytes);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "first-collision window: %s", cudaGetErrorString(e));
+  fc_correction_kernel<kGP, kMM><<<grid, dim3(kEmitPoints, G), kWindowBytes, s>>>(in, tb, pg, omegas, weights, K,
+                                                                                 moments, sums, scale, beta, cache);
+  note_launches();
+  return CITRUS_OK;
+}
+
+// materials held in registers: two (the common water and bone case) or up to eight
+template <int kGP>
+int launch_fc_correction(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                         const float* omegas, const float* weights, int K, const float* moments, float* sums,
+                         float* scale, float* beta, float* cache) {
+  if (tb.M <= 2)
+    return launch_fc_correction_m<kGP, 2>(grid, G, s, in, tb, pg, omegas, weights, K, moments, sums, scale, beta,
+                                          cache);
+  return launch_fc_correction_m<kGP, kMaxM>(grid, G, s, in, tb, pg, omegas, weights, K, moments, sums, scale, beta,
+                                            cache);
+}
+
+template <int kGP>
+void launch_fc_moments_cached(int64_t NC, int G, int K, cudaStream_t s, const FCInputs& in, const PointGrid& pg,
+                              const float* omegas, const float* cache, const int32_t* cache_index,
+                              const float* scale, const float* beta, float slope_scale, float* out,
+                              int64_t out_k_stride) {
+  dim3 grid((unsigned)cdiv(NC, kEmitPoints), (unsigned)cdiv(K, kFcBatch));
+  fc_moments_cached_kernel<kGP><<<grid, dim3(kEmitPoints, G), 0, s>>>(in, pg, omegas, K, cache, cache_index, scale,
+                                                                      beta, slope_scale, out, out_k_stride);
+  note_launches();
+}
+
+}  // namespace
+}  // namespace citrus
+
+#define CITRUS_GP_DISPATCH(G, CALL) \
+  ((G) <= 1 ? CALL(1) : (G) <= 2 ? CALL(2) : (G) <= 4 ? CALL(4) : (G) <= 8 ? CALL(8) : (G) <= 16 ? CALL(16) : CALL(32))
+
 extern "C" int citrus_first_collision_moments(const float* rho, int64_t num_materials, const float* phi,
                                               int64_t num_groups, const float* axes, const int64_t* point_dims,
                                               int64_t points_per_cell, const double* focal_spot, const float* table,
                                               int64_t num_eta, double eta_lo, double eta_hi, const float* omegas,
                                               int64_t num_directions, const float* scale, const float* beta,
-                                              float* out, int64_t out_direction_stride, void* stream) {
+                                              const float* cache, const int32_t* cache_index, float* out,
+                                              int64_t out_direction_stride, void* stream) {
   int st = check_table(table, num_materials, num_eta, num_groups);
   if (st) return st;
   CITRUS_REQUIRE(rho && phi && axes && point_dims && focal_spot && omegas && scale && beta && out,
                  "citrus_first_collision_moments: null pointer");
+  CITRUS_REQUIRE((cache == nullptr) == (cache_index == nullptr),
+                 "citrus_first_collision_moments: cache and cache_index go together");
   const int64_t f = points_per_cell;
   CITRUS_REQUIRE(f >= 1 && point_dims[0] % f == 0 && point_dims[1] % f == 0 && point_dims[2] % f == 0,
                  "citrus_first_collision_moments: the point grid is not cells x %lld", (long long)f);
@@ -586,7 +1042,7 @@ extern "C" int citrus_first_collision_moments(const float* rho, int64_t num_mate
   const int64_t V = point_dims[0] * point_dims[1] * point_dims[2];
   if (V == 0 || num_directions == 0) return CITRUS_OK;
   const FCInputs in = make_inputs(rho, phi, axes, V, focal_spot, point_dims);
-  const Table tb{table, (int)num_materials, (int)num_eta, (int)num_groups, (float)eta_lo, (float)eta_hi};
+  const Table tb = make_table(table, num_materials, num_eta, num_groups, eta_lo, eta_hi);
   const PointGrid pg = make_grid(point_dims, f);
   double mean_u2 = 0;
   for (int j = 0; j < f; ++j) {
@@ -596,9 +1052,18 @@ extern "C" int citrus_first_collision_moments(const float* rho, int64_t num_mate
   const float slope_scale = f > 1 ? (float)(1.0 / mean_u2) : 0.f;
   const int64_t NC = V / (f * f * f);
   const int G = (int)num_groups, K = (int)num_directions;
+  cudaStream_t s = as_stream(stream);
+  if (cache != nullptr) {
+#define CITRUS_FCM(GP) \
+  (launch_fc_moments_cached<GP>(NC, G, K, s, in, pg, omegas, cache, cache_index, scale, beta, slope_scale, out, \
+                                out_direction_stride), 0)
+    (void)CITRUS_GP_DISPATCH(G, CITRUS_FCM);
+#undef CITRUS_FCM
+    return launch_status("citrus_first_collision_moments");
+  }
   dim3 grid((unsigned)cdiv(NC, kPoints), (unsigned)K), block(kPoints, G);
-  CITRUS_G_DISPATCH(G, fc_moments_kernel, grid, block, 0, as_stream(stream), in, tb, pg, omegas, K, scale, beta,
-                    slope_scale, out, out_direction_stride)
+  CITRUS_G_DISPATCH(G, fc_moments_kernel, grid, block, 0, s, in, tb, pg, omegas, K, scale, beta, slope_scale, out,
+                    out_direction_stride)
   return launch_status("citrus_first_collision_moments");
 }
 
@@ -607,57 +1072,167 @@ extern "C" int citrus_first_collision_correction(const float* rho, int64_t num_m
                                                  const double* focal_spot, const float* table, int64_t num_eta,
                                                  double eta_lo, double eta_hi, const float* omegas,
                                                  const float* weights, int64_t num_directions, const float* moments,
-                                                 float* sums, float* scale, float* beta, void* stream) {
+                                                 float* sums, float* scale, float* beta, float* cache, void* stream) {
   int st = check_table(table, num_materials, num_eta, num_groups);
   if (st) return st;
   CITRUS_REQUIRE(rho && phi && axes && point_dims && focal_spot && omegas && weights && moments && scale && beta,
                  "citrus_first_collision_correction: null pointer");
+  if (num_groups % 4 == 0)
+    CITRUS_REQUIRE(((uintptr_t)table % 16) == 0, "citrus_first_collision_correction: table must be 16-byte aligned");
   const int64_t V = point_dims[0] * point_dims[1] * point_dims[2];
   if (V == 0) return CITRUS_OK;
   const FCInputs in = make_inputs(rho, phi, axes, V, focal_spot, point_dims);
-  const Table tb{table, (int)num_materials, (int)num_eta, (int)num_groups, (float)eta_lo, (float)eta_hi};
+  const Table tb = make_table(table, num_materials, num_eta, num_groups, eta_lo, eta_hi);
   const PointGrid pg = make_grid(point_dims, 1);
   const int G = (int)num_groups, K = (int)num_directions;
-  dim3 grid((unsigned)cdiv(V, kPoints)), block(kPoints, G);
-  CITRUS_G_DISPATCH(G, fc_sums_kernel, grid, block, 0, as_stream(stream), in, tb, pg, omegas, weights, K, moments,
-                    sums, scale, beta)
+  dim3 grid((unsigned)cdiv(V, kEmitPoints));
+  cudaStream_t s = as_stream(stream);
+#define CITRUS_FCC(GP) launch_fc_correction<GP>(grid, G, s, in, tb, pg, omegas, weights, K, moments, sums, scale, beta, cache)
+  st = CITRUS_GP_DISPATCH(G, CITRUS_FCC);
+#undef CITRUS_FCC
+  if (st) return st;
   return launch_status("citrus_first_collision_correction");
 }
+
+namespace citrus {
+namespace {
+
+template <int kGP, int kMM, bool kFused>
+int launch_emission_m(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                      const float* omegas, int K, const float* tau, const float* tau_mu, int TM, const float* mu,
+                      const float* multiple, const float* harmonics, const float* moments, int NS,
+                      const float* heights, const float* signal_weight, const double* deltas, float* out,
+                      float* partial) {
+  cudaError_t e = cudaFuncSetAttribute(emission_kernel<kGP, kMM, kFused>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kWindowBytes);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "emission window: %s", cudaGetErrorString(e));
+  emission_kernel<kGP, kMM, kFused><<<grid, kEmitPoints * kGP, kWindowBytes, s>>>(
+      in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, harmonics, moments, NS, heights, signal_weight, (float)deltas[0],
+      (float)deltas[1], (float)deltas[2], out, partial);
+  note_launches();
+  return CITRUS_OK;
+}
+
+template <int kGP, bool kFused>
+int launch_emission(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                    const float* omegas, int K, const float* tau, const float* tau_mu, int TM, const float* mu,
+                    const float* multiple, const float* harmonics, const float* moments, int NS,
+                    const float* heights, const float* signal_weight, const double* deltas, float* out,
+                    float* partial) {
+  if (tb.M <= 2 && TM <= 2)
+    return launch_emission_m<kGP, 2, kFused>(grid, G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                             harmonics, moments, NS, heights, signal_weight, deltas, out, partial);
+  return launch_emission_m<kGP, kMaxM, kFused>(grid, G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                               harmonics, moments, NS, heights, signal_weight, deltas, out, partial);
+}
+
+template <int kGP>
+int emission_for(int64_t V, int K, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                 const float* omegas, const float* tau, const float* tau_mu, int TM, const float* mu,
+                 const float* multiple,
+                 const float* harmonics, const float* moments, int NS, const float* heights,
+                 const float* signal_weight, const double* deltas, float* out, float* partial,
+                 float* height_sums) {
+  const int64_t nblocks = cdiv(V, kEmitPoints);
+  dim3 grid((unsigned)nblocks, (unsigned)cdiv(K, kEmitDirs));
+  const int st = moments != nullptr
+                     ? launch_emission<kGP, true>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
+                                                  multiple, harmonics, moments, NS, heights, signal_weight, deltas,
+                                                  out, partial)
+                     : launch_emission<kGP, false>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
+                                                   multiple, harmonics, moments, NS, heights, signal_weight, deltas,
+                                                   out, partial);
+  if (st) return st;
+  reduce_partials_kernel<<<K, dim3(256, 2), 0, s>>>(partial, nblocks, K, height_sums);
+  note_launches();
+  return CITRUS_OK;
+}
+
+// shared by the two entry points: multiple [K, G, NC] (moments NULL), or harmonics [K, NS] and moments [NS, G, NC]
+int attenuated_emission(const char* name, const float* rho, int64_t num_materials, const float* phi,
+                        int64_t num_groups, const float* axes, const int64_t* point_dims, int64_t points_per_cell,
+                        const double* point_deltas, const double* focal_spot, const float* table, int64_t num_eta,
+                        double eta_lo, double eta_hi, const float* omegas, int64_t num_directions, const float* tau,
+                        const float* tau_mu, int64_t tau_materials, const float* mu, const float* multiple,
+                        const float* harmonics, const float* moments,
+                        int64_t num_moments, const float* heights, const float* signal_weight, float* out,
+                        float* partial, int64_t partial_capacity, float* height_sums, void* stream) {
+  int st = check_table(table, num_materials, num_eta, num_groups);
+  if (st) return st;
+  CITRUS_REQUIRE(rho && phi && axes && point_dims && point_deltas && focal_spot && omegas && tau && mu && out &&
+                     partial && height_sums && (multiple || (harmonics && moments)),
+                 "%s: null pointer", name);
+  CITRUS_REQUIRE(tau_mu == nullptr || (tau_materials >= 1 && tau_materials <= kMaxM),
+                 "%s: %lld traced materials outside [1, %d]", name, (long long)tau_materials, kMaxM);
+  CITRUS_REQUIRE(moments == nullptr || (num_moments >= 1 && num_moments <= kMaxMoments),
+                 "%s: %lld moments outside [1, %d]", name, (long long)num_moments, kMaxMoments);
+  const int64_t f = points_per_cell;
+  CITRUS_REQUIRE(f >= 1 && point_dims[0] % f == 0 && point_dims[1] % f == 0 && point_dims[2] % f == 0,
+                 "%s: the point grid is not cells x %lld", name, (long long)f);
+  CITRUS_REQUIRE(num_directions >= 0 && num_directions <= 65535, "%s: bad direction count", name);
+  if (num_groups % 4 == 0)
+    CITRUS_REQUIRE(((uintptr_t)table % 16) == 0 && ((uintptr_t)out % 16) == 0,
+                   "%s: table and out must be 16-byte aligned", name);
+  const int64_t V = point_dims[0] * point_dims[1] * point_dims[2];
+  const int64_t nblocks = cdiv(V, kEmitPoints);
+  CITRUS_REQUIRE(partial_capacity >= nblocks * num_directions * 2, "%s: partial buffer holds %lld floats, needs %lld",
+                 name, (long long)partial_capacity, (long long)(nblocks * num_directions * 2));
+  if (V == 0 || num_directions == 0) return CITRUS_OK;
+  const FCInputs in = make_inputs(rho, phi, axes, V, focal_spot, point_dims);
+  const Table tb = make_table(table, num_materials, num_eta, num_groups, eta_lo, eta_hi);
+  const PointGrid pg = make_grid(point_dims, f);
+  const int G = (int)num_groups, K = (int)num_directions, NS = (int)num_moments;
+  cudaStream_t s = as_stream(stream);
+#define CITRUS_EMISSION(GP)                                                                                        \
+  emission_for<GP>(V, K, s, in, tb, pg, omegas, tau, tau_mu, (int)tau_materials, mu, multiple, harmonics, moments,  \
+                   NS, heights, signal_weight, \
+                   point_deltas, out, partial, height_sums)
+  if (G <= 1) st = CITRUS_EMISSION(1);
+  else if (G <= 2) st = CITRUS_EMISSION(2);
+  else if (G <= 4) st = CITRUS_EMISSION(4);
+  else if (G <= 8) st = CITRUS_EMISSION(8);
+  else if (G <= 16) st = CITRUS_EMISSION(16);
+  else st = CITRUS_EMISSION(32);
+#undef CITRUS_EMISSION
+  if (st) return st;
+  return launch_status(name);
+}
+
+}  // namespace
+}  // namespace citrus
 
 extern "C" int citrus_attenuated_emission(const float* rho, int64_t num_materials, const float* phi,
                                           int64_t num_groups, const float* axes, const int64_t* point_dims,
                                           int64_t points_per_cell, const double* point_deltas,
                                           const double* focal_spot, const float* table, int64_t num_eta,
                                           double eta_lo, double eta_hi, const float* omegas, int64_t num_directions,
-                                          const float* tau, const float* mu, const float* multiple,
-                                          const float* heights, const float* signal_weight, float* out,
-                                          float* partial, int64_t partial_capacity, float* height_sums,
-                                          void* stream) {
-  int st = check_table(table, num_materials, num_eta, num_groups);
-  if (st) return st;
-  CITRUS_REQUIRE(rho && phi && axes && point_dims && point_deltas && focal_spot && omegas && tau && mu && multiple &&
-                     out && partial && height_sums,
-                 "citrus_attenuated_emission: null pointer");
-  const int64_t f = points_per_cell;
-  CITRUS_REQUIRE(f >= 1 && point_dims[0] % f == 0 && point_dims[1] % f == 0 && point_dims[2] % f == 0,
-                 "citrus_attenuated_emission: the point grid is not cells x %lld", (long long)f);
-  CITRUS_REQUIRE(num_directions >= 0 && num_directions <= 65535, "citrus_attenuated_emission: bad direction count");
-  const int64_t V = point_dims[0] * point_dims[1] * point_dims[2];
-  const int64_t nblocks = cdiv(V, kPoints);
-  CITRUS_REQUIRE(partial_capacity >= nblocks * num_directions * 2,
-                 "citrus_attenuated_emission: partial buffer holds %lld floats, needs %lld",
-                 (long long)partial_capacity, (long long)(nblocks * num_directions * 2));
-  if (V == 0 || num_directions == 0) return CITRUS_OK;
-  const FCInputs in = make_inputs(rho, phi, axes, V, focal_spot, point_dims);
-  const Table tb{table, (int)num_materials, (int)num_eta, (int)num_groups, (float)eta_lo, (float)eta_hi};
-  const PointGrid pg = make_grid(point_dims, f);
-  const int G = (int)num_groups, K = (int)num_directions;
-  const int ky = K;  // one direction per block row: the point data is reused from registers across none; simple
-  dim3 grid((unsigned)nblocks, (unsigned)ky), block(kPoints, G);
-  cudaStream_t s = as_stream(stream);
-  CITRUS_G_DISPATCH(G, emission_kernel, grid, block, 0, s, in, tb, pg, omegas, K, tau, mu, multiple, heights,
-                    signal_weight, (float)point_deltas[0], (float)point_deltas[1], (float)point_deltas[2], out,
-                    partial)
-  reduce_partials_kernel<<<K, dim3(256, 2), 0, s>>>(partial, nblocks, K, height_sums);
-  return launch_status("citrus_attenuated_emission");
+                                          const float* tau, const float* tau_mu, int64_t tau_materials,
+                                          const float* mu, const float* multiple, const float* heights,
+                                          const float* signal_weight, float* out, float* partial,
+                                          int64_t partial_capacity, float* height_sums, void* stream) {
+  CITRUS_REQUIRE(multiple != nullptr, "citrus_attenuated_emission: null multiple-collision source");
+  return attenuated_emission("citrus_attenuated_emission", rho, num_materials, phi, num_groups, axes, point_dims,
+                             points_per_cell, point_deltas, focal_spot, table, num_eta, eta_lo, eta_hi, omegas,
+                             num_directions, tau, tau_mu, tau_materials, mu, multiple, nullptr, nullptr, 0, heights,
+                             signal_weight, out, partial, partial_capacity, height_sums, stream);
+}
+
+extern "C" int citrus_attenuated_emission_moments(const float* rho, int64_t num_materials, const float* phi,
+                                                  int64_t num_groups, const float* axes, const int64_t* point_dims,
+                                                  int64_t points_per_cell, const double* point_deltas,
+                                                  const double* focal_spot, const float* table, int64_t num_eta,
+                                                  double eta_lo, double eta_hi, const float* omegas,
+                                                  int64_t num_directions, const float* tau, const float* tau_mu,
+                                                  int64_t tau_materials, const float* mu, const float* harmonics,
+                                                  const float* moments, int64_t num_moments,
+                                                  const float* heights, const float* signal_weight, float* out,
+                                                  float* partial, int64_t partial_capacity, float* height_sums,
+                                                  void* stream) {
+  CITRUS_REQUIRE(harmonics != nullptr && moments != nullptr,
+                 "citrus_attenuated_emission_moments: null harmonics or moments");
+  return attenuated_emission("citrus_attenuated_emission_moments", rho, num_materials, phi, num_groups, axes,
+                             point_dims, points_per_cell, point_deltas, focal_spot, table, num_eta, eta_lo, eta_hi,
+                             omegas, num_directions, tau, tau_mu, tau_materials, mu, nullptr, harmonics, moments,
+                             num_moments, heights,
+                             signal_weight, out, partial, partial_capacity, height_sums, stream);
 }

@@ -23,6 +23,9 @@ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // Number of SMs of the current device (cached per device).
 int num_sms();
 
+// Adds n kernel launches to the library's launch counter (citrus_launch_count).
+void note_launches(int n = 1);
+
 #define CITRUS_REQUIRE(cond, ...)                                   \
   do {                                                              \
     if (!(cond)) return ::citrus::set_error(CITRUS_EINVAL, __VA_ARGS__); \

@@ -93,6 +93,203 @@ __global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __r
   }
 }
 
+// ---- streaming forms for a short inner dimension -----------------------------------------------------------------
+//
+// Column-stationary (K <= 64): a thread keeps the K values of its two columns of B in registers and walks the rows of
+// A (shared memory, read as float4 broadcasts), writing each output row as it goes; B is read once, C once.
+// Row-stationary (M <= 64, any K): a thread keeps the M outputs of its two columns in registers and streams the rows
+// of B past the columns of A (A^T in shared memory). Both add the products over k in increasing order with fused
+// multiply-adds, as the tiled kernel above does.
+constexpr int kStreamThreads = 128;
+constexpr int kStreamRows = 128;  // rows of A per block of the column-stationary form
+
+template <int kKP, bool kPair>
+__global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* __restrict__ A, int64_t lda,
+                                                                  const float* __restrict__ B, int64_t ldb,
+                                                                  float* __restrict__ C, int64_t ldc, int M, int K,
+                                                                  int64_t J, int64_t stride_b, int64_t stride_c,
+                                                                  int accumulate) {
+  extern __shared__ float4 s_a4[];
+  float (*As)[kKP] = reinterpret_cast<float (*)[kKP]>(s_a4);  // [kStreamRows + 3][kKP], zero past the tile
+  constexpr int kCols = kPair ? 2 : 1;
+  const int row0 = blockIdx.y * kStreamRows;
+  const int rows = min(kStreamRows, M - row0);
+  for (int i = threadIdx.x; i < (kStreamRows + 3) * kKP; i += kStreamThreads) {
+    const int r = i / kKP, k = i % kKP;
+    As[r][k] = (r < rows && k < K) ? A[(int64_t)(row0 + r) * lda + k] : 0.f;
+  }
+  B += blockIdx.z * stride_b;
+  C += blockIdx.z * stride_c;
+  const int64_t col = ((int64_t)blockIdx.x * kStreamThreads + threadIdx.x) * kCols;
+  const bool valid = col < J;
+  float b0[kKP], b1[kKP];
+#pragma unroll
+  for (int k = 0; k < kKP; ++k) {
+    b0[k] = 0.f;
+    b1[k] = 0.f;
+    if (valid && k < K) {
+      if (kPair) {
+        const float2 v = *reinterpret_cast<const float2*>(B + (int64_t)k * ldb + col);
+        b0[k] = v.x;
+        b1[k] = v.y;
+      } else {
+        b0[k] = B[(int64_t)k * ldb + col];
+      }
+    }
+  }
+  __syncthreads();
+  if (!valid) return;
+  // four rows at a time: eight independent multiply-add chains per thread
+  for (int r0 = 0; r0 < rows; r0 += 4) {
+    float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < kKP; k += 4) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 a = *reinterpret_cast<const float4*>(&As[r0 + q][k]);  // rows past the tile are zero
+        a0[q] = fmaf(a.x, b0[k], a0[q]);
+        a0[q] = fmaf(a.y, b0[k + 1], a0[q]);
+        a0[q] = fmaf(a.z, b0[k + 2], a0[q]);
+        a0[q] = fmaf(a.w, b0[k + 3], a0[q]);
+        if (kPair) {
+          a1[q] = fmaf(a.x, b1[k], a1[q]);
+          a1[q] = fmaf(a.y, b1[k + 1], a1[q]);
+          a1[q] = fmaf(a.z, b1[k + 2], a1[q]);
+          a1[q] = fmaf(a.w, b1[k + 3], a1[q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (r0 + q >= rows) break;
+      float* out = C + (int64_t)(row0 + r0 + q) * ldc + col;
+      if (kPair) {
+        float2 v = make_float2(a0[q], a1[q]);
+        if (accumulate) {
+          const float2 o = *reinterpret_cast<const float2*>(out);
+          v.x += o.x;
+          v.y += o.y;
+        }
+        *reinterpret_cast<float2*>(out) = v;
+      } else {
+        *out = accumulate ? *out + a0[q] : a0[q];
+      }
+    }
+  }
+}
+
+template <int kMP, bool kPair>
+__global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* __restrict__ A, int64_t lda,
+                                                                  const float* __restrict__ B, int64_t ldb,
+                                                                  float* __restrict__ C, int64_t ldc, int M, int K,
+                                                                  int64_t J, int64_t stride_b, int64_t stride_c,
+                                                                  int accumulate) {
+  extern __shared__ float4 s_at4[];
+  float* At = reinterpret_cast<float*>(s_at4);  // [K][kMP], A transposed, zero rows past M
+  constexpr int kCols = kPair ? 2 : 1;
+  for (int i = threadIdx.x; i < K * kMP; i += kStreamThreads) {
+    const int k = i / kMP, r = i % kMP;
+    At[i] = r < M ? A[(int64_t)r * lda + k] : 0.f;
+  }
+  B += blockIdx.z * stride_b;
+  C += blockIdx.z * stride_c;
+  const int64_t col = ((int64_t)blockIdx.x * kStreamThreads + threadIdx.x) * kCols;
+  const bool valid = col < J;
+  __syncthreads();
+  if (!valid) return;
+  float c0[kMP], c1[kMP];
+#pragma unroll
+  for (int r = 0; r < kMP; ++r) c0[r] = c1[r] = 0.f;
+  for (int k = 0; k < K; ++k) {
+    float x0, x1 = 0.f;
+    if (kPair) {
+      const float2 v = *reinterpret_cast<const float2*>(B + (int64_t)k * ldb + col);
+      x0 = v.x;
+      x1 = v.y;
+    } else {
+      x0 = B[(int64_t)k * ldb + col];
+    }
+    const float* at = At + k * kMP;
+#pragma unroll
+    for (int r = 0; r < kMP; r += 4) {
+      const float4 a = *reinterpret_cast<const float4*>(at + r);
+      c0[r] = fmaf(a.x, x0, c0[r]);
+      c0[r + 1] = fmaf(a.y, x0, c0[r + 1]);
+      c0[r + 2] = fmaf(a.z, x0, c0[r + 2]);
+      c0[r + 3] = fmaf(a.w, x0, c0[r + 3]);
+      if (kPair) {
+        c1[r] = fmaf(a.x, x1, c1[r]);
+        c1[r + 1] = fmaf(a.y, x1, c1[r + 1]);
+        c1[r + 2] = fmaf(a.z, x1, c1[r + 2]);
+        c1[r + 3] = fmaf(a.w, x1, c1[r + 3]);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kMP; ++r) {
+    if (r >= M) break;
+    float* out = C + (int64_t)r * ldc + col;
+    if (kPair) {
+      float2 v = make_float2(c0[r], c1[r]);
+      if (accumulate) {
+        const float2 o = *reinterpret_cast<const float2*>(out);
+        v.x += o.x;
+        v.y += o.y;
+      }
+      *reinterpret_cast<float2*>(out) = v;
+    } else {
+      *out = accumulate ? *out + c0[r] : c0[r];
+    }
+  }
+}
+
+template <int kKP, bool kPair>
+int launch_cols(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
+                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t s) {
+  const int64_t cols_per_block = (int64_t)kStreamThreads * (kPair ? 2 : 1);
+  const size_t smem = (size_t)(kStreamRows + 3) * kKP * sizeof(float);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_cols_kernel<kKP, kPair>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
+  }
+  dim3 grid((unsigned)cdiv(J, cols_per_block), (unsigned)cdiv(M, kStreamRows), (unsigned)batch);
+  gemm_cols_kernel<kKP, kPair><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
+                                                                 stride_c, accumulate);
+  note_launches();
+  return launch_status("citrus_small_k_gemm");
+}
+
+template <int kMP, bool kPair>
+int launch_rows(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
+                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t s) {
+  const size_t smem = (size_t)K * kMP * sizeof(float);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_rows_kernel<kMP, kPair>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
+  }
+  const int64_t cols_per_block = (int64_t)kStreamThreads * (kPair ? 2 : 1);
+  dim3 grid((unsigned)cdiv(J, cols_per_block), 1, (unsigned)batch);
+  gemm_rows_kernel<kMP, kPair><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
+                                                                  stride_c, accumulate);
+  note_launches();
+  return launch_status("citrus_small_k_gemm");
+}
+
+template <bool kPair>
+int launch_stream(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
+                  int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t s) {
+  if (K <= 16) return launch_cols<16, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  if (K <= 32) return launch_cols<32, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  if (K <= 48) return launch_cols<48, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  if (K <= 64) return launch_cols<64, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  if (M <= 16) return launch_rows<16, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  if (M <= 32) return launch_rows<32, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  if (M <= 48) return launch_rows<48, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+  return launch_rows<64, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+}
+
 template <int R, bool kAligned>
 int launch_variant(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
                    int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t stream) {
@@ -105,6 +302,7 @@ int launch_variant(const float* A, int64_t lda, const float* B, int64_t ldb, flo
   dim3 grid((unsigned)cdiv(J, kCols), (unsigned)cdiv(M, 8 * R), (unsigned)batch);
   small_k_gemm_kernel<R, kAligned><<<grid, kThreads, smem, stream>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
                                                                      stride_c, accumulate);
+  note_launches();
   return launch_status("citrus_small_k_gemm");
 }
 
@@ -137,6 +335,12 @@ extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, 
   const int m = (int)M, k = (int)K;
   const int rows = (m + 7) / 8;
   cudaStream_t s = as_stream(stream);
+  if (K <= 64 || (M <= 64 && K * 64 * 4 <= 200 * 1024)) {  // the streaming forms
+    const bool pair = J % 2 == 0 && ldb % 2 == 0 && ldc % 2 == 0 && stride_b % 2 == 0 && stride_c % 2 == 0 &&
+                      ((uintptr_t)B % 8) == 0 && ((uintptr_t)C % 8) == 0;
+    if (pair) return launch_stream<true>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    return launch_stream<false>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  }
   if (8ll * 16 * K * 4 + kChunk * kCols * 4 > 200 * 1024)
     return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: K %lld too large for the shared-memory tile", (long long)K);
   if (rows <= 1) return launch<1>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);

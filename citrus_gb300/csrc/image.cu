@@ -126,6 +126,7 @@ extern "C" int citrus_weighted_direction_sum(const float* image, int64_t num_dir
   weighted_direction_sum_kernel<<<(unsigned)cdiv(total, 256), 256, 0, as_stream(stream)>>>(
       image, (int)num_directions, (int)groups, (int)rows, (int)cols, is_k, is_g, is_r, is_c, weights,
       (int)weight_rows, (int)weight_cols, accumulator, accumulate);
+  note_launches();
   return launch_status("citrus_weighted_direction_sum");
 }
 
@@ -143,6 +144,7 @@ extern "C" int citrus_box_blur(const float* in, float* out, int64_t num_directio
   dim3 grid((unsigned)cdiv(lines * length, 256), (unsigned)num_directions);
   box_blur_kernel<<<grid, 256, 0, as_stream(stream)>>>(in, out, (int)num_directions, lines, (int)length, is_k, is_l,
                                                        is_p, os_k, os_l, os_p, wa);
+  note_launches();
   return launch_status("citrus_box_blur");
 }
 
@@ -153,6 +155,7 @@ extern "C" int citrus_box_matrix(const float* widths, int64_t num_directions, in
   if (num_directions == 0) return CITRUS_OK;
   dim3 grid((unsigned)cdiv(length * length, 256), (unsigned)num_directions);
   box_matrix_kernel<<<grid, 256, 0, as_stream(stream)>>>(widths, (int)length, out);
+  note_launches();
   return launch_status("citrus_box_matrix");
 }
 
@@ -166,6 +169,7 @@ extern "C" int citrus_weighted_group_sum(const float* image, const float* weight
   dim3 grid((unsigned)cdiv(rows * cols, 256), (unsigned)num_directions);
   weighted_group_sum_kernel<<<grid, 256, 0, as_stream(stream)>>>(image, weights, (int)num_directions, (int)rows,
                                                                  (int)groups, (int)cols, (int)weight_cols, out);
+  note_launches();
   return launch_status("citrus_weighted_group_sum");
 }
 
@@ -175,5 +179,6 @@ extern "C" int citrus_sum_directions(const float* image, int64_t num_directions,
   if (pixels == 0) return CITRUS_OK;
   sum_directions_kernel<<<(unsigned)cdiv(pixels, 256), 256, 0, as_stream(stream)>>>(image, (int)num_directions, pixels,
                                                                                    stride_k, accumulator, accumulate);
+  note_launches();
   return launch_status("citrus_sum_directions");
 }

@@ -123,5 +123,6 @@ extern "C" int citrus_scattering_moments(const float* transfer, const float* phi
     CITRUS_MOMENTS_LAUNCH(32)
   }
 #undef CITRUS_MOMENTS_LAUNCH
+  note_launches();
   return launch_status("citrus_scattering_moments");
 }

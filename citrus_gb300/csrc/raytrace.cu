@@ -295,14 +295,15 @@ template <int kC>
 __global__ void __launch_bounds__(kThreads) downstream_kernel(Box b, const float* __restrict__ vol, int C,
                                                               const float* __restrict__ omegas,
                                                               const uint8_t* __restrict__ toward, Panel panel,
-                                                              float diagonal, int64_t V, float* __restrict__ out) {
+                                                              float diagonal, int64_t V, float* __restrict__ out,
+                                                              int64_t os_k, int64_t os_c, int64_t os_v) {
   const int64_t v = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int k = blockIdx.y;
   if (v >= V) return;
   const int nC = kC > 0 ? kC : C;
-  float* o = out + (int64_t)k * nC * V + v;
+  float* o = out + (int64_t)k * os_k + v * os_v;
   if (toward != nullptr && toward[k] == 0) {
-    for (int c = 0; c < nC; ++c) o[(int64_t)c * V] = INFINITY;
+    for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = INFINITY;
     return;
   }
   const int64_t nzx = (int64_t)b.n[0] * b.n[2];
@@ -319,7 +320,134 @@ __global__ void __launch_bounds__(kThreads) downstream_kernel(Box b, const float
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
   integrate<kC, false, float>(b, r, p1, vol, C, acc);
-  for (int c = 0; c < nC; ++c) o[(int64_t)c * V] = acc[c];
+  for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = acc[c];
+}
+
+// ---- downstream on the lattice: one crossing sequence per direction ------------------------------------------
+// Every downstream ray starts at a voxel centre, so along a direction all of them meet the voxel planes at the same
+// distances from their start: the m-th crossing of axis a lies at (m + 1/2) delta_a / |omega_a|. The merged sequence
+// of these crossings (distance, flat index step) is built once per direction in float64 (crossing_table_kernel), and
+// a ray is then a walk down that table from its own voxel, up to the crossing at which it leaves the box or to the
+// panel, whichever comes first: one broadcast shared-memory read, one gather and the channel FMAs per segment.
+//
+// Table of direction k, E = nx + ny + nz words per part: t[E] (float distance of crossing j from the start, +inf past
+// the last), dv[E] (flat index step of crossing j), first[E] (entry of the m-th crossing of axis a at
+// first[off_a + m], off = 0, nx, nx + ny).
+__global__ void crossing_table_kernel(Box b, const float* __restrict__ omegas, int K, int32_t* __restrict__ table) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const int E = b.n[0] + b.n[1] + b.n[2];
+  float* t = reinterpret_cast<float*>(table + (int64_t)k * 3 * E);
+  int32_t* dv = table + (int64_t)k * 3 * E + E;
+  int32_t* first = table + (int64_t)k * 3 * E + 2 * E;
+  const int64_t stride[3] = {b.n[2], (int64_t)b.n[0] * b.n[2], 1};  // x: columns, y: rows, z: slices
+  const int off[3] = {0, b.n[0], b.n[0] + b.n[1]};
+  double step[3], next[3];
+  int m[3] = {0, 0, 0};
+  int32_t dir[3];
+  for (int a = 0; a < 3; ++a) {
+    const double w = omegas[3 * k + a];
+    step[a] = w != 0.0 ? b.delta[a] / fabs(w) : INFINITY;
+    next[a] = 0.5 * step[a];
+    dir[a] = (int32_t)(w > 0.0 ? stride[a] : -stride[a]);
+    for (int i = 0; i < b.n[a]; ++i) first[off[a] + i] = E;  // never reached along a parallel axis
+  }
+  for (int j = 0; j < E; ++j) {
+    int a = 0;
+    if (next[1] < next[a]) a = 1;
+    if (next[2] < next[a]) a = 2;
+    if (!(next[a] < INFINITY)) {
+      t[j] = INFINITY;
+      dv[j] = 0;
+      continue;
+    }
+    t[j] = (float)next[a];
+    dv[j] = dir[a];
+    first[off[a] + m[a]] = j;
+    ++m[a];
+    next[a] = m[a] < b.n[a] ? (m[a] + 0.5) * step[a] : INFINITY;
+  }
+}
+
+template <int kC>
+__global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, const float* __restrict__ vol, int C,
+                                                                      const float* __restrict__ omegas,
+                                                                      const uint8_t* __restrict__ toward, Panel panel,
+                                                                      float diagonal, int64_t V,
+                                                                      const int32_t* __restrict__ table,
+                                                                      float* __restrict__ out, int64_t os_k,
+                                                                      int64_t os_c, int64_t os_v) {
+  extern __shared__ int32_t s_tab[];  // [3E] of this direction
+  const int k = blockIdx.y;
+  const int E = b.n[0] + b.n[1] + b.n[2];
+  const int32_t* src = table + (int64_t)k * 3 * E;
+  for (int i = threadIdx.x; i < 3 * E; i += kThreads) s_tab[i] = src[i];
+  __syncthreads();
+  const float* t_cross = reinterpret_cast<const float*>(s_tab);
+  const int32_t* dv = s_tab + E;
+  const int32_t* first = s_tab + 2 * E;
+  const int64_t v = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (v >= V) return;
+  const int nC = kC > 0 ? kC : C;
+  float* o = out + (int64_t)k * os_k + v * os_v;
+  if (toward != nullptr && toward[k] == 0) {
+    for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = INFINITY;
+    return;
+  }
+  const int64_t nzx = (int64_t)b.n[0] * b.n[2];
+  const int iy = (int)(v / nzx);
+  const int64_t rem = v - (int64_t)iy * nzx;
+  const int ix = (int)(rem / b.n[2]);
+  const int iz = (int)(rem - (int64_t)ix * b.n[2]);
+  const float r[3] = {(float)(b.lo[0] + b.delta[0] * (ix + 0.5)), (float)(b.lo[1] + b.delta[1] * (iy + 0.5)),
+                      (float)(b.lo[2] + b.delta[2] * (iz + 0.5))};
+  const float w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
+  float t_end = fminf(fmaxf(panel_distance(panel, r, w), 0.f), diagonal);
+  // the crossing that leaves the box: along axis a after the voxels left between i_a and the face ahead
+  const int idx[3] = {ix, iy, iz};
+  const int off[3] = {0, b.n[0], b.n[0] + b.n[1]};
+  int exit_j = E;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (w[a] == 0.f) continue;
+    const int left = w[a] > 0.f ? b.n[a] - 1 - idx[a] : idx[a];
+    exit_j = min(exit_j, first[off[a] + left]);
+  }
+  if (exit_j < E) t_end = fminf(t_end, t_cross[exit_j]);
+  float acc[kC > 0 ? kC : kMaxChannels];
+  for (int c = 0; c < nC; ++c) acc[c] = 0.f;
+  int64_t cur = v;
+  float prev = 0.f;
+  for (int j = 0; j <= exit_j && j < E && prev < t_end; ++j) {
+    const float tj = t_cross[j];
+    const float seg = fminf(tj, t_end) - prev;
+    const float* vox = vol + cur * nC;
+    if (kC == 8 || kC == 4) {
+#pragma unroll
+      for (int c = 0; c < (kC > 0 ? kC : 1); c += 4) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(vox + c));
+        acc[c] = fmaf(seg, q.x, acc[c]);
+        acc[c + 1] = fmaf(seg, q.y, acc[c + 1]);
+        acc[c + 2] = fmaf(seg, q.z, acc[c + 2]);
+        acc[c + 3] = fmaf(seg, q.w, acc[c + 3]);
+      }
+    } else if (kC == 2) {
+      const float2 q = __ldg(reinterpret_cast<const float2*>(vox));
+      acc[0] = fmaf(seg, q.x, acc[0]);
+      acc[kC > 1 ? 1 : 0] = fmaf(seg, q.y, acc[kC > 1 ? 1 : 0]);
+    } else {
+      for (int c = 0; c < nC; ++c) acc[c] = fmaf(seg, __ldg(vox + c), acc[c]);
+    }
+    prev = tj;
+    cur += dv[j];
+  }
+  if ((kC == 8 || kC == 4) && os_c == 1 && os_v == nC) {  // voxel-major out: the channels of a ray in float4s
+#pragma unroll
+    for (int c = 0; c < (kC > 0 ? kC : 1); c += 4)
+      *reinterpret_cast<float4*>(o + c) = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
+  } else {
+    for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = acc[c];
+  }
 }
 
 // ---- oblique: through every pixel centre along each direction, clipped to the box on both sides --------------
@@ -373,7 +501,8 @@ int check_common(const float* vol, int64_t C, const double* box, const int64_t* 
     case 4: KERNEL<4><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;                \
     case 8: KERNEL<8><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;                \
     default: KERNEL<0><<<GRID, kThreads, 0, STREAM>>>(__VA_ARGS__); break;               \
-  }
+  }                                                                                       \
+  note_launches();
 
 }  // namespace
 }  // namespace citrus
@@ -422,7 +551,8 @@ extern "C" int citrus_trace_from_source(const float* volume, int64_t channels, c
 extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channels, const double* box,
                                             const int64_t* dims, const float* omegas, const uint8_t* toward,
                                             int64_t num_directions, const double* panel, double diagonal,
-                                            float* out, void* stream) {
+                                            float* out, int64_t os_k, int64_t os_c, int64_t os_v, int32_t* crossings,
+                                            int64_t crossings_words, void* stream) {
   int status = check_common(volume, channels, box, dims, out);
   if (status) return status;
   CITRUS_REQUIRE(omegas && panel, "citrus_downstream_cumulative: null directions or panel");
@@ -440,8 +570,35 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
   const int64_t V = dims[0] * dims[1] * dims[2];
   const int C = (int)channels;
   dim3 grid((unsigned)cdiv(V, kThreads), (unsigned)num_directions);
-  CITRUS_CHANNEL_DISPATCH(C, downstream_kernel, grid, as_stream(stream), b, volume, C, omegas, toward, p,
-                          (float)diagonal, V, out)
+  cudaStream_t s = as_stream(stream);
+  if (crossings == nullptr) {
+    CITRUS_CHANNEL_DISPATCH(C, downstream_kernel, grid, s, b, volume, C, omegas, toward, p, (float)diagonal, V, out,
+                            os_k, os_c, os_v)
+    return launch_status("citrus_downstream_cumulative");
+  }
+  const int64_t E = dims[0] + dims[1] + dims[2];
+  CITRUS_REQUIRE(crossings_words >= 3 * E * num_directions,
+                 "citrus_downstream_cumulative: crossing table holds %lld words, needs %lld",
+                 (long long)crossings_words, (long long)(3 * E * num_directions));
+  CITRUS_REQUIRE(3 * E * 4 <= 48 * 1024, "citrus_downstream_cumulative: grid too large for the crossing table");
+  if (C % 2 == 0) CITRUS_REQUIRE(((uintptr_t)volume % 16) == 0, "citrus_downstream_cumulative: unaligned volume");
+  if (C % 4 == 0 && os_c == 1 && os_v == C)
+    CITRUS_REQUIRE(((uintptr_t)out % 16) == 0 && os_k % 4 == 0, "citrus_downstream_cumulative: unaligned out");
+  crossing_table_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, s>>>(b, omegas, (int)num_directions, crossings);
+  note_launches();
+  const size_t smem = (size_t)3 * E * sizeof(int32_t);
+#define CITRUS_LATTICE(KC)                                                                                        \
+  downstream_lattice_kernel<KC><<<grid, kThreads, smem, s>>>(b, volume, C, omegas, toward, p, (float)diagonal, V, \
+                                                            crossings, out, os_k, os_c, os_v)
+  switch (C) {
+    case 1: CITRUS_LATTICE(1); break;
+    case 2: CITRUS_LATTICE(2); break;
+    case 4: CITRUS_LATTICE(4); break;
+    case 8: CITRUS_LATTICE(8); break;
+    default: CITRUS_LATTICE(0); break;
+  }
+#undef CITRUS_LATTICE
+  note_launches();
   return launch_status("citrus_downstream_cumulative");
 }
 

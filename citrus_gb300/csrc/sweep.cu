@@ -114,6 +114,7 @@ int launch_planes(float* store, const float* mu, const float* c, const int* octa
     if (total <= 0) continue;
     plane_kernel<kG><<<(unsigned)cdiv(total, kThreads), kThreads, 0, stream>>>(
         store, mu, c, octant, cell, upstream, start, E, N, G, Dc, views, view_stride);
+    note_launches();
   }
   return launch_status("citrus_sweep_planes");
 }
@@ -137,6 +138,7 @@ int launch_persistent(float* store, const float* mu, const float* c, const int* 
   e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG>, dim3((unsigned)blocks), dim3(kThreads), args, 0,
                                   stream);
   if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_persistent: %s", cudaGetErrorString(e));
+  note_launches();
   return CITRUS_OK;
 }
 

@@ -159,22 +159,36 @@ class GB300Projectors:
 
     # ---- (c) downstream -----------------------------------------------------------------------------------------
     def downstream_cumulative(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
-                              omegas: Tensor, out: Optional[Tensor] = None) -> Tensor:
+                              omegas: Tensor, out: Optional[Tensor] = None, lattice: bool = True,
+                              voxel_major: bool = False) -> Tensor:
         """[K, C, R, Cc, S] from every voxel centre along each direction to the panel; +inf where the direction does
-        not face the panel (``omega . (-n_hat) <= 0``), 0 beyond the panel."""
+        not face the panel (``omega . (-n_hat) <= 0``), 0 beyond the panel. ``lattice`` walks every ray down its
+        direction's shared crossing table (the default), else each ray runs its own walk. ``voxel_major`` returns
+        the same values as a contiguous [K, V, C] tensor (``out`` ignored)."""
         vol = _voxel_major(mu, grid)
         device = mu.device
         omegas = omegas.to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
         K = omegas.shape[0]
         n_hat = torch.tensor(geometry.panel_axes(angle)[2], dtype=torch.float32, device=device)
         toward = ((omegas * (-n_hat)).sum(-1) > 0).to(torch.uint8).contiguous()
-        if out is None:
-            out = torch.empty(K, *mu.shape, device=device, dtype=torch.float32)
+        C, V = int(mu.shape[0]), grid.num_voxels
+        if voxel_major:
+            out = torch.empty(K, V, C, device=device, dtype=torch.float32)
+            strides = (V * C, 1, C)
+        else:
+            if out is None:
+                out = torch.empty(K, *mu.shape, device=device, dtype=torch.float32)
+            if tuple(out.shape) != (K, *mu.shape) or out.dtype != torch.float32 or not out.is_contiguous():
+                raise ValueError(f"out must be a contiguous float32 tensor of shape {(K, *mu.shape)}")
+            strides = (C * V, V, 1)
         host = HostArgs()
         box, dims = _grid_args(host, grid)
         diagonal = math.sqrt(sum(e * e for e in grid.extent)) * (1 + 1e-9) + 1e-9
+        crossings = (torch.empty(3 * (grid.num_rows + grid.num_cols + grid.num_slices) * K, dtype=torch.int32,
+                                 device=device) if lattice else None)
         _lib.call("citrus_downstream_cumulative", vol.data_ptr(), mu.shape[0], box, dims, omegas.data_ptr(),
-                  toward.data_ptr(), K, panel_args(host, geometry, angle), diagonal, out.data_ptr(),
+                  toward.data_ptr(), K, panel_args(host, geometry, angle), diagonal, out.data_ptr(), *strides,
+                  None if crossings is None else crossings.data_ptr(), 0 if crossings is None else crossings.numel(),
                   _lib.stream_handle(device))
         return out
 

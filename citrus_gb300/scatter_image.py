@@ -1,9 +1,9 @@
 """Collapsed-cone scatter image and primary image of one view (mirrors ``citrus/scatter_solver/scatter_image.py``).
 
 Per chunk of panel-facing cone directions the image runs: the downstream optical depth of the transport cells
-(``Projectors.downstream_cumulative``), the multiple-collision source ``Y_k @ T`` (``kernels.small_k_gemm``), the
-attenuated total emission at the quadrature points with its height sums (``citrus_attenuated_emission``; with
-direction-only signal weights the groups are summed there), the projection through every pixel centre
+(``Projectors.downstream_cumulative``), the attenuated total emission at the quadrature points with its height sums
+(``citrus_attenuated_emission_moments``, which forms the multiple-collision source ``Y_k @ T`` of each point's cell in
+registers; with direction-only signal weights the groups are summed there), the projection through every pixel centre
 (``Projectors.oblique_project``, written rows-outer), the finite-cone footprint blur (``citrus_box_blur``, widths from
 the height sums on the device) and the weighted accumulation (``citrus_weighted_group_sum``,
 ``citrus_sum_directions``, ``citrus_weighted_direction_sum``).
@@ -72,7 +72,12 @@ class DirectionSetContext:
 
     Device tensors (float32): omega [K, 3], weight [K], cos_theta0 [K], cell_width [K, 2]; ``signal_group_weight``
     [K, G] when the signal weights are the same at every pixel (flat panel), else ``signal_channel_weight``
-    [K, G, Cd] (curved panel: incidence per channel); ``planar_weight`` [K, 1 | Cd].
+    [K, G, Cd] (curved panel: incidence per channel); ``planar_weight`` [K, 1 | Cd]. A curved panel whose detector
+    response separates into a factor of the energy and a factor of the incidence (the ideal counting response, for
+    one) also has ``signal_group_weight`` [K, G] and ``signal_column_weight`` [K, Cd] with
+    ``signal_channel_weight[k, g, c] = signal_group_weight[k, g] * signal_column_weight[k, c]``: the signal image is
+    then the group sum weighted in the emission, blurred, and weighted per channel in the sum over the directions
+    (the channel blur acts before the channel weights in the reference, and the row blur commutes with them).
     """
 
     quadrature: Quadrature
@@ -88,6 +93,7 @@ class DirectionSetContext:
     planar_weight: Tensor
     chunk_bounds: tuple
     image_shape: tuple
+    signal_column_weight: Optional[Tensor] = None
     _cache: dict = field(default_factory=dict, repr=False)
 
     @property
@@ -127,6 +133,7 @@ def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle
     """Keep the panel-facing directions and precompute their weights (reference ``scatter_image.py:542-696``)."""
     energy = np.asarray(library.group_energy, dtype=np.float64)
     G = energy.size
+    signal_column = None
     _, _, n_hat = geometry.panel_axes(angle)
     n_hat = np.asarray(n_hat)
     # the selection in the images' float32, as the projectors see a grazing direction
@@ -143,9 +150,18 @@ def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle
         normals = geometry.local_normals_np(pixels[0], angle)                   # [Cd, 3]
         cos_channel = np.clip(omega @ (-normals).T, 0.0, 1.0)                   # [K, Cd]
         planar = weight[:, None] * cos_channel
-        channel = planar[None] * detector.at(energy, np.arccos(cos_channel)) * grid_t[:, None, None]  # [G, K, Cd]
+        response = detector.at(energy, np.arccos(cos_channel))                 # [G, K, Cd]
+        channel = planar[None] * response * grid_t[:, None, None]              # [G, K, Cd]
         signal_group, signal_channel = None, to_device(channel.transpose(1, 0, 2), device)
         planar_weight = to_device(planar, device)
+        # a response D(E, theta) = f(E) h(theta): group factors f_g / f_0 and channel factors D(E_0, theta_kc)
+        first = response[:1]
+        if K and np.all(first > 0):
+            ratio = response / first
+            if np.allclose(ratio, ratio[:, :1, :1], rtol=1e-12, atol=0.0):
+                group = np.broadcast_to((ratio[:, 0, 0] * grid_t)[None, :], (K, G))
+                signal_group = to_device(np.ascontiguousarray(group), device)
+                signal_column = to_device(planar * first[0], device)
     else:
         response = detector.at(energy, detector_angle(omega, geometry, angle)) if K else np.zeros((G, 0))
         direction = (weight * cos64)[None] * response * grid_t[:, None]          # [G, K]
@@ -157,9 +173,16 @@ def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle
         weight=to_device(weight, device), cos_theta0=to_device(cos64, device),
         cell_width=to_device(quadrature.cell_width[kept], device), signal_group_weight=signal_group,
         signal_channel_weight=signal_channel, planar_weight=planar_weight,
-        chunk_bounds=tuple((s, min(s + chunk, K)) for s in range(0, K, chunk)), image_shape=(Rd, Cd))
+        chunk_bounds=tuple((s, min(s + chunk, K)) for s in range(0, K, chunk)), image_shape=(Rd, Cd),
+        signal_column_weight=signal_column)
     ctx._omega64 = omega
     return ctx
+
+
+# How the image's emission gets the multiple-collision source: "fused" forms Y_k T per point in registers
+# (citrus_attenuated_emission_moments); "product" writes Y_k T with the small-K product first and reads it
+# (citrus_attenuated_emission, the reference's interface).
+EMISSION_FORM = "product"
 
 
 def _blur(src: Tensor, dst: Tensor, lines: int, length: int, strides_in: tuple, strides_out: tuple, k: int,
@@ -173,11 +196,14 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
                            grid_quadrature: Grid, q: int, scatter_source_moments: Tensor, L: int,
                            geometry: ConeGeometry, angle: float, mu_t_coarse: Tensor, projectors,
                            context: DirectionSetContext, grid_coarse: Optional[Grid] = None,
-                           signal_only: bool = False, footprint: bool = True) -> dict:
+                           signal_only: bool = False, footprint: bool = True, rho_coarse: Optional[Tensor] = None,
+                           attenuation: Optional[Tensor] = None) -> dict:
     """Total scatter image of one view, first order plus multiple collision (reference ``scatter_image.py:1141-1323``).
 
     Returns ``{"signal": [Rd, Cd]}`` with ``signal_only``, else fluence, planar_fluence and signal_per_group
-    [G, Rd, Cd] and signal [Rd, Cd].
+    [G, Rd, Cd] and signal [Rd, Cd]. When ``mu_t_coarse`` is ``sum_m attenuation[m, g] rho_coarse[m]`` (the solver's
+    fields) and both are given, the downstream optical depths are traced through the M cell densities instead of the
+    G attenuation channels and combined per group in the emission (the same line integrals, by linearity).
     """
     device = phi_uncollided.device
     f = int(q)
@@ -190,8 +216,9 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
     N_sh = (L + 1) ** 2
     if tuple(scatter_source_moments.shape) != (G, N_sh, *grid_coarse.shape):
         raise ValueError(f"scatter_source_moments must be [{G}, {N_sh}, {grid_coarse.shape}]")
-    # [N_sh, G * cells]: a view of moment-major storage, else one copy
-    T = scatter_source_moments.transpose(0, 1).reshape(N_sh, G * NC).contiguous()
+    # [N_sh, cells, G] (the groups of a cell contiguous, as the emission reads them): a view of cell-major storage,
+    # else one copy
+    T = scatter_source_moments.permute(1, 2, 3, 4, 0).reshape(N_sh, NC * G).contiguous()
     Y = context.harmonics(L)
     Rd, Cd = context.image_shape
     heights, center_height = context.footprint(grid_quadrature)
@@ -207,18 +234,36 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
     partial = torch.empty(K_max * nblocks * 2, device=device)
     sums = torch.empty(K_max, 2, device=device)
     stream = _lib.stream_handle(device)
+    traced = tau_mu = None
+    if rho_coarse is not None and attenuation is not None:
+        traced = rho_coarse.to(device=device, dtype=torch.float32).contiguous()
+        tau_mu = attenuation.to(device=device, dtype=torch.float32).contiguous()
+        if tuple(tau_mu.shape) != (traced.shape[0], G) or tuple(traced.shape[1:]) != tuple(grid_coarse.shape):
+            raise ValueError(f"attenuation must be [M, {G}] and rho_coarse [M, {grid_coarse.shape}]")
     for s, e in context.chunk_bounds:
         k = e - s
         dirs = context.omega[s:e]
-        tau = projectors.downstream_cumulative(mu_t_coarse, grid_coarse, geometry, angle, dirs)  # [k, G, cells]
-        multiple = torch.empty(k, G * NC, device=device)
-        kernels.small_k_gemm(Y[s:e].contiguous(), T, multiple)
+        if traced is not None:
+            tau = projectors.downstream_cumulative(traced, grid_coarse, geometry, angle, dirs,
+                                                   voxel_major=True)                      # [k, cells, M]
+        else:
+            tau = projectors.downstream_cumulative(mu_t_coarse, grid_coarse, geometry, angle, dirs,
+                                                   voxel_major=True)                      # [k, cells, G]
+        Yk = Y[s:e].contiguous()
         emission = torch.empty(k, V, C, device=device)
-        _lib.call("citrus_attenuated_emission", *fc.common(), f, deltas, fc.focal, fc.table.data_ptr(), fc.num_eta,
-                  fc.eta_lo, fc.eta_hi, dirs.data_ptr(), k, tau.data_ptr(), mu.data_ptr(), multiple.data_ptr(),
-                  heights.data_ptr(), context.signal_group_weight[s:e].contiguous().data_ptr() if flat_signal else None,
-                  emission.data_ptr(), partial.data_ptr(), partial.numel(), sums.data_ptr(), stream)
-        del tau, multiple
+        head = (*fc.common(), f, deltas, fc.focal, fc.table.data_ptr(), fc.num_eta, fc.eta_lo, fc.eta_hi,
+                dirs.data_ptr(), k, tau.data_ptr(), None if traced is None else tau_mu.data_ptr(),
+                0 if traced is None else int(traced.shape[0]), mu.data_ptr())
+        tail = (heights.data_ptr(), context.signal_group_weight[s:e].contiguous().data_ptr() if flat_signal else None,
+                emission.data_ptr(), partial.data_ptr(), partial.numel(), sums.data_ptr(), stream)
+        if EMISSION_FORM == "fused":
+            _lib.call("citrus_attenuated_emission_moments", *head, Yk.data_ptr(), T.data_ptr(), N_sh, *tail)
+        else:
+            multiple = torch.empty(k, NC * G, device=device)                               # [k, cells, G]
+            kernels.small_k_gemm(Yk, T, multiple)
+            _lib.call("citrus_attenuated_emission", *head, multiple.data_ptr(), *tail)
+            del multiple
+        del tau
         rows_outer = torch.empty(k, Rd, C, Cd, device=device)
         projectors.oblique_project(emission, grid_quadrature, geometry, angle, dirs,
                                    out=rows_outer.permute(0, 2, 1, 3), voxel_major=True)
@@ -243,6 +288,11 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
             _blur(image, rows, C_img * Cd, Rd, (Rd * C_img * Cd, 1, C_img * Cd), (Rd * C_img * Cd, 1, C_img * Cd), k,
                   sums, cw, 1, geometry.delta_det_row, center_height)
             image = rows
+        if signal_only and flat_signal and context.signal_column_weight is not None:
+            columns = context.signal_column_weight[s:e].contiguous()           # [k, Cd]
+            _lib.call("citrus_weighted_direction_sum", image.data_ptr(), k, 1, Rd, Cd, Rd * Cd, Rd * Cd, Cd, 1,
+                      columns.data_ptr(), 1, Cd, acc.data_ptr(), 1, stream)
+            continue
         if signal_only:
             _lib.call("citrus_sum_directions", image.data_ptr(), k, Rd * Cd, Rd * Cd, acc.data_ptr(), 1, stream)
             continue
@@ -251,9 +301,9 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
         ones = context.weight[s:e].reshape(k, 1, 1, 1).expand(k, G, 1, 1).contiguous()
         planar = context.planar_weight[s:e]
         planar = planar.reshape(k, 1, 1, -1).expand(k, G, 1, planar.shape[-1]).contiguous()
-        signal = (context.signal_group_weight[s:e].reshape(k, G, 1, 1).contiguous()
-                  if context.signal_group_weight is not None
-                  else context.signal_channel_weight[s:e].reshape(k, G, 1, Cd).contiguous())
+        signal = (context.signal_channel_weight[s:e].reshape(k, G, 1, Cd).contiguous()
+                  if context.signal_channel_weight is not None
+                  else context.signal_group_weight[s:e].reshape(k, G, 1, 1).contiguous())
         for j, w in enumerate((ones, planar, signal)):
             _lib.call("citrus_weighted_direction_sum", img.data_ptr(), k, G, Rd, Cd, *strides, w.data_ptr(), 1,
                       w.shape[-1], acc[j].data_ptr(), 1, stream)

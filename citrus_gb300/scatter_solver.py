@@ -248,8 +248,11 @@ class ScatterSolver:
         ctx = self.sweep_context(fields.grid_coarse) if sweep_context is None else sweep_context
         om = torch.as_tensor(ctx.quadrature.omega, dtype=torch.float32).to(self.device)
         w = torch.as_tensor(ctx.quadrature.weight, dtype=torch.float32).to(self.device)
+        # keep the source values for the LD moments of the sweep's source when they fit the chunk budget
+        keep = om.shape[0] * self.num_groups * fields.grid_quadrature.num_voxels * 4 <= SWEEP_CHUNK_BUDGET_BYTES
         return first_collision_sampling_correction(self.library, fields.rho_quadrature, phi_uncollided,
-                                                   fields.grid_quadrature, self.geometry, angle, om, w)
+                                                   fields.grid_quadrature, self.geometry, angle, om, w,
+                                                   keep_cache=keep)
 
     def first_collision_moment_source(self, fields: MaterialFields, angle: float, phi_uncollided: Tensor,
                                       sweep_context: Optional[SweepContext] = None):
@@ -260,10 +263,12 @@ class ScatterSolver:
         library, geometry = self.library, self.geometry
 
         def source_function(direction_index: Tensor, out: Optional[Tensor] = None) -> Tensor:
-            directions = omega.index_select(0, direction_index.to(self.device))
+            index = direction_index.to(self.device)
+            directions = omega.index_select(0, index)
             return first_collision_moments_at_directions(library, fields.rho_quadrature, phi_uncollided,
                                                          fields.grid_quadrature, geometry, angle, directions,
-                                                         correction, fields.q, out=out, cell_major=True)
+                                                         correction, fields.q, out=out, cell_major=True,
+                                                         direction_index=index)
 
         source_function.cell_major = True  # type: ignore[attr-defined]
         return source_function
@@ -292,7 +297,8 @@ class ScatterSolver:
         return combined_scatter_image(self.library, fields.rho_quadrature, phi_uncollided, fields.grid_quadrature,
                                       fields.q, scatter_source_moments, self.L, self.geometry, angle,
                                       fields.mu_t_coarse, self.projectors, context, fields.grid_coarse,
-                                      signal_only=signal_only)
+                                      signal_only=signal_only, rho_coarse=fields.rho_coarse,
+                                      attenuation=self.transport_library.tensor("mu_t", self.device))
 
     def primary(self, fields: MaterialFields, angle: float) -> dict:
         return primary_image(self.library, fields.rho_fine, fields.grid_fine, self.geometry, angle, self.source,

@@ -64,9 +64,9 @@ def scatter_source_function(ctx: SweepContext, T: Tensor):
 
 
 def multiple_collision_source_moments(mu_s_l_volume_coarse: Tensor, phi_total: Tensor) -> Tensor:
-    """Cell-mean moments T of the multiple-collision source, moment-major ``[G, N_sh, R, C, S]`` view
+    """Cell-mean moments T of the multiple-collision source, a ``[G, N_sh, R, C, S]`` view of cell-major storage
     (reference ``scatter_solver.py:899-910``)."""
-    return kernels.scattering_moments(mu_s_l_volume_coarse, phi_total[:, :, 0], "moment_major")
+    return kernels.scattering_moments(mu_s_l_volume_coarse, phi_total[:, :, 0], "cell_major")
 
 
 def _scalar_norms(*phis: Tensor) -> list:

@@ -153,11 +153,13 @@ def uncollided_fluence(library: MultigroupLibrary, rho: Tensor, grid: Grid, geom
 @dataclass(frozen=True, eq=False)
 class FirstCollisionSamplingCorrection:
     """Per-point, per-group ``scale`` and ``beta`` [G, R, C, S] of ``S <- scale S (1 + beta Omega . Omega_UC)``
-    (reference ``uncollided.py:382-411``); ``sums`` [5, G, R, C, S] holds I0, I1, I2, E0, E1 when kept."""
+    (reference ``uncollided.py:382-411``); ``sums`` [5, G, R, C, S] holds I0, I1, I2, E0, E1 when kept, and ``cache``
+    the first-collision source at the correction's directions, which the LD moments of the sweep's source read back."""
 
     scale: Tensor
     beta: Tensor
     sums: Optional[Tensor] = None
+    cache: Optional[Tensor] = None  # [K, G, V] source values at the correction's directions, when kept
 
 
 class _FCArgs:
@@ -189,19 +191,22 @@ class _FCArgs:
 
 def first_collision_sampling_correction(library: MultigroupLibrary, rho: Tensor, phi_uncollided: Tensor, grid: Grid,
                                         geometry: ConeGeometry, angle: float, omegas: Tensor, weights: Tensor,
-                                        keep_sums: bool = False) -> FirstCollisionSamplingCorrection:
+                                        keep_sums: bool = False,
+                                        keep_cache: bool = False) -> FirstCollisionSamplingCorrection:
     """Factors that make the sweep quadrature integrate the sampled first-collision source exactly for l = 0, 1
-    (reference ``uncollided.py:414-461``)."""
+    (reference ``uncollided.py:414-461``); ``keep_cache`` keeps the source values [K, G, V] as well."""
     a = _FCArgs(library, rho, phi_uncollided, grid, geometry, angle)
     om = omegas.to(device=a.device, dtype=torch.float32).reshape(-1, 3).contiguous()
     w = weights.to(device=a.device, dtype=torch.float32).reshape(-1).contiguous()
     scale = torch.empty(a.G, *grid.shape, device=a.device)
     beta = torch.empty_like(scale)
     sums = torch.empty(5, a.G, *grid.shape, device=a.device) if keep_sums else None
+    cache = torch.empty(om.shape[0], a.G, a.V, device=a.device) if keep_cache else None
     _lib.call("citrus_first_collision_correction", *a.common(), a.focal, a.table.data_ptr(), a.num_eta, a.eta_lo,
               a.eta_hi, om.data_ptr(), w.data_ptr(), om.shape[0], moment_table(library, a.device).data_ptr(),
-              None if sums is None else sums.data_ptr(), scale.data_ptr(), beta.data_ptr(), a.stream)
-    return FirstCollisionSamplingCorrection(scale, beta, sums)
+              None if sums is None else sums.data_ptr(), scale.data_ptr(), beta.data_ptr(),
+              None if cache is None else cache.data_ptr(), a.stream)
+    return FirstCollisionSamplingCorrection(scale, beta, sums, cache)
 
 
 def first_collision_source_at_directions(library: MultigroupLibrary, rho: Tensor, phi_uncollided: Tensor, grid: Grid,
@@ -218,9 +223,12 @@ def first_collision_source_at_directions(library: MultigroupLibrary, rho: Tensor
 def first_collision_moments_at_directions(library: MultigroupLibrary, rho: Tensor, phi_uncollided: Tensor, grid: Grid,
                                           geometry: ConeGeometry, angle: float, omegas: Tensor,
                                           correction: FirstCollisionSamplingCorrection, factor: int,
-                                          out: Optional[Tensor] = None, cell_major: bool = True) -> Tensor:
+                                          out: Optional[Tensor] = None, cell_major: bool = True,
+                                          direction_index: Optional[Tensor] = None) -> Tensor:
     """LD moments of the corrected source per cell (reference ``uncollided.py:464-511``): cell-major
-    [K, Rc, Cc, Sc, G, 4] (the sweep's layout, written into ``out`` when given) or [K, G, 4, Rc, Cc, Sc]."""
+    [K, Rc, Cc, Sc, G, 4] (the sweep's layout, written into ``out`` when given) or [K, G, 4, Rc, Cc, Sc]. When the
+    correction kept its source values and ``direction_index`` gives the rows of ``omegas`` among the correction's
+    directions, the values are read back instead of evaluated again."""
     a = _FCArgs(library, rho, phi_uncollided, grid, geometry, angle)
     f = int(factor)
     coarse = grid.coarsen(f)
@@ -233,7 +241,13 @@ def first_collision_moments_at_directions(library: MultigroupLibrary, rho: Tenso
         raise ValueError(f"out must be a contiguous float32 tensor of shape {expected}")
     scale = correction.scale.contiguous()
     beta = correction.beta.contiguous()
+    cache = index = None
+    if correction.cache is not None and direction_index is not None:
+        cache = correction.cache
+        index = direction_index.to(device=a.device, dtype=torch.int32).reshape(-1).contiguous()
+        if index.numel() != K:
+            raise ValueError("direction_index must give one cache row per direction")
     _lib.call("citrus_first_collision_moments", *a.common(), f, a.focal, a.table.data_ptr(), a.num_eta, a.eta_lo,
-              a.eta_hi, om.data_ptr(), K, scale.data_ptr(), beta.data_ptr(), out.data_ptr(),
-              coarse.num_voxels * a.G * 4, a.stream)
+              a.eta_hi, om.data_ptr(), K, scale.data_ptr(), beta.data_ptr(), None if cache is None else cache.data_ptr(),
+              None if index is None else index.data_ptr(), out.data_ptr(), coarse.num_voxels * a.G * 4, a.stream)
     return out if cell_major else out.permute(0, 4, 5, 1, 2, 3)

@@ -103,12 +103,16 @@ def single_view(seed: int = 1) -> Workload:
                     cylinder_phantom(grid, 7.0, 1.0, seed), lib, 4, 12, 3, 0.5, 1)
 
 
-def batched_views(seed: int = 1) -> Workload:
-    grid = Grid((64, 64, 64), 0.4)
+def batched_views(seed: int = 1, cells: int = 64) -> Workload:
+    """The circular cone-beam workload: a 25.6 cm cube of ``cells``^3 cells (64: 0.4 cm), 8 groups from 120 to 30 keV,
+    P5, 6 x 20 sweep directions, cone 16 x 32, curved 256 x 192 panel of 0.16 cm pixels, 60 views. Smaller ``cells``
+    give the same scene on a coarser grid (the small case of the profiles)."""
+    grid = Grid((cells, cells, cells), 25.6 / cells)
     edges = np.linspace(120.0, 30.0, 9)
     lib = spectral_library(edges, bremsstrahlung_spectrum(seed=0), [WATER, BONE], legendre_order=5)
     geo = ConeGeometry(100.0, 150.0, 192, 256, 0.16, 0.16, use_curved_detector=True)
-    return Workload("batched_views", grid, geo, cylinder_phantom(grid, 11.0, 1.5, seed), lib, 6, 20, 5, 0.4, 60)
+    return Workload("batched_views", grid, geo, cylinder_phantom(grid, 11.0, 1.5, seed), lib, 6, 20, 5, 25.6 / cells,
+                    60)
 
 
 # ---- sweep-only problem of the benchmark ----------------------------------------------------------------------------

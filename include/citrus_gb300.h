@@ -31,6 +31,10 @@ int citrus_abi_version(void);
 /* Message of the last failed call on this host thread ("" if none). */
 const char* citrus_last_error_string(void);
 
+/* Kernels this library has launched in this process (all threads and devices), a counter for measurements; no
+ * counterpart in the reference. */
+int64_t citrus_launch_count(void);
+
 /* ------------------------------------------------------------------------------------------------------------------
  * Linear-discontinuous transport sweep.
  * Replaces citrus/scatter_solver/kernels/sweep_kernels.py:265-290 (sweep_planes) and the plane kernel of
@@ -119,13 +123,18 @@ int citrus_trace_from_source(const float* volume, int64_t channels, const double
                              const double* axis_z, const int64_t* point_dims, int64_t num_points, float* out,
                              void* stream);
 
-/* From every voxel centre along each direction omegas[k] ([K, 3]) to the panel, out [K, C, V]; +inf for directions
- * with toward[k] == 0 (uint8 [K], NULL: all toward), 0 beyond the panel. panel (host double [11]) = curved flag,
+/* From every voxel centre along each direction omegas[k] ([K, 3]) to the panel, out element (k, c, v) at
+ * k * os_k + c * os_c + v * os_v (the reference's [K, C, V]: C V, V, 1; voxel-major [K, V, C]: V C, 1, C); +inf for
+ * directions with toward[k] == 0 (uint8 [K], NULL: all toward), 0 beyond the panel. panel (host double [11]) = curved flag,
  * flat-panel centre [3], normal [3], focal spot [3], cylinder radius; diagonal clamps the distance.
+ * crossings: device scratch of crossings_words >= 3 (nx + ny + nz) K int32 words for the per-direction crossing
+ * tables (every ray starts at a voxel centre, so one merged sequence of plane crossings serves all rays of a
+ * direction), or NULL for an independent walk per ray.
  * Replaces downstream_cumulative (ray_tracing.py:501-545, ray_tracing_kernels.py:516-639). */
 int citrus_downstream_cumulative(const float* volume, int64_t channels, const double* box, const int64_t* dims,
                                  const float* omegas, const uint8_t* toward, int64_t num_directions,
-                                 const double* panel, double diagonal, float* out, void* stream);
+                                 const double* panel, double diagonal, float* out, int64_t os_k, int64_t os_c,
+                                 int64_t os_v, int32_t* crossings, int64_t crossings_words, void* stream);
 
 /* Line through every pixel centre (float64 pixels [rows, cols, 3]) along each direction, clipped to the box on both
  * sides (float64 set-up);
@@ -171,36 +180,59 @@ int citrus_first_collision_source(const float* rho, int64_t num_materials, const
 
 /* LD moments (mean, x, y, z slopes) of the corrected source scale (1 + beta cos) S_FC over the points_per_cell^3
  * points of each transport cell, cell-major into out [K, NC, G, 4] with out_direction_stride floats between
- * directions (the sweep's store). Replaces first_collision_moments_at_directions (uncollided.py:464-511,
- * uncollided_kernels.py:552-634). */
+ * directions (the sweep's store). With cache (from citrus_first_collision_correction) S_FC of chunk direction k is
+ * read from cache row cache_index[k] (int32 [K]) instead of evaluated from the table again.
+ * Replaces first_collision_moments_at_directions (uncollided.py:464-511, uncollided_kernels.py:552-634). */
 int citrus_first_collision_moments(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
                                    const float* axes, const int64_t* point_dims, int64_t points_per_cell,
                                    const double* focal_spot, const float* table, int64_t num_eta, double eta_lo,
                                    double eta_hi, const float* omegas, int64_t num_directions, const float* scale,
-                                   const float* beta, float* out, int64_t out_direction_stride, void* stream);
+                                   const float* beta, const float* cache, const int32_t* cache_index, float* out,
+                                   int64_t out_direction_stride, void* stream);
 
 /* Sampling correction: quadrature sums I0, I1, I2 over the K sweep directions (weights [K]) and exact moments E0, E1
  * from moments [M, 2, G_out, G_in] (Legendre l = 0, 1), optionally stored in sums [5, G, V], and the float64 factors
- * scale, beta [G, V] (uncollided.py:357-461, 538-636, uncollided_kernels.py:636-710). */
+ * scale, beta [G, V] (uncollided.py:357-461, 538-636, uncollided_kernels.py:636-710). With cache (NULL: none) the
+ * source values S_FC are kept, cache [K, G, V], for citrus_first_collision_moments. The quadrature sums run over
+ * the directions in the order of their cosine with each block's first point (a rounding-level difference from the
+ * reference's direction order). */
 int citrus_first_collision_correction(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
                                       const float* axes, const int64_t* point_dims, const double* focal_spot,
                                       const float* table, int64_t num_eta, double eta_lo, double eta_hi,
                                       const float* omegas, const float* weights, int64_t num_directions,
-                                      const float* moments, float* sums, float* scale, float* beta, void* stream);
+                                      const float* moments, float* sums, float* scale, float* beta, float* cache,
+                                      void* stream);
 
-/* Attenuated total emission of the collapsed-cone image: (S_FC + multiple[k, g, cell]) exp(-max(0, tau[k, g, cell]
+/* Attenuated total emission of the collapsed-cone image: (S_FC + multiple[k, cell, g]) exp(-max(0, tau[k, cell, g]
  * - mu[g, cell] omega . (r - r_cell))) written voxel-major out [K, V, G], or with signal_weight [K, G] its weighted
  * group sum [K, V]; height_sums [K, 2] = (sum e, sum e h) with the panel heights h [V] (NULL: 0), summed in a fixed
- * order through partial [K, ceil(V / 32), 2] (device scratch of partial_capacity floats).
+ * order through partial [K, ceil(V / 32), 2] (device scratch of partial_capacity floats). With tau_mu [TM, G]
+ * (NULL: none), tau holds material path lengths [K, NC, TM] (TM = tau_materials, the downstream trace of the cell
+ * densities) and the optical depth is tau[k, cell, g] = sum_m tau_mu[m, g] P[k, cell, m].
  * Replaces attenuated_emission (uncollided_kernels.py:712-795, 1138-1205) and supervoxel_subpoint_emission
  * (scatter_image.py:829-874). */
 int citrus_attenuated_emission(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
                                const float* axes, const int64_t* point_dims, int64_t points_per_cell,
                                const double* point_deltas, const double* focal_spot, const float* table,
                                int64_t num_eta, double eta_lo, double eta_hi, const float* omegas,
-                               int64_t num_directions, const float* tau, const float* mu, const float* multiple,
-                               const float* heights, const float* signal_weight, float* out, float* partial,
-                               int64_t partial_capacity, float* height_sums, void* stream);
+                               int64_t num_directions, const float* tau, const float* tau_mu, int64_t tau_materials,
+                               const float* mu, const float* multiple, const float* heights,
+                               const float* signal_weight, float* out, float* partial, int64_t partial_capacity,
+                               float* height_sums, void* stream);
+
+/* The same emission with the multiple-collision source formed in registers, S_MC[k, g, cell] = sum_n
+ * harmonics[k, n] moments[n, cell, g] (harmonics [K, num_moments], moments [num_moments, NC, G], num_moments <= 64),
+ * instead of read from a [K, NC, G] buffer. Replaces the product torch.mm(harmonics, moments) of
+ * scatter_image.py:1246 together with attenuated_emission (uncollided_kernels.py:1138-1205). */
+int citrus_attenuated_emission_moments(const float* rho, int64_t num_materials, const float* phi, int64_t num_groups,
+                                       const float* axes, const int64_t* point_dims, int64_t points_per_cell,
+                                       const double* point_deltas, const double* focal_spot, const float* table,
+                                       int64_t num_eta, double eta_lo, double eta_hi, const float* omegas,
+                                       int64_t num_directions, const float* tau, const float* tau_mu,
+                                       int64_t tau_materials, const float* mu, const float* harmonics,
+                                       const float* moments, int64_t num_moments,
+                                       const float* heights, const float* signal_weight, float* out, float* partial,
+                                       int64_t partial_capacity, float* height_sums, void* stream);
 
 /* ------------------------------------------------------------------------------------------------------------------
  * Finite-cone footprint and accumulation of the collapsed-cone image (scatter_image.py:897-1135, 1234-1323).

@@ -19,7 +19,7 @@ def _declared_functions() -> list:
     names = []
     for header in sorted((ROOT / "include").glob("*.h")):
         text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
-        names += re.findall(r"^\s*(?:const\s+)?(?:int|char\s*\*|const char\s*\*)\s*\*?\s*(citrus_\w+)\s*\(", text,
+        names += re.findall(r"^\s*(?:const\s+)?(?:int64_t|int|char\s*\*|const char\s*\*)\s*\*?\s*(citrus_\w+)\s*\(", text,
                             flags=re.M)
     return sorted(set(names))
 

@@ -99,3 +99,34 @@ def test_oblique_line_grazing_a_box_face(cuda_device):
     got = GB300Projectors().oblique_project(torch.as_tensor(field, dtype=torch.float32, device=cuda_device), grid,
                                             geo, 0.6, torch.as_tensor(om, dtype=torch.float32, device=cuda_device))
     assert rel_err(got, ref) < 1e-5
+
+
+@pytest.mark.parametrize("channels", [1, 2, 3, 8])
+@pytest.mark.parametrize("curved", [False, True])
+def test_downstream_lattice_walk_matches_per_ray_walk_and_oracle(cuda_device, channels, curved):
+    """The shared per-direction crossing table against the independent per-ray walk and the float64 oracle, with
+    directions along the axes, in the planes of two axes and oblique, on a grid with unequal voxel sizes."""
+    grid = Grid((9, 7, 6), 1.1, 0.8 / 1.1, 1.3 / 1.1)
+    rng = np.random.default_rng(channels)
+    vol_np = rng.random((channels, *grid.shape))
+    geo = ConeGeometry(30.0, 45.0, 10, 12, 1.5, 1.5, use_curved_detector=curved)
+    angle = 0.4
+    n_hat = np.asarray(geo.panel_axes(angle)[2])
+    om = rng.standard_normal((40, 3))
+    om[0] = -n_hat
+    om[1] = [0.0, 0.0, 1.0]
+    om[2] = [1.0, 0.0, 0.0]
+    om[3] = [0.0, -1.0, 0.0]
+    om[4] = [0.6, -0.8, 0.0]
+    om[5] = [0.0, 0.6, 0.8]
+    om /= np.linalg.norm(om, axis=1, keepdims=True)
+    om32 = om.astype(np.float32)
+    vol = torch.as_tensor(vol_np, dtype=torch.float32, device=cuda_device)
+    omt = torch.as_tensor(om32, device=cuda_device)
+    p = GB300Projectors()
+    lattice = p.downstream_cumulative(vol, grid, geo, angle, omt).cpu().numpy()
+    walk = p.downstream_cumulative(vol, grid, geo, angle, omt, lattice=False).cpu().numpy()
+    ref = siddon.downstream_cumulative(vol_np, grid, geo, angle, om32.astype(np.float64))
+    assert np.array_equal(np.isinf(lattice), np.isinf(ref))
+    assert finite_rel_err(lattice, walk) < 1e-5
+    assert finite_rel_err(lattice, ref) < 1e-5

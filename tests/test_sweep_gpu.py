@@ -98,7 +98,10 @@ def test_persistent_barrier_timeout_is_reported(cuda_device):
 
 @pytest.mark.parametrize("M, K, J, batch, accumulate", [(120, 36, 4096, 1, False), (36, 120, 1028, 1, True),
                                                         (5, 7, 64, 3, True), (240, 64, 512, 2, False),
-                                                        (1, 1, 4, 1, False)])
+                                                        (1, 1, 4, 1, False), (133, 36, 515, 1, True),
+                                                        (129, 17, 1000, 2, False), (64, 65, 777, 1, True),
+                                                        (3, 300, 258, 2, False), (100, 80, 96, 1, True),
+                                                        (512, 36, 2050, 1, False)])
 def test_small_k_gemm_matches_numpy(cuda_device, M, K, J, batch, accumulate):
     rng = np.random.default_rng(M * 7 + K)
     A = rng.standard_normal((M, K))

@@ -72,3 +72,17 @@ def test_config_library_first_collision_on_refined_grid(cuda_device):
     got = first_collision_moments_at_directions(library, dev(rho), dev(phi), grid, geo, 1.1, dev(q.omega[:16]), corr,
                                                 3, cell_major=False)
     assert rel_err(got, ref) < 2e-5
+    # the kept source values read back at scattered rows give the same moments
+    kept = first_collision_sampling_correction(library, dev(rho), dev(phi), grid, geo, 1.1, dev(q.omega),
+                                               dev(q.weight), keep_cache=True)
+    assert torch.equal(kept.scale, corr.scale) and torch.equal(kept.beta, corr.beta)
+    rows = torch.tensor([5, 0, 77, 119, 31, 64], device=cuda_device)
+    cached = first_collision_moments_at_directions(library, dev(rho), dev(phi), grid, geo, 1.1,
+                                                   dev(q.omega)[rows], kept, 3, cell_major=False,
+                                                   direction_index=rows)
+    direct = first_collision_moments_at_directions(library, dev(rho), dev(phi), grid, geo, 1.1, dev(q.omega)[rows],
+                                                   kept, 3, cell_major=False)
+    assert rel_err(cached, direct) < 1e-6
+    ref_rows = physics.first_collision_moments(library, rho, phi, grid, geo, 1.1, q.omega[rows.cpu().numpy()], scale,
+                                               beta, 3)
+    assert rel_err(cached, ref_rows) < 2e-5
