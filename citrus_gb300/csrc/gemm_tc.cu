@@ -1,0 +1,277 @@
+// Small-K matrix products C[b] (=|+=) A @ B[b] on the 5th-generation tensor cores (tcgen05), BF16 inputs with a
+// split-precision correction and FP32 accumulation in tensor memory.
+//
+// Each float32 operand x is split into x_hi = bf16(x) and x_lo = bf16(x - x_hi); the product is formed as
+// A_hi B_hi + A_hi B_lo + A_lo B_hi (the A_lo B_lo term is below the float32 rounding of the sum), which keeps about
+// sixteen bits of every input: relative errors near 1e-5 instead of bfloat16's 4e-3. The contraction of the
+// scattering source has a short inner dimension (K <= 128) and a very long column dimension J, so the kernel streams
+// J in tiles of 128 columns:
+//
+//   * A (M <= 128 rows, zero-padded to 128) is split once per CTA into shared memory in the K-major canonical layout
+//     without swizzle: 8-row x 16-byte core matrices, adjacent in K 128 bytes apart (leading byte offset) and in M 256
+//     bytes apart (stride byte offset), one region per 16-wide K step.
+//   * Per tile, thread t reads column t of B in groups of 8 rows (coalesced across the warp), splits it and writes
+//     one 16-byte core-matrix row of B_hi and of B_lo: the same K-major layout with N in place of M.
+//   * One thread issues the 3 x (K / 16) MMAs (M = 128, N = 128, K = 16, kind::f16 with bf16 operands) into a
+//     128-lane x 128-column float32 accumulator in tensor memory and commits them to an mbarrier; every wait on it is
+//     bounded by a wall-clock limit, after which the CTA records the error and leaves.
+//   * The four warps read their 32 lanes of the accumulator (tcgen05.ld 32x32b) and store or add the rows of C.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace citrus {
+namespace {
+
+constexpr int kTcThreads = 128;  // four warps: warp w owns accumulator lanes 32w .. 32w + 31
+constexpr int kTcM = 128;        // MMA rows (A rows, zero-padded)
+constexpr int kTcN = 128;        // MMA columns per tile (B columns)
+constexpr int kTcMaxK = 128;     // inner dimension, padded to a multiple of 16
+constexpr uint64_t kTcTimeoutNs = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// bf16 bits of x, round to nearest even (finite inputs)
+__device__ __forceinline__ uint32_t bf16_bits(float x) {
+  const uint32_t u = __float_as_uint(x);
+  return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+}
+
+__device__ __forceinline__ void split_pair(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+  const uint32_t h0 = bf16_bits(x0), h1 = bf16_bits(x1);
+  const float r0 = x0 - __uint_as_float(h0 << 16), r1 = x1 - __uint_as_float(h1 << 16);
+  hi = h0 | (h1 << 16);
+  lo = bf16_bits(r0) | (bf16_bits(r1) << 16);
+}
+
+// Shared-memory matrix descriptor, K-major, no swizzle: start address, leading byte offset (between core matrices
+// adjacent in K), stride byte offset (between 8-row groups), the descriptor version bit of this architecture.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;  // base offset 0, swizzle none
+}
+
+// Instruction descriptor of kind::f16: bf16 A and B, float32 accumulator, both K-major, N = 128, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                            ((uint32_t)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint64_t t0) {
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (global_timer_ns() - t0 > kTcTimeoutNs) return false;
+  }
+}
+
+// Core-matrix byte offset of element row r (M or N index), column k (K index) inside one 16-wide K step region.
+__device__ __forceinline__ uint32_t core_offset(int r, int k) {
+  return (uint32_t)((((r >> 3) * 2 + (k >> 3)) * 128) + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __restrict__ A, int64_t lda,
+                                                             const float* __restrict__ B, int64_t ldb,
+                                                             float* __restrict__ C, int64_t ldc, int M, int K,
+                                                             int64_t J, int64_t stride_b, int64_t stride_c,
+                                                             int accumulate, int64_t tiles_per_batch,
+                                                             int64_t num_tiles, uint32_t* __restrict__ error_word) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int KS = (K + 15) / 16;            // K steps
+  const uint32_t a_step = kTcM * 16 * 2;   // bytes of one K step of A (4 KB)
+  const uint32_t b_step = kTcN * 16 * 2;   // bytes of one K step of B (4 KB)
+  uint8_t* a_hi = smem;
+  uint8_t* a_lo = a_hi + KS * a_step;
+  uint8_t* b_hi = a_lo + KS * a_step;
+  uint8_t* b_lo = b_hi + KS * b_step;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+
+  // A, split once: thread t packs rows t of all K steps, 8 columns (one core-matrix row) at a time
+  for (int s = 0; s < KS; ++s) {
+    for (int k8 = 0; k8 < 16; k8 += 8) {
+      float x[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = s * 16 + k8 + q;
+        x[q] = (tid < M && k < K) ? A[(int64_t)tid * lda + k] : 0.f;
+      }
+      uint4 hi, lo;
+      split_pair(x[0], x[1], hi.x, lo.x);
+      split_pair(x[2], x[3], hi.y, lo.y);
+      split_pair(x[4], x[5], hi.z, lo.z);
+      split_pair(x[6], x[7], hi.w, lo.w);
+      const uint32_t off = s * a_step + core_offset(tid, k8);
+      *reinterpret_cast<uint4*>(a_hi + off) = hi;
+      *reinterpret_cast<uint4*>(a_lo + off) = lo;
+    }
+  }
+  if (tid == 0) {
+    abort_flag = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // the accumulator: 128 lanes x 128 float32 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"((uint32_t)kTcN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const uint32_t mbar_addr = smem_u32(&mbar);
+  uint32_t phase = 0;
+
+  for (int64_t tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+    const int64_t bz = tile / tiles_per_batch;
+    const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
+    const float* Bz = B + bz * stride_b;
+    float* Cz = C + bz * stride_c;
+    // B tile: column n0 + tid, split into the K-major layout
+    const int64_t col = n0 + tid;
+    const bool cvalid = col < J;
+    for (int s = 0; s < KS; ++s) {
+      for (int k8 = 0; k8 < 16; k8 += 8) {
+        float x[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int k = s * 16 + k8 + q;
+          x[q] = (cvalid && k < K) ? __ldg(Bz + (int64_t)k * ldb + col) : 0.f;
+        }
+        uint4 hi, lo;
+        split_pair(x[0], x[1], hi.x, lo.x);
+        split_pair(x[2], x[3], hi.y, lo.y);
+        split_pair(x[4], x[5], hi.z, lo.z);
+        split_pair(x[6], x[7], hi.w, lo.w);
+        const uint32_t off = s * b_step + core_offset(tid, k8);
+        *reinterpret_cast<uint4*>(b_hi + off) = hi;
+        *reinterpret_cast<uint4*>(b_lo + off) = lo;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the operands, visible to the tensor cores
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int s = 0; s < KS; ++s) {
+        const uint64_t ah = smem_desc(smem_u32(a_hi + s * a_step), 128, 256);
+        const uint64_t al = smem_desc(smem_u32(a_lo + s * a_step), 128, 256);
+        const uint64_t bh = smem_desc(smem_u32(b_hi + s * b_step), 128, 256);
+        const uint64_t bl = smem_desc(smem_u32(b_lo + s * b_step), 128, 256);
+        mma_bf16(tmem, ah, bh, s > 0 ? 1u : 0u);
+        mma_bf16(tmem, ah, bl, 1u);
+        mma_bf16(tmem, al, bh, 1u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
+                   : "memory");
+    }
+    const bool ok = mbar_wait(mbar_addr, phase, global_timer_ns());
+    phase ^= 1u;
+    if (!ok) {
+      if (error_word != nullptr) atomicExch(error_word, 1u);
+      abort_flag = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (abort_flag) break;
+    // epilogue: row 32 warp + lane, 32 columns per load
+    const int row = warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcN; c0 += 32) {
+      uint32_t r[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < M) {
+        float* out = Cz + (int64_t)row * ldc + n0 + c0;
+        const int64_t left = J - (n0 + c0);
+        if (left >= 32 && ((uintptr_t)out % 16) == 0) {
+#pragma unroll
+          for (int q = 0; q < 32; q += 4) {
+            float4 v = make_float4(__uint_as_float(r[q]), __uint_as_float(r[q + 1]), __uint_as_float(r[q + 2]),
+                                   __uint_as_float(r[q + 3]));
+            if (accumulate) {
+              const float4 o = reinterpret_cast<const float4*>(out)[q / 4];
+              v.x += o.x;
+              v.y += o.y;
+              v.z += o.z;
+              v.w += o.w;
+            }
+            reinterpret_cast<float4*>(out)[q / 4] = v;
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 32; ++q)
+            if (q < left) out[q] = accumulate ? out[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // the accumulator and the B tile are free for the next tile
+  }
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kTcN) : "memory");
+}
+
+}  // namespace
+}  // namespace citrus
+
+using namespace citrus;
+
+extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                                          int64_t ldc, int64_t M, int64_t K, int64_t J, int64_t batch,
+                                          int64_t stride_b, int64_t stride_c, int32_t accumulate,
+                                          uint32_t* error_word, void* stream) {
+  CITRUS_REQUIRE(A && B && C, "citrus_small_k_gemm_bf16x3: null pointer argument");
+  CITRUS_REQUIRE(M >= 1 && M <= kTcM && K >= 1 && K <= kTcMaxK && J >= 0 && batch >= 1,
+                 "citrus_small_k_gemm_bf16x3: M %lld (<= %d) or K %lld (<= %d) out of range", (long long)M, kTcM,
+                 (long long)K, kTcMaxK);
+  CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "citrus_small_k_gemm_bf16x3: leading dimensions too small");
+  if (J == 0) return CITRUS_OK;
+  const int KS = (int)((K + 15) / 16);
+  // operands, and at least 60 KB so that no more than three CTAs (3 x 128 of the 512 tensor-memory columns) share
+  // an SM: every CTA's allocation then succeeds at once
+  const size_t smem = std::max<size_t>((size_t)KS * (2 * kTcM * 16 * 2 + 2 * kTcN * 16 * 2), 60 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: %s", cudaGetErrorString(e));
+  const int64_t tiles_per_batch = cdiv(J, kTcN);
+  const int64_t num_tiles = tiles_per_batch * batch;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gemm_tc_kernel, kTcThreads, smem);
+  if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: occupancy query");
+  if (per_sm > 3) per_sm = 3;
+  const int64_t grid = std::min<int64_t>(num_tiles, (int64_t)per_sm * num_sms());
+  gemm_tc_kernel<<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(A, lda, B, ldb, C, ldc, (int)M, (int)K, J,
+                                                                         stride_b, stride_c, accumulate,
+                                                                         tiles_per_batch, num_tiles, error_word);
+  note_launches();
+  return launch_status("citrus_small_k_gemm_bf16x3");
+}

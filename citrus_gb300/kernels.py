@@ -129,11 +129,20 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
 # small-K products
 # =====================================================================================================================
 
-def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False) -> Tensor:
+PRECISIONS = ("fp32", "bf16x3")
+
+
+def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, precision: str = "fp32",
+                 error_word: Optional[Tensor] = None) -> Tensor:
     """``C (=|+=) A @ B`` for A [M, K] and B, C [.., K or M, J] row-major 2-D (or batched 3-D) views.
 
-    B and C may be strided views whose last axis is contiguous; J must be a multiple of 4.
+    B and C may be strided views whose last axis is contiguous. ``precision`` "fp32" multiplies in float32 on the CUDA
+    cores; "bf16x3" splits both operands into bfloat16 high and low parts and accumulates A_hi B_hi + A_hi B_lo +
+    A_lo B_hi in float32 on the tcgen05 tensor cores (M <= 128, K <= 128; ``error_word``, an int32 device tensor,
+    becomes non-zero if a wait for the tensor cores ran out).
     """
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
     _check_cuda_f32("A", A, contiguous=False)
     _check_cuda_f32("B", B, contiguous=False)
     _check_cuda_f32("C", C, contiguous=False)
@@ -149,9 +158,13 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False) -> T
         raise ValueError(f"shape mismatch: A {tuple(A.shape)}, B {tuple(B.shape)}, C {tuple(C.shape)}")
     if B.stride(2) != 1 or C.stride(2) != 1:
         raise ValueError("B and C need a contiguous last axis")
-    _lib.call("citrus_small_k_gemm", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(), C.stride(1),
-              M, K, J, batch, B.stride(0) if batch > 1 else 0, C.stride(0) if batch > 1 else 0, int(bool(accumulate)),
-              _lib.stream_handle(A.device))
+    args = (A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(), C.stride(1), M, K, J, batch,
+            B.stride(0) if batch > 1 else 0, C.stride(0) if batch > 1 else 0, int(bool(accumulate)))
+    if precision == "bf16x3":
+        _lib.call("citrus_small_k_gemm_bf16x3", *args, None if error_word is None else error_word.data_ptr(),
+                  _lib.stream_handle(A.device))
+    else:
+        _lib.call("citrus_small_k_gemm", *args, _lib.stream_handle(A.device))
     return C
 
 

@@ -90,6 +90,16 @@ int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb
                         int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int32_t accumulate,
                         void* stream);
 
+/* The same product on the tcgen05 tensor cores, M <= 128 and K <= 128: each float32 operand is split into a bfloat16
+ * high part and a bfloat16 low part (x - hi), the product accumulated in float32 as A_hi B_hi + A_hi B_lo + A_lo B_hi
+ * (relative error ~1e-5 of the largest term). error_word (NULL: none), when given, is set to 1 if a wait for the
+ * tensor cores ran out (the result is then invalid). The BF16 hi/lo scattering-source contraction of the mixed-
+ * precision configuration; no counterpart in the reference, which contracts in float32 (transport_sweep.py:524-528,
+ * source_iteration.py:94-103, scatter_image.py:1246). */
+int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                               int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
+                               int32_t accumulate, uint32_t* error_word, void* stream);
+
 /* ------------------------------------------------------------------------------------------------------------------
  * Spherical-harmonic moments of the scattering source,
  * T[g, n, k, x] = sum_g' transfer[g', g, l(n), x] phi[g', n, k, x], phi and T through element strides.

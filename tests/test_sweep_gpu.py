@@ -114,6 +114,27 @@ def test_small_k_gemm_matches_numpy(cuda_device, M, K, J, batch, accumulate):
     assert rel_err(C, expected) < 1e-5
 
 
+@pytest.mark.parametrize("M, K, J, batch, accumulate", [(120, 36, 4096, 1, False), (36, 120, 1028, 1, True),
+                                                        (5, 7, 64, 3, True), (1, 1, 4, 1, False),
+                                                        (128, 128, 333, 2, True), (64, 36, 130, 1, False)])
+def test_bf16x3_tensor_core_gemm_error_against_float64(cuda_device, M, K, J, batch, accumulate):
+    """The bfloat16 hi/lo product on the tensor cores: its error against float64 stays at the split's ~1e-5 of the
+    largest term, far below bfloat16's own."""
+    rng = np.random.default_rng(M * 13 + K)
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((batch, K, J))
+    C0 = rng.standard_normal((batch, M, J))
+    expected = np.einsum("mk,bkj->bmj", A, B) + (C0 if accumulate else 0)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    C = dev(C0)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+    kernels.small_k_gemm(dev(A), dev(B), C, accumulate=accumulate, precision="bf16x3", error_word=err)
+    torch.cuda.synchronize()
+    assert int(err[0]) == 0
+    scale = np.abs(A).max() * np.abs(B).max() * K
+    assert np.abs(C.cpu().numpy() - expected).max() / scale < 3e-5
+
+
 def test_scattering_moments_match_reference_fixture(cuda_device):
     g = golden("scatter_moments_small")
     dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
