@@ -40,6 +40,9 @@ def _parse():
     p.add_argument("--method", default="persistent", choices=["persistent", "planes"])
     p.add_argument("--dc", type=int, default=0, help="directions per octant per sweep chunk (0: all)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    p.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3"],
+                   help="arithmetic of the spherical-harmonic products (bf16x3: tcgen05 tensor cores, hi/lo split)")
+    p.add_argument("--batch", type=int, default=1, help="views per persistent sweep launch (1: citrus_view_step)")
     p.add_argument("--cells", type=int, default=64, help="cells per axis of the step workload (64; smaller for "
                                                          "profiling captures)")
     return p.parse_args()
@@ -380,7 +383,7 @@ def cpu_baseline_step(cells: int = 64, image_directions: int = 1, fc_directions:
 # the scatter step of every view
 # =====================================================================================================================
 
-def make_step_solver(device, views: int = 0, cells: int = 64):
+def make_step_solver(device, views: int = 0, cells: int = 64, precision: str = "fp32"):
     """The batched-views workload: solver, fields input, view angles (64^3, G = 8, P5, 120 directions, curved 256 x 192
     panel, cone 16 x 32, ideal counting detector, no grid)."""
     from citrus_gb300.responses import ideal_counting_response, no_grid
@@ -391,7 +394,7 @@ def make_step_solver(device, views: int = 0, cells: int = 64):
     config = SolverConfig(num_groups=w.library.num_groups, legendre_order=w.legendre_order, num_polar=w.num_polar,
                           num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
                           quadrature_point_spacing_cm=0.5, cone_num_polar=w.cone_num_polar,
-                          cone_num_azimuthal=w.cone_num_azimuthal)
+                          cone_num_azimuthal=w.cone_num_azimuthal, moment_precision=precision)
     solver = ScatterSolver(w.library, config, w.geometry, detector=ideal_counting_response(), grid_response=no_grid(),
                            device=device)
     angles = w.angles()
@@ -472,10 +475,39 @@ def count_launches(fn) -> dict:
     return {"citrus": _lib.launch_count() - before}
 
 
+def spr_error(w, solver, angles, device) -> dict:
+    """Scatter-to-primary ratio of the first step of a few views in the solver's moment precision against the float32
+    products: max over panel pixels of |SPR - SPR_fp32| / SPR_fp32, and the scatter signal's error relative to its
+    maximum."""
+    import dataclasses
+
+    import torch
+
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step
+    from citrus_gb300.scatter_solver import ScatterSolver
+
+    ref_solver = ScatterSolver(solver.library, dataclasses.replace(solver.config, moment_precision="fp32"),
+                               solver.geometry, detector=solver.detector, grid_response=solver.grid_response,
+                               device=device)
+    rho = torch.as_tensor(w.rho, dtype=torch.float32, device=device)
+    fields, ref_fields = solver.material_fields(rho, w.grid), ref_solver.material_fields(rho, w.grid)
+    worst_spr, worst_signal = 0.0, 0.0
+    for angle in angles:
+        s, p, _ = citrus_view_step(solver, CitrusState(), fields, float(angle), primary=True)
+        s_ref, _, _ = citrus_view_step(ref_solver, CitrusState(), ref_fields, float(angle), primary=False)
+        mask = p > 1e-3 * p.max()
+        spr, spr_ref = s[mask] / p[mask], s_ref[mask] / p[mask]
+        worst_spr = max(worst_spr, float(((spr - spr_ref).abs() / spr_ref.abs().clamp_min(1e-30)).max()))
+        worst_signal = max(worst_signal, float((s - s_ref).abs().max() / s_ref.abs().max()))
+    return {"against": "the same step with float32 spherical-harmonic products", "views": len(angles),
+            "spr_max_rel": worst_spr, "signal_max_rel": worst_signal}
+
+
 def run_step(args):
     import torch
 
     from citrus_gb300 import _lib
+    from citrus_gb300.batched import batched_view_steps
     from citrus_gb300.citrus_step import CitrusState, citrus_view_step
 
     rank = int(os.environ.get("RANK", "0"))
@@ -487,7 +519,7 @@ def run_step(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=device)
-    w, solver, angles = make_step_solver(device, args.views, args.cells)
+    w, solver, angles = make_step_solver(device, args.views, args.cells, args.precision)
     # weak scaling: every rank runs its own set of views (offset by the rank) of the same phantom
     angles = angles + rank * (2 * math.pi / len(angles)) / max(1, world)
     V = len(angles)
@@ -498,6 +530,13 @@ def run_step(args):
 
     def one_step(rho, signals=None):
         fields = solver.material_fields(rho, w.grid)
+        if args.batch > 1:
+            out, _, new_states = batched_view_steps(solver, states, fields, [float(a) for a in angles],
+                                                    batch=args.batch)
+            states[:] = new_states
+            if signals is not None:
+                signals.copy_(out, non_blocking=True)
+            return
         for v, angle in enumerate(angles):
             scatter, _, states[v] = citrus_view_step(solver, states[v], fields, float(angle), primary=False)
             if signals is not None:
@@ -546,6 +585,7 @@ def run_step(args):
     torch.cuda.synchronize()
     e2e = e0.elapsed_time(e1) / 1e3
     launches = count_launches(lambda: one_step(rho_dev))
+    spr = spr_error(w, solver, angles[:2], device) if args.precision != "fp32" else None
     ms_per_view = elapsed * 1e3 / (args.steps * V)
     N = w.grid.num_voxels
     updates = 8 * (w.num_polar * w.num_azimuthal // 8) * N * w.library.num_groups
@@ -557,7 +597,8 @@ def run_step(args):
         "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom and library)",
         "config": {"workload": step_workload_name(args.cells, V),
-                   "l2": "inputs larger than L2 (4 GB sweep store per view)"},
+                   "l2": "inputs larger than L2 (4 GB sweep store per view)",
+                   "moment_precision": args.precision, "views_per_sweep_launch": args.batch},
         "updates_per_s": updates * V * args.steps * world / elapsed,
         "e2e": {"value": e2e * 1e3 / (args.steps * V) / max(1, world), "unit": "ms/view",
                 "h2d_bytes_per_step": rho_host.numel() * 4, "d2h_bytes_per_step": host_signals.numel() * 4},
@@ -572,6 +613,8 @@ def run_step(args):
                                     for n, t in sorted(per_entry.items(), key=lambda x: -sum(x[1]))},
         "clocks": sampler.summary(),
     }
+    if spr is not None:
+        line["spr_error"] = spr
     if rank == 0:
         line["cpu_baseline"] = None if args.no_cpu else cpu_baseline_step(cells=args.cells)
         print(json.dumps(line), flush=True)

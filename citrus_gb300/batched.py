@@ -26,6 +26,7 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
     Returns (scatter signals [V, Rd, Cd], primary signals [V, Rd, Cd] or None, new states).
     """
     ctx = solver.sweep_context(fields.grid_coarse)
+    precision = solver.config.moment_precision
     G, N, N_sh, D8 = solver.num_groups, ctx.num_cells, ctx.num_moments, ctx.directions_per_octant
     Q = 4 * G
     J = N * Q
@@ -59,11 +60,11 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
                 if p is not None:
                     kernels.scattering_moments(fields.mu_s_l_coarse, p, "cell_major",
                                                out=T_all[j].view((N_sh,) + shape + (G, 4)))
-            kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True)
+            kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
             del T_all
         kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c, method="persistent")
         moments = torch.empty(B, N_sh, J, device=device)
-        kernels.small_k_gemm(Yw_t, store.view(B, 8 * D8, J), moments)
+        kernels.small_k_gemm(Yw_t, store.view(B, 8 * D8, J), moments, precision=precision)
         del store
         for j, v in enumerate(views):
             new = moments[j].view(N_sh, N, G, 4).permute(2, 0, 3, 1).reshape(G, N_sh, 4, *shape)

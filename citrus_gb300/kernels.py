@@ -158,13 +158,21 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, prec
         raise ValueError(f"shape mismatch: A {tuple(A.shape)}, B {tuple(B.shape)}, C {tuple(C.shape)}")
     if B.stride(2) != 1 or C.stride(2) != 1:
         raise ValueError("B and C need a contiguous last axis")
-    args = (A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(), C.stride(1), M, K, J, batch,
-            B.stride(0) if batch > 1 else 0, C.stride(0) if batch > 1 else 0, int(bool(accumulate)))
-    if precision == "bf16x3":
-        _lib.call("citrus_small_k_gemm_bf16x3", *args, None if error_word is None else error_word.data_ptr(),
-                  _lib.stream_handle(A.device))
-    else:
-        _lib.call("citrus_small_k_gemm", *args, _lib.stream_handle(A.device))
+    sb, sc = (B.stride(0), C.stride(0)) if batch > 1 else (0, 0)
+    stream = _lib.stream_handle(A.device)
+    if precision == "fp32":
+        _lib.call("citrus_small_k_gemm", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
+                  C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), stream)
+        return C
+    # the tensor-core product takes at most 128 rows and 128 inner terms per call: tiles of A, partial sums added
+    err = None if error_word is None else error_word.data_ptr()
+    for r0 in range(0, M, 128):
+        rows = min(128, M - r0)
+        for k0 in range(0, K, 128):
+            inner = min(128, K - k0)
+            _lib.call("citrus_small_k_gemm_bf16x3", A[r0:, k0:].data_ptr(), A.stride(0),
+                      B[:, k0:].data_ptr(), B.stride(1), C[:, r0:].data_ptr(), C.stride(1), rows, inner, J, batch,
+                      sb, sc, int(bool(accumulate) or k0 > 0), err, stream)
     return C
 
 

@@ -197,13 +197,14 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
                            geometry: ConeGeometry, angle: float, mu_t_coarse: Tensor, projectors,
                            context: DirectionSetContext, grid_coarse: Optional[Grid] = None,
                            signal_only: bool = False, footprint: bool = True, rho_coarse: Optional[Tensor] = None,
-                           attenuation: Optional[Tensor] = None) -> dict:
+                           attenuation: Optional[Tensor] = None, precision: str = "fp32") -> dict:
     """Total scatter image of one view, first order plus multiple collision (reference ``scatter_image.py:1141-1323``).
 
     Returns ``{"signal": [Rd, Cd]}`` with ``signal_only``, else fluence, planar_fluence and signal_per_group
     [G, Rd, Cd] and signal [Rd, Cd]. When ``mu_t_coarse`` is ``sum_m attenuation[m, g] rho_coarse[m]`` (the solver's
     fields) and both are given, the downstream optical depths are traced through the M cell densities instead of the
     G attenuation channels and combined per group in the emission (the same line integrals, by linearity).
+    ``precision`` is the arithmetic of the multiple-collision product ``Y_k T`` (``kernels.small_k_gemm``).
     """
     device = phi_uncollided.device
     f = int(q)
@@ -260,7 +261,7 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
             _lib.call("citrus_attenuated_emission_moments", *head, Yk.data_ptr(), T.data_ptr(), N_sh, *tail)
         else:
             multiple = torch.empty(k, NC * G, device=device)                               # [k, cells, G]
-            kernels.small_k_gemm(Yk, T, multiple)
+            kernels.small_k_gemm(Yk, T, multiple, precision=precision)
             _lib.call("citrus_attenuated_emission", *head, multiple.data_ptr(), *tail)
             del multiple
         del tau

@@ -56,6 +56,7 @@ class SolverConfig:
     cone_num_azimuthal: int = 32
     direction_chunk: int = 8
     dtype: str = "float32"
+    moment_precision: str = "fp32"  # the spherical-harmonic products: "fp32" or "bf16x3" (tensor-core hi/lo split)
 
     def quadrature_points(self, fine_voxel_cm: float) -> int:
         """q = min(max(1, round(cell / spacing)), max(1, round(cell / voxel))) (reference ``config.py:130-144``)."""
@@ -73,6 +74,8 @@ class SolverConfig:
             raise ValueError(f"num_azimuthal={self.num_azimuthal} must be >= 2*legendre_order+1={2 * L + 1}")
         if self.num_polar % 2 or self.num_azimuthal % 4:
             raise ValueError("the sweep set needs an even num_polar and num_azimuthal divisible by 4")
+        if self.moment_precision not in kernels.PRECISIONS:
+            raise ValueError(f"moment_precision must be one of {kernels.PRECISIONS}")
         if self.uncollided_trace_grid not in ("coarse", "quadrature", "fine"):
             raise ValueError(f"uncollided_trace_grid must be 'coarse', 'quadrature' or 'fine'")
         if self.max_source_iterations < 1 or self.source_iteration_tolerance <= 0:
@@ -276,16 +279,18 @@ class ScatterSolver:
     def scatter_moment_source(self, fields: MaterialFields, phi: Tensor,
                               sweep_context: Optional[SweepContext] = None):
         ctx = self.sweep_context(fields.grid_coarse) if sweep_context is None else sweep_context
-        return scatter_source_function(ctx, scatter_moments(fields.mu_s_l_coarse, phi))
+        return scatter_source_function(ctx, scatter_moments(fields.mu_s_l_coarse, phi),
+                                       precision=self.config.moment_precision)
 
     def transport_sweep(self, fields: MaterialFields, source_function) -> Tensor:
         return sweep(self.sweep_context(fields.grid_coarse), fields.mu_t_coarse, source_function,
-                     direction_chunk=self.sweep_direction_chunk(fields))
+                     direction_chunk=self.sweep_direction_chunk(fields), precision=self.config.moment_precision)
 
     def run_source_iteration(self, fields: MaterialFields, first_collision_source_function) -> SourceIterationResult:
         return source_iteration(self.sweep_context(fields.grid_coarse), fields.mu_t_coarse, fields.mu_s_l_coarse,
                                 first_collision_source_function, self.config.source_iteration_tolerance,
-                                self.config.max_source_iterations, self.sweep_direction_chunk(fields))
+                                self.config.max_source_iterations, self.sweep_direction_chunk(fields),
+                                precision=self.config.moment_precision)
 
     def multiple_collision_source_moments(self, fields: MaterialFields, phi_collided: Tensor) -> Tensor:
         return multiple_collision_source_moments(fields.mu_s_l_coarse, phi_collided)
@@ -298,7 +303,8 @@ class ScatterSolver:
                                       fields.q, scatter_source_moments, self.L, self.geometry, angle,
                                       fields.mu_t_coarse, self.projectors, context, fields.grid_coarse,
                                       signal_only=signal_only, rho_coarse=fields.rho_coarse,
-                                      attenuation=self.transport_library.tensor("mu_t", self.device))
+                                      attenuation=self.transport_library.tensor("mu_t", self.device),
+                                      precision=self.config.moment_precision)
 
     def primary(self, fields: MaterialFields, angle: float) -> dict:
         return primary_image(self.library, fields.rho_fine, fields.grid_fine, self.geometry, angle, self.source,

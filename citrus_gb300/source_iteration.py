@@ -37,8 +37,9 @@ def scatter_moments(mu_s_l_volume: Tensor, phi: Tensor) -> Tensor:
     return kernels.scattering_moments(mu_s_l_volume, phi, "cell_major")
 
 
-def scatter_source_function(ctx: SweepContext, T: Tensor):
-    """Source function of the scattering source with moments T (reference ``source_iteration.py:65-106``).
+def scatter_source_function(ctx: SweepContext, T: Tensor, precision: str = "fp32"):
+    """Source function of the scattering source with moments T (reference ``source_iteration.py:65-106``); the
+    expansion ``Y @ T`` runs in ``precision`` (``kernels.small_k_gemm``).
 
     The callable ``source(direction_index, out=None, accumulate=False)`` returns cell-major
     ``[Dsel, R, C, S, G, 4]`` moments ``sum_n Y[d, n] T[:, n]``, written into (or added to) ``out``.
@@ -56,7 +57,8 @@ def scatter_source_function(ctx: SweepContext, T: Tensor):
         if out is None:
             out = torch.empty((Y_sel.shape[0],) + spatial + (G, 4), device=T.device, dtype=T.dtype)
             accumulate = False
-        kernels.small_k_gemm(Y_sel, matrix, out.view(Y_sel.shape[0], -1), accumulate=accumulate)
+        kernels.small_k_gemm(Y_sel, matrix, out.view(Y_sel.shape[0], -1), accumulate=accumulate,
+                             precision=precision)
         return out
 
     source.cell_major = True  # type: ignore[attr-defined]
@@ -76,7 +78,7 @@ def _scalar_norms(*phis: Tensor) -> list:
 def source_iteration(ctx: SweepContext, mu_t_coarse: Tensor, mu_s_l_volume_coarse: Tensor,
                      first_collision_source_function, tolerance: float, max_iterations: int,
                      direction_chunk: Optional[int] = None,
-                     callback: Optional[Callable] = None) -> SourceIterationResult:
+                     callback: Optional[Callable] = None, precision: str = "fp32") -> SourceIterationResult:
     """Collision-order iteration from the first-collision source (reference ``source_iteration.py:138-204``)."""
     if max_iterations < 1:
         raise ValueError("max_iterations must be >= 1")
@@ -86,7 +88,7 @@ def source_iteration(ctx: SweepContext, mu_t_coarse: Tensor, mu_s_l_volume_coars
     source_function = first_collision_source_function
     n = 0
     for n in range(1, max_iterations + 1):
-        phi_n = sweep(ctx, mu_t_coarse, source_function, direction_chunk=direction_chunk)
+        phi_n = sweep(ctx, mu_t_coarse, source_function, direction_chunk=direction_chunk, precision=precision)
         source_function = None
         if phi_total is None:
             phi_total = phi_n.clone()
@@ -103,7 +105,8 @@ def source_iteration(ctx: SweepContext, mu_t_coarse: Tensor, mu_s_l_volume_coars
             break
         if n == max_iterations:
             break
-        source_function = scatter_source_function(ctx, scatter_moments(mu_s_l_volume_coarse, phi_n))
+        source_function = scatter_source_function(ctx, scatter_moments(mu_s_l_volume_coarse, phi_n),
+                                                  precision=precision)
         del phi_n
     return SourceIterationResult(phi_total=phi_total, num_iterations=n, history=history, phi_norms=norms,
                                  converged=converged)

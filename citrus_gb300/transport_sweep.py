@@ -188,7 +188,7 @@ def _fill_source(ctx: SweepContext, source_function, d0: int, d1: int, G: int, o
 
 
 def sweep(ctx: SweepContext, mu_t: Tensor, source_function, direction_chunk: Optional[int] = None,
-          return_psi: bool = False, method: str = "persistent", check: bool = True):
+          return_psi: bool = False, method: str = "persistent", check: bool = True, precision: str = "fp32"):
     """Sweep every direction and group (reference ``transport_sweep.py:457-537``).
 
     Args:
@@ -200,6 +200,7 @@ def sweep(ctx: SweepContext, mu_t: Tensor, source_function, direction_chunk: Opt
         return_psi: also return the angular fluence ``[M, G, 4, R, C, S]`` (tests).
         method: plane driver of ``kernels.sweep_planes``.
         check: read back the barrier words and raise on a timeout (one host synchronization per sweep).
+        precision: arithmetic of the moment accumulation ``Yw^T psi`` (``kernels.small_k_gemm``).
 
     Returns:
         phi ``[G, N_sh, 4, R, C, S]`` (a view of cell-major storage), or (phi, psi).
@@ -229,7 +230,8 @@ def sweep(ctx: SweepContext, mu_t: Tensor, source_function, direction_chunk: Opt
         if sync is not None:
             syncs.append(sync)
         weights = ctx.Y_weighted.index_select(0, index).t().contiguous()  # [N_sh, 8 dc]
-        kernels.small_k_gemm(weights, store.view(8 * chunk, N * Q), moments, accumulate=not first)
+        kernels.small_k_gemm(weights, store.view(8 * chunk, N * Q), moments, accumulate=not first,
+                             precision=precision)
         first = False
         if psi_out is not None:
             psi_out[index] = store.view(8 * chunk, N, Q).permute(0, 2, 1).reshape(8 * chunk, G, 4, N)

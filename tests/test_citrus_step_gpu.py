@@ -20,13 +20,13 @@ STEP_CONFIG = dict(num_groups=3, legendre_order=2, num_polar=4, num_azimuthal=8,
                    source_iteration_tolerance=1e-4, max_source_iterations=40)
 
 
-def _solver(name, device):
+def _solver(name, device, **overrides):
     g = golden("citrus_step_small")
     library, _, _ = _uncollided_setup()
     det = DetectorResponse(g["det_e"], g["det_theta"], g["det_table"])
     geo = ConeGeometry(40.0, 60.0, 12, 16, 1.2, 1.2, use_curved_detector=name == "curved")
-    return g, ScatterSolver(library, SolverConfig(**STEP_CONFIG), geo, detector=det, grid_response=no_grid(),
-                            device=device)
+    return g, ScatterSolver(library, SolverConfig(**dict(STEP_CONFIG, **overrides)), geo, detector=det,
+                            grid_response=no_grid(), device=device)
 
 
 @pytest.mark.parametrize("name", ["flat", "curved"])
@@ -57,3 +57,23 @@ def test_solve_view_matches_reference(cuda_device, name):
                                atol=1e-6)
     assert rel_err(result.scatter_signal, g[f"{name}_solve_scatter"]) < 1e-4
     assert rel_err(result.primary["signal"], g[f"{name}_solve_primary"]) < 2e-6
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_bf16x3_moment_products_keep_the_step_and_spr_within_bounds(cuda_device, name):
+    """The mixed-precision step (tensor-core bfloat16 hi/lo spherical-harmonic products) against the reference's
+    float64 step: collided moments and scatter signal within 2e-4, the scatter-to-primary ratio within 0.5 %."""
+    g, solver = _solver(name, cuda_device, moment_precision="bf16x3")
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device)
+    fields = solver.material_fields(rho, grid)
+    state = CitrusState()
+    for step in (1, 2):
+        scatter, primary, state = citrus_view_step(solver, state, fields, 0.6, primary=True)
+        assert rel_err(state.collided_moments, g[f"{name}_step{step}_collided"]) < 2e-4
+        assert rel_err(scatter, g[f"{name}_step{step}_scatter"]) < 2e-4
+    p = primary.detach().cpu().double().numpy()
+    mask = p > 1e-3 * p.max()
+    spr = scatter.detach().cpu().double().numpy()[mask] / p[mask]
+    spr_ref = g[f"{name}_step2_scatter"][mask] / g[f"{name}_primary"][mask]
+    assert np.abs(spr / spr_ref - 1.0).max() < 5e-3
