@@ -103,12 +103,11 @@ __global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __r
 constexpr int kStreamThreads = 128;
 constexpr int kStreamRows = 128;  // rows of A per block of the column-stationary form
 
-template <int kKP, bool kPair>
+template <int kKP, bool kPair, bool kAccumulate>
 __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* __restrict__ A, int64_t lda,
                                                                   const float* __restrict__ B, int64_t ldb,
                                                                   float* __restrict__ C, int64_t ldc, int M, int K,
-                                                                  int64_t J, int64_t stride_b, int64_t stride_c,
-                                                                  int accumulate) {
+                                                                  int64_t J, int64_t stride_b, int64_t stride_c) {
   extern __shared__ float4 s_a4[];
   float (*As)[kKP] = reinterpret_cast<float (*)[kKP]>(s_a4);  // [kStreamRows + 3][kKP], zero past the tile
   constexpr int kCols = kPair ? 2 : 1;
@@ -159,31 +158,37 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* 
         }
       }
     }
+    float* out = C + (int64_t)(row0 + r0) * ldc + col;
+    if (kAccumulate) {  // the four loads before the first store
+      float2 o[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        o[q] = make_float2(0.f, 0.f);
+        if (r0 + q < rows) {
+          if (kPair) o[q] = *reinterpret_cast<const float2*>(out + (int64_t)q * ldc);
+          else o[q].x = out[(int64_t)q * ldc];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a0[q] += o[q].x;
+        a1[q] += o[q].y;
+      }
+    }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       if (r0 + q >= rows) break;
-      float* out = C + (int64_t)(row0 + r0 + q) * ldc + col;
-      if (kPair) {
-        float2 v = make_float2(a0[q], a1[q]);
-        if (accumulate) {
-          const float2 o = *reinterpret_cast<const float2*>(out);
-          v.x += o.x;
-          v.y += o.y;
-        }
-        *reinterpret_cast<float2*>(out) = v;
-      } else {
-        *out = accumulate ? *out + a0[q] : a0[q];
-      }
+      if (kPair) *reinterpret_cast<float2*>(out + (int64_t)q * ldc) = make_float2(a0[q], a1[q]);
+      else out[(int64_t)q * ldc] = a0[q];
     }
   }
 }
 
-template <int kMP, bool kPair>
+template <int kMP, bool kPair, bool kAccumulate>
 __global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* __restrict__ A, int64_t lda,
                                                                   const float* __restrict__ B, int64_t ldb,
                                                                   float* __restrict__ C, int64_t ldc, int M, int K,
-                                                                  int64_t J, int64_t stride_b, int64_t stride_c,
-                                                                  int accumulate) {
+                                                                  int64_t J, int64_t stride_b, int64_t stride_c) {
   extern __shared__ float4 s_at4[];
   float* At = reinterpret_cast<float*>(s_at4);  // [K][kMP], A transposed, zero rows past M
   constexpr int kCols = kPair ? 2 : 1;
@@ -225,69 +230,80 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* 
       }
     }
   }
+  if (kAccumulate) {  // eight rows' loads before their stores
+#pragma unroll
+    for (int r8 = 0; r8 < kMP; r8 += 8) {
+      float2 o[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        o[q] = make_float2(0.f, 0.f);
+        if (r8 + q < M) {
+          const float* in = C + (int64_t)(r8 + q) * ldc + col;
+          if (kPair) o[q] = *reinterpret_cast<const float2*>(in);
+          else o[q].x = *in;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        c0[r8 + q] += o[q].x;
+        c1[r8 + q] += o[q].y;
+      }
+    }
+  }
 #pragma unroll
   for (int r = 0; r < kMP; ++r) {
     if (r >= M) break;
     float* out = C + (int64_t)r * ldc + col;
-    if (kPair) {
-      float2 v = make_float2(c0[r], c1[r]);
-      if (accumulate) {
-        const float2 o = *reinterpret_cast<const float2*>(out);
-        v.x += o.x;
-        v.y += o.y;
-      }
-      *reinterpret_cast<float2*>(out) = v;
-    } else {
-      *out = accumulate ? *out + c0[r] : c0[r];
-    }
+    if (kPair) *reinterpret_cast<float2*>(out) = make_float2(c0[r], c1[r]);
+    else *out = c0[r];
   }
 }
 
-template <int kKP, bool kPair>
+template <int kKP, bool kPair, bool kAcc>
 int launch_cols(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
-                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t s) {
+                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, cudaStream_t s) {
   const int64_t cols_per_block = (int64_t)kStreamThreads * (kPair ? 2 : 1);
   const size_t smem = (size_t)(kStreamRows + 3) * kKP * sizeof(float);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_cols_kernel<kKP, kPair>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(gemm_cols_kernel<kKP, kPair, kAcc>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
   }
   dim3 grid((unsigned)cdiv(J, cols_per_block), (unsigned)cdiv(M, kStreamRows), (unsigned)batch);
-  gemm_cols_kernel<kKP, kPair><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
-                                                                 stride_c, accumulate);
+  gemm_cols_kernel<kKP, kPair, kAcc><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
+                                                                       stride_c);
   note_launches();
   return launch_status("citrus_small_k_gemm");
 }
 
-template <int kMP, bool kPair>
+template <int kMP, bool kPair, bool kAcc>
 int launch_rows(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
-                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t s) {
+                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, cudaStream_t s) {
   const size_t smem = (size_t)K * kMP * sizeof(float);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_rows_kernel<kMP, kPair>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(gemm_rows_kernel<kMP, kPair, kAcc>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
   }
   const int64_t cols_per_block = (int64_t)kStreamThreads * (kPair ? 2 : 1);
   dim3 grid((unsigned)cdiv(J, cols_per_block), 1, (unsigned)batch);
-  gemm_rows_kernel<kMP, kPair><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
-                                                                  stride_c, accumulate);
+  gemm_rows_kernel<kMP, kPair, kAcc><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
+                                                                       stride_c);
   note_launches();
   return launch_status("citrus_small_k_gemm");
 }
 
-template <bool kPair>
+template <bool kPair, bool kAcc>
 int launch_stream(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
-                  int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, cudaStream_t s) {
-  if (K <= 16) return launch_cols<16, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  if (K <= 32) return launch_cols<32, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  if (K <= 48) return launch_cols<48, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  if (K <= 64) return launch_cols<64, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  if (M <= 16) return launch_rows<16, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  if (M <= 32) return launch_rows<32, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  if (M <= 48) return launch_rows<48, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
-  return launch_rows<64, kPair>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, s);
+                  int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, cudaStream_t s) {
+  if (K <= 16) return launch_cols<16, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (K <= 32) return launch_cols<32, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (K <= 48) return launch_cols<48, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (K <= 64) return launch_cols<64, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (M <= 16) return launch_rows<16, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (M <= 32) return launch_rows<32, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (M <= 48) return launch_rows<48, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  return launch_rows<64, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
 }
 
 template <int R, bool kAligned>
@@ -338,8 +354,11 @@ extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, 
   if (K <= 64 || (M <= 64 && K * 64 * 4 <= 200 * 1024)) {  // the streaming forms
     const bool pair = J % 2 == 0 && ldb % 2 == 0 && ldc % 2 == 0 && stride_b % 2 == 0 && stride_c % 2 == 0 &&
                       ((uintptr_t)B % 8) == 0 && ((uintptr_t)C % 8) == 0;
-    if (pair) return launch_stream<true>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-    return launch_stream<false>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    if (pair && accumulate)
+      return launch_stream<true, true>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s);
+    if (pair) return launch_stream<true, false>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s);
+    if (accumulate) return launch_stream<false, true>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s);
+    return launch_stream<false, false>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s);
   }
   if (8ll * 16 * K * 4 + kChunk * kCols * 4 > 200 * 1024)
     return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: K %lld too large for the shared-memory tile", (long long)K);

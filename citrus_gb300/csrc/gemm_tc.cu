@@ -194,8 +194,10 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (abort_flag) break;
-    // epilogue: row 32 warp + lane, 32 columns per load
-    const int row = warp * 32 + lane;
+    // epilogue, 32 columns at a time: warp w reads accumulator lanes (rows) 32w .. 32w + 31 and turns them through
+    // shared memory (the B region, free once the MMAs completed), so that every store (and load, when accumulating)
+    // of C covers 32 consecutive columns of one row: 128 contiguous bytes
+    float (*stage)[33] = reinterpret_cast<float (*)[33]>(b_hi) + warp * 32;
 #pragma unroll 1
     for (int c0 = 0; c0 < kTcN; c0 += 32) {
       uint32_t r[32];
@@ -209,29 +211,23 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
           : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
-        float* out = Cz + (int64_t)row * ldc + n0 + c0;
-        const int64_t left = J - (n0 + c0);
-        if (left >= 32 && ((uintptr_t)out % 16) == 0) {
 #pragma unroll
-          for (int q = 0; q < 32; q += 4) {
-            float4 v = make_float4(__uint_as_float(r[q]), __uint_as_float(r[q + 1]), __uint_as_float(r[q + 2]),
-                                   __uint_as_float(r[q + 3]));
-            if (accumulate) {
-              const float4 o = reinterpret_cast<const float4*>(out)[q / 4];
-              v.x += o.x;
-              v.y += o.y;
-              v.z += o.z;
-              v.w += o.w;
-            }
-            reinterpret_cast<float4*>(out)[q / 4] = v;
-          }
-        } else {
+      for (int q = 0; q < 32; ++q) stage[lane][q] = __uint_as_float(r[q]);
+      __syncwarp();
+      const int64_t col = n0 + c0 + lane;
+      const int rows = min(32, M - warp * 32);
+      if (col < J && rows > 0) {
+        float* out = Cz + (int64_t)(warp * 32) * ldc + col;
+        float prev[32];
+        if (accumulate) {  // every load issued before the first store
 #pragma unroll
-          for (int q = 0; q < 32; ++q)
-            if (q < left) out[q] = accumulate ? out[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
+          for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? out[(int64_t)rr * ldc] : 0.f;
         }
+#pragma unroll
+        for (int rr = 0; rr < 32; ++rr)
+          if (rr < rows) out[(int64_t)rr * ldc] = accumulate ? prev[rr] + stage[rr][lane] : stage[rr][lane];
       }
+      __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();  // the accumulator and the B tile are free for the next tile
@@ -257,9 +253,10 @@ extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const flo
   CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "citrus_small_k_gemm_bf16x3: leading dimensions too small");
   if (J == 0) return CITRUS_OK;
   const int KS = (int)((K + 15) / 16);
-  // operands, and at least 60 KB so that no more than three CTAs (3 x 128 of the 512 tensor-memory columns) share
-  // an SM: every CTA's allocation then succeeds at once
-  const size_t smem = std::max<size_t>((size_t)KS * (2 * kTcM * 16 * 2 + 2 * kTcN * 16 * 2), 60 * 1024);
+  // A and B operands (the epilogue's staging, 128 x 33 floats, reuses the B region), and at least 50 KB so that no
+  // more than four CTAs (4 x 128 of the 512 tensor-memory columns) share an SM: every allocation succeeds at once
+  const size_t b_bytes = std::max<size_t>((size_t)KS * 2 * kTcN * 16 * 2, (size_t)kTcM * 33 * sizeof(float));
+  const size_t smem = std::max<size_t>((size_t)KS * 2 * kTcM * 16 * 2 + b_bytes, 50 * 1024);
   cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: %s", cudaGetErrorString(e));
   const int64_t tiles_per_batch = cdiv(J, kTcN);
@@ -267,7 +264,7 @@ extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const flo
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gemm_tc_kernel, kTcThreads, smem);
   if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: occupancy query");
-  if (per_sm > 3) per_sm = 3;
+  if (per_sm > 4) per_sm = 4;
   const int64_t grid = std::min<int64_t>(num_tiles, (int64_t)per_sm * num_sms());
   gemm_tc_kernel<<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(A, lda, B, ldb, C, ldc, (int)M, (int)K, J,
                                                                          stride_b, stride_c, accumulate,
