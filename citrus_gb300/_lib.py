@@ -29,6 +29,9 @@ SIGNATURES = {
     "citrus_sweep_persistent_static": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, P],
     "citrus_small_k_gemm": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P],
     "citrus_small_k_gemm_bf16x3": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P, P],
+    "citrus_state_encode": [P, I64, I64, I64, I64, I64, I64, P, P, P],
+    "citrus_state_decode": [P, P, I64, I64, I64, P, I64, I64, I64, I64, P],
+    "citrus_attenuation_to_density": [P, I64, P, P, P, I64, I64, P, P],
     "citrus_scattering_moments": [P, P, P] + [I64] * 14 + [P],
     "citrus_line_integrals": [P, I64, P, P, P, P, I64, P, P],
     "citrus_trace_from_source": [P, I64, P, P, P, P, P, P, P, P, I64, P, P],

@@ -15,7 +15,9 @@ import numpy as np
 import torch
 from torch import Tensor
 
+from .scatter_image import primary_from_path_lengths, primary_path_lengths
 from .scatter_solver import MaterialFields, ScatterSolver
+from .uncollided import present_materials
 
 
 @dataclass
@@ -141,3 +143,32 @@ def citrus_step(solver: ScatterSolver, state: CitrusState, rho, grid, angle: flo
                 fields: Optional[MaterialFields] = None) -> tuple:
     """One CITRUS scatter step of one view from the densities (reference ``citrus.py:285-317``)."""
     return citrus_view_step(solver, state, _fields(solver, rho, grid, fields), angle)
+
+
+def primary_signals(solver: ScatterSolver, fields: MaterialFields, angles, out: Optional[Tensor] = None,
+                    quantity: str = "signal") -> Tensor:
+    """Primary signal (or planar fluence summed over the groups) of every view, ``[V, Rd, Cd]`` (reference
+    ``citrus.py:369-458``).
+
+    The reference projects the material maps with the reconstruction's MBIRTORCH projector, which is not part of this
+    package; here the path lengths are the Siddon line integrals from the focal spot to the pixel centres through the
+    fine-grid density maps (``GB300Projectors.primary_project``), one launch per view over the materials present, and
+    ``primary_from_path_lengths`` turns them into the primary of each view, as the reference does.
+    """
+    if quantity not in ("signal", "planar_fluence"):
+        raise ValueError(f"quantity must be 'signal' or 'planar_fluence', got {quantity!r}")
+    angle_array = np.asarray(angles, dtype=np.float64).reshape(-1)
+    Rd, Cd = solver.geometry.image_shape
+    if out is None:
+        out = torch.empty((angle_array.size, Rd, Cd), device=solver.device, dtype=torch.float32)
+    elif tuple(out.shape) != (angle_array.size, Rd, Cd):
+        raise ValueError(f"out must be [{angle_array.size}, {Rd}, {Cd}], got {tuple(out.shape)}")
+    rho = fields.rho_fine
+    present = present_materials(rho)                                   # once for all views
+    traced = (rho if present is None else rho[list(present)]).contiguous()
+    for v, angle in enumerate(angle_array):
+        path = primary_path_lengths(solver.projectors, traced, fields.grid_fine, solver.geometry, float(angle))
+        image = primary_from_path_lengths(solver.library, path, present, solver.geometry, float(angle), solver.source,
+                                          solver.detector, solver.grid_response)
+        out[v] = image["signal"] if quantity == "signal" else image["planar_fluence"].sum(0)
+    return out

@@ -236,6 +236,20 @@ class ScatterSolver:
                               mu_t_volume(self.transport_library, rho_c), transfer_moments_volume(
                                   self.transport_library, rho_c), None if traced is None else tuple(traced))
 
+    def material_fields_from_attenuation(self, X: Tensor, grid_fine: Grid, density_model) -> MaterialFields:
+        """The fields of the densities ``density_model(X)``, one material map at a time (reference ``:692-743``).
+
+        Every material map is resampled onto the transport and quadrature grids as it is made; the maps of the
+        materials present are kept as the fine densities (the primary traces them). Equals :meth:`material_fields`
+        of the stacked maps.
+        """
+        if tuple(X.shape) != tuple(grid_fine.shape):
+            raise ValueError(f"X shape {tuple(X.shape)} != grid shape {grid_fine.shape}")
+        X = X.to(device=self.device, dtype=torch.float32).contiguous()
+        M = self.library.num_materials
+        maps = [density_model.material(X, m) for m in range(M)]
+        return self.material_fields(torch.stack(maps), grid_fine)
+
     def uncollided_fluence(self, fields: MaterialFields, angle: float) -> Tensor:
         """[G, Rq, Cq, Sq] uncollided fluence at the quadrature points (reference ``:745-772``)."""
         trace = self.config.uncollided_trace_grid

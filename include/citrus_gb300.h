@@ -276,6 +276,29 @@ int citrus_weighted_direction_sum(const float* image, int64_t num_directions, in
 int citrus_sum_directions(const float* image, int64_t num_directions, int64_t pixels, int64_t stride_k,
                           float* accumulator, int32_t accumulate, void* stream);
 
+/* ------------------------------------------------------------------------------------------------------------------
+ * Per-view accumulator storage: the linear-discontinuous cell mean in scaled float16 (citrus/citrus.py:620-720,
+ * StateStore.put / get).
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* data [groups, moments, cells] float16 = mean / scale and scale [groups, moments] = max |mean| / 2^14 (1 where the
+ * maximum is 0), from the cell-mean component of an accumulator at g s_g + n s_n + cell s_x. */
+int citrus_state_encode(const float* accumulator, int64_t groups, int64_t moments, int64_t cells, int64_t s_g,
+                        int64_t s_n, int64_t s_x, uint16_t* data, float* scale, void* stream);
+
+/* The accumulator back, element (g, n, k, cell) at g o_g + n o_n + k o_k + cell o_x: k = 0 the decoded cell mean,
+ * k = 1..3 (the slopes) zero. */
+int citrus_state_decode(const uint16_t* data, const float* scale, int64_t groups, int64_t moments, int64_t cells,
+                        float* accumulator, int64_t o_g, int64_t o_n, int64_t o_k, int64_t o_x, void* stream);
+
+/* ------------------------------------------------------------------------------------------------------------------
+ * Density model of the CITRUS loop (citrus/utilities.py:710-799, attenuation_to_density).
+ * out [V] = density of the material in bracketing slot `slot` of X [V] (1/cm): mu, mass, nominal [M] float32 are the
+ * nominal attenuations, mass attenuations and nominal densities of the materials sorted by nominal attenuation.
+ * ------------------------------------------------------------------------------------------------------------------ */
+int citrus_attenuation_to_density(const float* X, int64_t num_voxels, const float* mu, const float* mass,
+                                  const float* nominal, int64_t num_materials, int64_t slot, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -287,6 +287,34 @@ def citrus_step_small():
     save("citrus_step_small", **arrays)
 
 
+
+
+@case
+def density_model():
+    """The reference's interpolating density model (float32 maps of a seeded attenuation volume from below 0 to above
+    the densest material) for a three-material library, with its effective energy, mass attenuations and order."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from citrus_gb300.cross_sections import AVOGADRO, BONE, WATER, MaterialModel, spectral_library
+    from citrus_gb300.workloads import bremsstrahlung_spectrum
+    from citrus.utilities import (attenuation_to_densities, attenuation_to_density, effective_energy,
+                                  mass_attenuation_at, material_order)
+    soft = MaterialModel("soft_tissue", AVOGADRO * 0.549, 0.0185, 0.0115, 1.04)
+    lib = spectral_library(np.linspace(120.0, 40.0, 4), bremsstrahlung_spectrum(seed=3), [WATER, BONE, soft], 1,
+                           num_eta=21, fine_per_group=4)
+    ref = reference_library(lib)
+    g = torch.Generator().manual_seed(11)
+    X = (torch.rand(6, 7, 5, generator=g) * 1.4 - 0.2).to(torch.float32)
+    e = effective_energy(ref)
+    rho = attenuation_to_densities(ref, X)
+    single = torch.stack([attenuation_to_density(ref, X, m) for m in range(3)])
+    X50 = X * 0.7
+    rho50 = attenuation_to_densities(ref, X50, 50.0)
+    save("density_model", X=X, rho=rho, single=single, X50=X50, rho50=rho50, energy=np.array(e),
+         mass=mass_attenuation_at(ref, e), order=np.array(material_order(ref)),
+         lib_fine_energy=lib.fine_energy, lib_fine_mu_t=lib.fine_mu_t, lib_fine_weight=lib.fine_weight,
+         lib_nominal=lib.nominal_density)
+
+
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)
     for n in names:

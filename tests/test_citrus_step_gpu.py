@@ -77,3 +77,21 @@ def test_bf16x3_moment_products_keep_the_step_and_spr_within_bounds(cuda_device,
     spr = scatter.detach().cpu().double().numpy()[mask] / p[mask]
     spr_ref = g[f"{name}_step2_scatter"][mask] / g[f"{name}_primary"][mask]
     assert np.abs(spr / spr_ref - 1.0).max() < 5e-3
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_primary_signals_of_all_views(cuda_device, name):
+    from citrus_gb300.citrus_step import primary_signals
+    g, solver = _solver(name, cuda_device)
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device)
+    fields = solver.material_fields(rho, grid)
+    angles = [0.6, 1.3, 2.9]
+    signals = primary_signals(solver, fields, angles)
+    assert rel_err(signals[0], g[f"{name}_primary"]) < 2e-6
+    for v, a in enumerate(angles):
+        assert torch.equal(signals[v], solver.primary(fields, a)["signal"])
+    planar = primary_signals(solver, fields, angles, quantity="planar_fluence")
+    assert torch.allclose(planar[1], solver.primary(fields, 1.3)["planar_fluence"].sum(0))
+    with pytest.raises(ValueError):
+        primary_signals(solver, fields, angles, quantity="counts")
