@@ -421,13 +421,15 @@ def _dims(address) -> tuple:
 
 def emission_bytes(args) -> int:
     """Algorithmic bytes of one citrus_attenuated_emission_moments call: every input read once (the densities and
-    fluence of the points, the cells' attenuation, optical depths and scattering-source moments, the harmonics), the
-    emission written once."""
-    M, G, dims, f, k, NS = int(args[1]), int(args[3]), _dims(args[5]), int(args[6]), int(args[14]), int(args[19])
+    fluence of the points, the cells' attenuation, optical depths or material path lengths and scattering-source
+    moments, the harmonics), the emission written once."""
+    M, G, dims, f, k = int(args[1]), int(args[3]), _dims(args[5]), int(args[6]), int(args[14])
+    TM, NS = int(args[17]), int(args[21])
     V = dims[0] * dims[1] * dims[2]
     NC = V // (f ** 3)
-    C = 1 if args[21] is not None else G
-    floats = (M + G + 1) * V + G * NC + k * G * NC + NS * G * NC + k * NS + k * G + k * V * C + 2 * k * (-(-V // 32))
+    C = 1 if args[23] is not None else G
+    tau = k * NC * (TM if args[16] is not None else G)
+    floats = (M + G + 1) * V + G * NC + tau + NS * G * NC + k * NS + k * G + k * V * C + 2 * k * (-(-V // 32))
     return 4 * floats
 
 
@@ -435,10 +437,12 @@ def product_emission_bytes(args) -> int:
     """Algorithmic bytes of one citrus_attenuated_emission call: as the fused form, with the multiple-collision
     source [K, NC, G] read in place of the moments and harmonics."""
     M, G, dims, f, k = int(args[1]), int(args[3]), _dims(args[5]), int(args[6]), int(args[14])
+    TM = int(args[17])
     V = dims[0] * dims[1] * dims[2]
     NC = V // (f ** 3)
-    C = 1 if args[19] is not None else G
-    floats = (M + G + 1) * V + G * NC + 2 * k * G * NC + k * G + k * V * C + 2 * k * (-(-V // 32))
+    C = 1 if args[21] is not None else G
+    tau = k * NC * (TM if args[16] is not None else G)
+    floats = (M + G + 1) * V + G * NC + tau + k * G * NC + k * G + k * V * C + 2 * k * (-(-V // 32))
     return 4 * floats
 
 

@@ -104,6 +104,51 @@ __device__ __forceinline__ Setup<T> ray_setup(const Box& b, const T p0[3], const
   return s;
 }
 
+// The same set-up with float64 only where it decides which voxels the line touches: the clipping parameters (the
+// reference's float64 slab test) and the entry and exit points relative to the box corner; the direction in voxel
+// units, the length and the fractional positions are float32 (their relative errors are those of the float32 walk).
+// FP64 is a small fraction of the float32 rate on this GPU, and the dense image rays need this set-up once per ray.
+__device__ __forceinline__ Setup<float> ray_setup_mixed(const Box& b, const double p0[3], const double p1[3]) {
+  Setup<float> s;
+  double d[3];
+  double a_lo = 0, a_hi = 1;
+  for (int a = 0; a < 3; ++a) {
+    d[a] = p1[a] - p0[a];
+    const double lo = b.lo[a], hi = add_rn(lo, mul_rn(b.delta[a], (double)b.n[a]));
+    if (d[a] != 0) {
+      const double inv = 1.0 / d[a];
+      const double t1 = (lo - p0[a]) * inv, t2 = (hi - p0[a]) * inv;
+      a_lo = fmax(a_lo, fmin(t1, t2));
+      a_hi = fmin(a_hi, fmax(t1, t2));
+    } else if (!(p0[a] >= lo && p0[a] <= hi)) {
+      a_hi = -1;  // parallel to this slab and outside it
+    }
+  }
+  const float df[3] = {(float)d[0], (float)d[1], (float)d[2]};
+  const float len = sqrtf(df[0] * df[0] + df[1] * df[1] + df[2] * df[2]);
+  s.hit = a_hi > a_lo && len > 0.f;
+  if (!s.hit) {
+    s.total = 0.f;
+    return s;
+  }
+  s.total = (float)(a_hi - a_lo) * len;
+  for (int a = 0; a < 3; ++a) {
+    const float delta = (float)b.delta[a];
+    s.v[a] = df[a] / len / delta;
+    const float q = (float)(p0[a] + a_lo * d[a] - b.lo[a]) / delta;   // entry, in voxels from the corner
+    int i = (int)floorf(q);
+    if (i < 0) i = 0;
+    if (i > b.n[a] - 1) i = b.n[a] - 1;
+    s.idx[a] = i;
+    s.f[a] = fminf(fmaxf(q - (float)i, 0.f), 1.f);
+    int ie = (int)floorf((float)(p0[a] + a_hi * d[a] - b.lo[a]) / delta);   // exit voxel, clamped alike
+    if (ie < 0) ie = 0;
+    if (ie > b.n[a] - 1) ie = b.n[a] - 1;
+    s.cross[a] = ie > i ? ie - i : i - ie;
+  }
+  return s;
+}
+
 // Walk one clipped ray and add the integral of the C channels to acc (in cm times the field unit).
 template <int kC, bool kCompensated>
 __device__ __forceinline__ void ray_walk(const Box& b, const Setup<float>& s, const float* __restrict__ vol, int C,
@@ -463,21 +508,31 @@ __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* _
                                                            int64_t os_r, int64_t os_col, int64_t cols) {
   const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int k = blockIdx.y;
+  // the direction's |omega|^2 and half-length, once per block (the block shares the direction)
+  __shared__ double s_dir[2];
+  if (threadIdx.x == 0) {
+    const double w0 = omegas[3 * k], w1 = omegas[3 * k + 1], w2z = omegas[3 * k + 2];
+    const double sq = add_rn(add_rn(mul_rn(w0, w0), mul_rn(w1, w1)), mul_rn(w2z, w2z));
+    s_dir[0] = sq;
+    s_dir[1] = half / sqrt(sq);
+  }
+  __syncthreads();
   if (p >= P) return;
   const double w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
   const double px = pixels[3 * p], py = pixels[3 * p + 1], pz = pixels[3 * p + 2];
   // the endpoints of ray_tracing.py:588-595, operation by operation
-  const double w2 = add_rn(add_rn(mul_rn(w[0], w[0]), mul_rn(w[1], w[1])), mul_rn(w[2], w[2]));
+  const double w2 = s_dir[0];
   const double dot = add_rn(add_rn(mul_rn(cx - px, w[0]), mul_rn(cy - py, w[1])), mul_rn(cz - pz, w[2]));
   const double cp = dot / w2;
-  const double h = half / sqrt(w2);
+  const double h = s_dir[1];
   const double tm = cp - h, tp = cp + h;
   const double a[3] = {add_rn(px, mul_rn(tm, w[0])), add_rn(py, mul_rn(tm, w[1])), add_rn(pz, mul_rn(tm, w[2]))};
   const double e[3] = {add_rn(px, mul_rn(tp, w[0])), add_rn(py, mul_rn(tp, w[1])), add_rn(pz, mul_rn(tp, w[2]))};
   const int nC = kC > 0 ? kC : C;
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
-  integrate<kC, false, double>(b, a, e, vol + (int64_t)k * field_stride, C, acc);
+  const Setup<float> st = ray_setup_mixed(b, a, e);
+  if (st.hit) ray_walk<kC, false>(b, st, vol + (int64_t)k * field_stride, C, acc);
   const int64_t row = p / cols;
   float* o = out + (int64_t)k * os_k + row * os_r + (p - row * cols) * os_col;
   for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = acc[c];
