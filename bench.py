@@ -5,8 +5,10 @@
 Prints one JSON line. The default workload is the batched circular cone-beam scatter step: 64^3 cells of 0.4 cm,
 8 groups (30-120 keV), P5, 120 sweep directions, a 256 x 192 curved panel, 60 views per outer iteration; one step
 is the full scatter step of every view (uncollided fluence, one accumulator sweep, the signal-only collapsed-cone
-image). ``--workload sweep`` times the accumulator sweep alone (scattering moments, source expansion, wavefront
-sweep, moment accumulation) of one view.
+image), with the accumulator sweeps of 4 views in one persistent launch (``--batch``) and float32 spherical-harmonic
+products (``--precision bf16x3`` runs them on the tcgen05 tensor cores with a bfloat16 hi/lo split and reports the
+scatter-to-primary error against float32). ``--workload sweep`` times the accumulator sweep alone (scattering
+moments, source expansion, wavefront sweep, moment accumulation) of one view.
 
 The reference arm (``--impl reference``) times the float64 CPU restatement of the same path on the host cores, on a
 bounded sample of the same workload, and reports the same metric.
@@ -42,7 +44,8 @@ def _parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3"],
                    help="arithmetic of the spherical-harmonic products (bf16x3: tcgen05 tensor cores, hi/lo split)")
-    p.add_argument("--batch", type=int, default=1, help="views per persistent sweep launch (1: citrus_view_step)")
+    p.add_argument("--batch", type=int, default=4,
+                   help="views per persistent sweep launch (1: citrus_view_step per view)")
     p.add_argument("--cells", type=int, default=64, help="cells per axis of the step workload (64; smaller for "
                                                          "profiling captures)")
     return p.parse_args()
@@ -270,7 +273,7 @@ def run_reference(args):
         line = {"metric": STEP_METRIC, "value": value, "unit": "ms/view", "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
                 "dtype": "f64", "data": "synthetic (seeded phantom and library)",
-                "config": {"workload": step_workload_name(args.cells, 60)}, "cpu_baseline": base,
+                "config": {"workload": step_workload_name(args.cells, 60, args.batch)}, "cpu_baseline": base,
                 "e2e": {"value": value, "unit": "ms/view", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -406,10 +409,12 @@ def make_step_solver(device, views: int = 0, cells: int = 64, precision: str = "
 STEP_METRIC = "scatter-step ms/view (all views of one outer iteration; cell*dir*group updates/s alongside)"
 
 
-def step_workload_name(cells: int, views: int) -> str:
+def step_workload_name(cells: int, views: int, batch: int = 1) -> str:
+    how = ("citrus_view_step per view" if batch <= 1 else
+           f"batched_view_steps, the accumulator sweeps of {batch} views per persistent launch")
     return (f"batched_views: {cells}^3 cells x {25.6 / cells:g} cm, G=8 (30-120 keV), P5, 120 sweep directions, cone "
-            f"16x32, curved 256x192 panel, {views} views per rank per step, one accumulator sweep per view "
-            f"(citrus_view_step, signal only)")
+            f"16x32, curved 256x192 panel, {views} views per rank per step, one accumulator sweep per view ({how}, "
+            f"signal only)")
 
 
 def _dims(address) -> tuple:
@@ -462,7 +467,7 @@ def sweep_bytes(args) -> int:
 STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_attenuated_emission": product_emission_bytes,
               "citrus_downstream_cumulative": downstream_bytes,
               "citrus_sweep_persistent": sweep_bytes, "citrus_oblique_project": None, "citrus_box_blur": None,
-              "citrus_small_k_gemm": None, "citrus_first_collision_moments": None,
+              "citrus_small_k_gemm": None, "citrus_small_k_gemm_bf16x3": None, "citrus_first_collision_moments": None,
               "citrus_first_collision_correction": None, "citrus_scattering_moments": None}
 
 
@@ -600,7 +605,7 @@ def run_step(args):
         "value": ms_per_view / max(1, world), "unit": "ms/view", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom and library)",
-        "config": {"workload": step_workload_name(args.cells, V),
+        "config": {"workload": step_workload_name(args.cells, V, args.batch),
                    "l2": "inputs larger than L2 (4 GB sweep store per view)",
                    "moment_precision": args.precision, "views_per_sweep_launch": args.batch},
         "updates_per_s": updates * V * args.steps * world / elapsed,

@@ -501,6 +501,7 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
   extern __shared__ float4 s_dyn4[];
   float* s_tab = reinterpret_cast<float*>(s_dyn4);  // the table window (dynamic, kWindowBytes)
   __shared__ float s_om[kEmitDirs][3];
+  __shared__ float s_sw[kEmitDirs][kGP];          // signal weights of the block's directions
   __shared__ __align__(16) float s_y[kFused ? kEmitDirs : 1][kFused ? kMaxMoments : 4];
   __shared__ float s_sum[kEmitDirs][kWarps][2];   // per-direction, per-warp sums of e and e h
   __shared__ int s_range[2][32];
@@ -513,6 +514,11 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
   const int nd = min(kEmitDirs, K - d0);
   constexpr int nthreads = kEmitPoints * kGP;
   for (int i = tid; i < kEmitDirs * 3; i += nthreads) s_om[i / 3][i % 3] = i < nd * 3 ? omegas[3 * d0 + i] : 0.f;
+  if (signal_weight != nullptr)
+    for (int i = tid; i < kEmitDirs * kGP; i += nthreads) {
+      const int dd = i / kGP, q = i % kGP;
+      s_sw[dd][q] = (dd < nd && q < G) ? signal_weight[(int64_t)(d0 + dd) * G + q] : 0.f;
+    }
   if (kFused)
     for (int i = tid; i < kEmitDirs * NS; i += nthreads)
       s_y[i / NS][i % NS] = i < nd * NS ? harmonics[(int64_t)d0 * NS + i] : 0.f;
@@ -568,7 +574,7 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
       int i0;
       float w;
       table_position(tb, cosine, i0, w);
-      const float offset = oy * offy + ox * offx + oz * offz;
+      const float offset = pg.f > 1 ? oy * offy + ox * offx + oz * offz : 0.f;  // one point per cell: its centre
       const float src = fc_group<kGP, kMM>(tb, s_tab, win_lo, i0, w, g, rho, phi);
       const int64_t kc = ((int64_t)d * NC + cell) * G + g;
       float smc = 0.f;
@@ -596,11 +602,11 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
       } else {
         t = __ldg(tau + kc);
       }
-      const float depth = fmaxf(t - muc * offset, 0.f);
+      const float depth = pg.f > 1 ? fmaxf(t - muc * offset, 0.f) : fmaxf(t, 0.f);
       e = (src + smc) * expf(-depth);
     }
     // group sums over the kGP lanes of the point (in group order), then the warp's points
-    float tot = e, sgl = signal_weight != nullptr && valid && gvalid ? __ldg(signal_weight + (int64_t)d * G + g) * e : 0.f;
+    float tot = e, sgl = signal_weight != nullptr ? s_sw[dd][g] * e : 0.f;
 #pragma unroll
     for (int off = 1; off < kGP; off <<= 1) {
       tot += __shfl_xor_sync(0xffffffffu, tot, off);
@@ -795,9 +801,24 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
   }
   const float inv = 1.f / (float)(F * F * F);
   const int dlast = min(K, (int)(blockIdx.y + 1) * kFcBatch);
+  // one point per cell (the common case): its primary direction and correction factors once for all directions
+  float u1x = 0.f, u1y = 0.f, u1z = 0.f, sc1 = 0.f, be1 = 0.f;
+  int64_t v1 = 0;
+  if (F == 1 && valid) {
+    v1 = ((int64_t)ic * pg.C + jc) * pg.S + kc;
+    primary_direction(__ldg(in.ax_x + jc), __ldg(in.ax_y + ic), __ldg(in.ax_z + kc), in.r0x, in.r0y, in.r0z, u1x,
+                      u1y, u1z);
+    sc1 = __ldg(scale + (int64_t)g * in.V + v1);
+    be1 = __ldg(beta + (int64_t)g * in.V + v1);
+  }
   for (int d = blockIdx.y * kFcBatch; d < dlast; ++d) {
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (valid) {
+    if (valid && F == 1) {
+      const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+      const float cosine = u1x * ox + u1y * oy + u1z * oz;
+      const float* src = cache + (int64_t)__ldg(cache_index + d) * G * in.V + (int64_t)g * in.V;
+      r.x = __ldg(src + v1) * sc1 * (1.f + be1 * cosine) * inv;
+    } else if (valid) {
       const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
       const float* src = cache + (int64_t)__ldg(cache_index + d) * G * in.V + (int64_t)g * in.V;
       float m0 = 0.f, mx = 0.f, my = 0.f, mz = 0.f;

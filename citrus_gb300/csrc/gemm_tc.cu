@@ -258,14 +258,16 @@ extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const flo
   const size_t b_bytes = std::max<size_t>((size_t)KS * 2 * kTcN * 16 * 2, (size_t)kTcM * 33 * sizeof(float));
   const size_t smem = std::max<size_t>((size_t)KS * 2 * kTcM * 16 * 2 + b_bytes, 50 * 1024);
   cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // all of the unified L1 / shared-memory capacity as shared memory, so that four CTAs fit an SM
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: %s", cudaGetErrorString(e));
   const int64_t tiles_per_batch = cdiv(J, kTcN);
   const int64_t num_tiles = tiles_per_batch * batch;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gemm_tc_kernel, kTcThreads, smem);
-  if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: occupancy query");
-  if (per_sm > 4) per_sm = 4;
-  const int64_t grid = std::min<int64_t>(num_tiles, (int64_t)per_sm * num_sms());
+  // four CTAs per SM: the shared-memory floor keeps a fifth from becoming resident (tensor memory holds four
+  // 128-column accumulators), and CTAs beyond what fits simply wait for a free slot
+  const int64_t grid = std::min<int64_t>(num_tiles, 4 * (int64_t)num_sms());
   gemm_tc_kernel<<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(A, lda, B, ldb, C, ldc, (int)M, (int)K, J,
                                                                          stride_b, stride_c, accumulate,
                                                                          tiles_per_batch, num_tiles, error_word);

@@ -164,12 +164,14 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, prec
         _lib.call("citrus_small_k_gemm", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
                   C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), stream)
         return C
-    # the tensor-core product takes at most 128 rows and 128 inner terms per call: tiles of A, partial sums added
+    # the tensor-core product takes at most 128 rows and 128 inner terms per call; inner dimensions above 64 go in
+    # steps of 64 (partial sums added), which keeps the split operands of a CTA small enough for three per SM
     err = None if error_word is None else error_word.data_ptr()
+    step = K if K <= 64 else 64
     for r0 in range(0, M, 128):
         rows = min(128, M - r0)
-        for k0 in range(0, K, 128):
-            inner = min(128, K - k0)
+        for k0 in range(0, K, step):
+            inner = min(step, K - k0)
             _lib.call("citrus_small_k_gemm_bf16x3", A[r0:, k0:].data_ptr(), A.stride(0),
                       B[:, k0:].data_ptr(), B.stride(1), C[:, r0:].data_ptr(), C.stride(1), rows, inner, J, batch,
                       sb, sc, int(bool(accumulate) or k0 > 0), err, stream)
