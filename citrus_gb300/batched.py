@@ -41,6 +41,7 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
     Y = ctx.Y.index_select(0, index).contiguous()                  # [8 D8, N_sh]
     Yw_t = ctx.Y_weighted.index_select(0, index).t().contiguous()  # [N_sh, 8 D8]
     mu_cells = fields.mu_t_coarse.reshape(G, N).t().contiguous()
+    syncs = []
     for b0 in range(0, V, batch):
         views = list(range(b0, min(V, b0 + batch)))
         B = len(views)
@@ -62,7 +63,7 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
                                                out=T_all[j].view((N_sh,) + shape + (G, 4)))
             kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
             del T_all
-        kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c, method="persistent")
+        syncs.append(kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c, method="persistent"))
         moments = torch.empty(B, N_sh, J, device=device)
         kernels.small_k_gemm(Yw_t, store.view(B, 8 * D8, J), moments, precision=precision)
         del store
@@ -83,4 +84,6 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
                 change = diff / norm if norm > 0 else 0.0
             new_states[v] = CitrusState(angle=float(angles[v]), collided_moments=new, cone_quadrature=cone,
                                         num_steps=states[v].num_steps + 1, history=states[v].history + [change])
+    if syncs and bool(torch.stack([w[2] for w in syncs]).ne(0).any()):
+        raise kernels._lib.CitrusKernelError("batched sweep: a grid-barrier wait of the persistent sweep ran out")
     return signals, primaries, new_states

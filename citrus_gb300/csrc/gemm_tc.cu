@@ -57,15 +57,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;  // base offset 0, swizzle none
 }
 
-// Instruction descriptor of kind::f16: bf16 A and B, float32 accumulator, both K-major, N = 128, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
-                            ((uint32_t)(kTcM >> 4) << 24);
+// Instruction descriptor of kind::f16: bf16 A and B, float32 accumulator, both K-major, M = 128 and N columns.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+}
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
@@ -87,6 +89,10 @@ __device__ __forceinline__ uint32_t core_offset(int r, int k) {
   return (uint32_t)((((r >> 3) * 2 + (k >> 3)) * 128) + (r & 7) * 16 + (k & 7) * 2);
 }
 
+// kT = false: the MMA's A is the small matrix (rows of C), its B the 128-column tile, D = C[:, tile] in 128 x 128
+// accumulator columns. kT = true (M <= 64): the roles swap, D = C[:, tile]^T with the tile's 128 columns as the MMA
+// rows and the (M rounded up to 16) rows of C as its N: each accumulator lane is one column of C, stored directly.
+template <bool kT>
 __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __restrict__ A, int64_t lda,
                                                              const float* __restrict__ B, int64_t ldb,
                                                              float* __restrict__ C, int64_t ldc, int M, int K,
@@ -130,9 +136,12 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {  // the accumulator: 128 lanes x 128 float32 columns
+  constexpr uint32_t kCols = kT ? 64u : (uint32_t)kTcN;  // accumulator columns (a power of two >= 32)
+  const int n_t = ((M + 15) / 16) * 16;                   // MMA N of the swapped form
+  const uint32_t idesc = kT ? idesc_bf16(n_t) : idesc_bf16(kTcN);
+  if (warp == 0) {  // the accumulator: 128 lanes x kCols float32 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"((uint32_t)kTcN)
+                 "r"(kCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -178,9 +187,15 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
         const uint64_t al = smem_desc(smem_u32(a_lo + s * a_step), 128, 256);
         const uint64_t bh = smem_desc(smem_u32(b_hi + s * b_step), 128, 256);
         const uint64_t bl = smem_desc(smem_u32(b_lo + s * b_step), 128, 256);
-        mma_bf16(tmem, ah, bh, s > 0 ? 1u : 0u);
-        mma_bf16(tmem, ah, bl, 1u);
-        mma_bf16(tmem, al, bh, 1u);
+        if (kT) {
+          mma_bf16(tmem, bh, ah, idesc, s > 0 ? 1u : 0u);
+          mma_bf16(tmem, bh, al, idesc, 1u);
+          mma_bf16(tmem, bl, ah, idesc, 1u);
+        } else {
+          mma_bf16(tmem, ah, bh, idesc, s > 0 ? 1u : 0u);
+          mma_bf16(tmem, ah, bl, idesc, 1u);
+          mma_bf16(tmem, al, bh, idesc, 1u);
+        }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
                    : "memory");
@@ -194,6 +209,38 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (abort_flag) break;
+    if (kT) {
+      // epilogue of the swapped form: lane 32 warp + lane is column n0 + 32 warp + lane of C, its accumulator
+      // columns the rows of C; every store covers 32 consecutive columns of one row
+      const int64_t col = n0 + warp * 32 + lane;
+#pragma unroll 1
+      for (int m0 = 0; m0 < n_t; m0 += 16) {
+        uint32_t r[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)m0)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (col < J) {
+          const int rows = min(16, M - m0);
+          float* out = Cz + (int64_t)m0 * ldc + col;
+          float prev[16];
+          if (accumulate) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) prev[q] = q < rows ? out[(int64_t)q * ldc] : 0.f;
+          }
+#pragma unroll
+          for (int q = 0; q < 16; ++q)
+            if (q < rows) out[(int64_t)q * ldc] = accumulate ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      continue;
+    }
     // epilogue, 32 columns at a time: warp w reads accumulator lanes (rows) 32w .. 32w + 31 and turns them through
     // shared memory (the B region, free once the MMAs completed), so that every store (and load, when accumulating)
     // of C covers 32 consecutive columns of one row: 128 contiguous bytes
@@ -234,7 +281,7 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
   }
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kTcN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
 }
 
 }  // namespace
@@ -257,20 +304,26 @@ extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const flo
   // more than four CTAs (4 x 128 of the 512 tensor-memory columns) share an SM: every allocation succeeds at once
   const size_t b_bytes = std::max<size_t>((size_t)KS * 2 * kTcN * 16 * 2, (size_t)kTcM * 33 * sizeof(float));
   const size_t smem = std::max<size_t>((size_t)KS * 2 * kTcM * 16 * 2 + b_bytes, 50 * 1024);
-  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const bool swapped = M <= 64;
+  const void* fn = swapped ? (const void*)gemm_tc_kernel<true> : (const void*)gemm_tc_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   // all of the unified L1 / shared-memory capacity as shared memory, so that four CTAs fit an SM
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: %s", cudaGetErrorString(e));
   const int64_t tiles_per_batch = cdiv(J, kTcN);
   const int64_t num_tiles = tiles_per_batch * batch;
   // four CTAs per SM: the shared-memory floor keeps a fifth from becoming resident (tensor memory holds four
   // 128-column accumulators), and CTAs beyond what fits simply wait for a free slot
   const int64_t grid = std::min<int64_t>(num_tiles, 4 * (int64_t)num_sms());
-  gemm_tc_kernel<<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(A, lda, B, ldb, C, ldc, (int)M, (int)K, J,
-                                                                         stride_b, stride_c, accumulate,
-                                                                         tiles_per_batch, num_tiles, error_word);
+  if (swapped)
+    gemm_tc_kernel<true><<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
+        A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
+        error_word);
+  else
+    gemm_tc_kernel<false><<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
+        A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
+        error_word);
   note_launches();
   return launch_status("citrus_small_k_gemm_bf16x3");
 }

@@ -54,6 +54,66 @@ __global__ void box_blur_kernel(const float* __restrict__ in, float* __restrict_
   out[k * os_k + line * os_l + (int64_t)c * os_p] = acc / (hi - lo);
 }
 
+// The same filter with O(1) work per output pixel: a block owns one line, stages its N pixels in shared memory with
+// their float64 prefix sums (a block scan), and each output pixel is its partial first pixel, the prefix-sum
+// difference over the fully covered pixels and its partial last pixel, divided by the window length.
+constexpr int kScanThreads = 256;
+constexpr int kScanMaxN = 1024;
+
+__global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float* __restrict__ in,
+                                                                     float* __restrict__ out, int64_t lines, int N,
+                                                                     int64_t is_k, int64_t is_l, int64_t is_p,
+                                                                     int64_t os_k, int64_t os_l, int64_t os_p,
+                                                                     WidthArgs wa) {
+  __shared__ float x[kScanMaxN];
+  __shared__ double P[kScanMaxN + 1];   // P[j] = sum of x[0 .. j - 1]
+  __shared__ double warp_tot[kScanThreads / 32];
+  const int k = blockIdx.y;
+  const int64_t line = blockIdx.x;
+  const float* src = in + k * is_k + line * is_l;
+  for (int j = threadIdx.x; j < N; j += kScanThreads) x[j] = src[j * is_p];
+  __syncthreads();
+  // each thread sums a contiguous run of per = ceil(N / 256) pixels; a block-wide exclusive scan of the run sums
+  const int per = (N + kScanThreads - 1) / kScanThreads;
+  const int j0 = threadIdx.x * per, j1 = min(N, j0 + per);
+  double run = 0.0;
+  for (int j = j0; j < j1; ++j) run += (double)x[j];
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  double incl = run;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  double base = 0.0;
+  for (int w = 0; w < warp; ++w) base += warp_tot[w];
+  double acc = base + incl - run;    // exclusive prefix of this thread's run
+  if (threadIdx.x == 0) P[0] = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    acc += (double)x[j];
+    P[j + 1] = acc;
+  }
+  __syncthreads();
+  const float half = 0.5f * fmaxf(blur_width(wa, k), 1e-3f);
+  const float nf = (float)N;
+  float* dst = out + k * os_k + line * os_l;
+  for (int c = threadIdx.x; c < N; c += kScanThreads) {
+    const float center = (float)c + 0.5f;
+    const float lo = fminf(fmaxf(center - half, 0.f), nf), hi = fminf(fmaxf(center + half, 0.f), nf);
+    const int a = max(0, (int)floorf(lo)), b = min(N - 1, (int)ceilf(hi) - 1);
+    float sum;
+    if (a >= b) {
+      sum = fmaxf(hi - lo, 0.f) * x[a];
+    } else {
+      const float first = ((float)a + 1.f - lo) * x[a], last = (hi - (float)b) * x[b];
+      sum = (float)((double)first + (P[b] - P[a + 1]) + (double)last);
+    }
+    dst[(int64_t)c * os_p] = sum / (hi - lo);
+  }
+}
+
 // the dense overlap matrices of the same filter, [K, N, N] (scatter_image.py:952-981)
 __global__ void box_matrix_kernel(const float* __restrict__ widths, int N, float* __restrict__ out) {
   const int k = blockIdx.y;
@@ -141,9 +201,15 @@ extern "C" int citrus_box_blur(const float* in, float* out, int64_t num_directio
   CITRUS_REQUIRE(in != out, "citrus_box_blur: in and out must not alias");
   if (num_directions == 0 || lines == 0) return CITRUS_OK;
   WidthArgs wa{widths, height_sums, cell_width, axis, (float)(pitch > 0 ? 1.0 / pitch : 0.0), (float)center_height};
-  dim3 grid((unsigned)cdiv(lines * length, 256), (unsigned)num_directions);
-  box_blur_kernel<<<grid, 256, 0, as_stream(stream)>>>(in, out, (int)num_directions, lines, (int)length, is_k, is_l,
-                                                       is_p, os_k, os_l, os_p, wa);
+  if (length <= kScanMaxN && lines <= 0x7fffffff) {
+    dim3 grid((unsigned)lines, (unsigned)num_directions);
+    box_blur_scan_kernel<<<grid, kScanThreads, 0, as_stream(stream)>>>(in, out, lines, (int)length, is_k, is_l, is_p,
+                                                                       os_k, os_l, os_p, wa);
+  } else {
+    dim3 grid((unsigned)cdiv(lines * length, 256), (unsigned)num_directions);
+    box_blur_kernel<<<grid, 256, 0, as_stream(stream)>>>(in, out, (int)num_directions, lines, (int)length, is_k,
+                                                         is_l, is_p, os_k, os_l, os_p, wa);
+  }
   note_launches();
   return launch_status("citrus_box_blur");
 }
