@@ -44,6 +44,8 @@ def _parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3"],
                    help="arithmetic of the spherical-harmonic products (bf16x3: tcgen05 tensor cores, hi/lo split)")
+    p.add_argument("--no-mixed", action="store_true",
+                   help="skip the second measurement of the step with the tensor-core bf16 hi/lo products")
     p.add_argument("--batch", type=int, default=4,
                    help="views per persistent sweep launch (1: citrus_view_step per view)")
     p.add_argument("--cells", type=int, default=64, help="cells per axis of the step workload (64; smaller for "
@@ -512,6 +514,45 @@ def spr_error(w, solver, angles, device) -> dict:
             "spr_max_rel": worst_spr, "signal_max_rel": worst_signal}
 
 
+def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
+    """The same step with the spherical-harmonic products on the tcgen05 tensor cores (bfloat16 hi/lo split, float32
+    accumulation): ms/view over ``args.steps`` steps after one warm-up step, and its scatter-to-primary error against
+    the float32 products."""
+    import dataclasses
+
+    import torch
+
+    from citrus_gb300.batched import batched_view_steps
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step
+    from citrus_gb300.scatter_solver import ScatterSolver
+
+    mixed = ScatterSolver(solver.library, dataclasses.replace(solver.config, moment_precision="bf16x3"),
+                          solver.geometry, detector=solver.detector, grid_response=solver.grid_response,
+                          device=device)
+    states = [CitrusState() for _ in angles]
+
+    def step():
+        fields = mixed.material_fields(rho_dev, w.grid)
+        if args.batch > 1:
+            _, _, new = batched_view_steps(mixed, states, fields, [float(a) for a in angles], batch=args.batch)
+            states[:] = new
+        else:
+            for v, a in enumerate(angles):
+                _, _, states[v] = citrus_view_step(mixed, states[v], fields, float(a), primary=False)
+
+    step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return {"value": e0.elapsed_time(e1) / (args.steps * len(angles)), "unit": "ms/view", "steps": args.steps,
+            "spr_error": spr_error(w, mixed, angles[:2], device)}
+
+
 def run_step(args):
     import torch
 
@@ -595,6 +636,9 @@ def run_step(args):
     e2e = e0.elapsed_time(e1) / 1e3
     launches = count_launches(lambda: one_step(rho_dev))
     spr = spr_error(w, solver, angles[:2], device) if args.precision != "fp32" else None
+    mixed = None
+    if args.precision == "fp32" and not args.no_mixed:
+        mixed = mixed_precision_step(args, w, solver, angles, rho_dev, device)
     ms_per_view = elapsed * 1e3 / (args.steps * V)
     N = w.grid.num_voxels
     updates = 8 * (w.num_polar * w.num_azimuthal // 8) * N * w.library.num_groups
@@ -624,6 +668,8 @@ def run_step(args):
     }
     if spr is not None:
         line["spr_error"] = spr
+    if mixed is not None:
+        line["mixed_precision_bf16x3"] = mixed
     if rank == 0:
         line["cpu_baseline"] = None if args.no_cpu else cpu_baseline_step(cells=args.cells)
         print(json.dumps(line), flush=True)
