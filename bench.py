@@ -50,6 +50,13 @@ def _parse():
                    help="views per persistent sweep launch (1: citrus_view_step per view)")
     p.add_argument("--cells", type=int, default=64, help="cells per axis of the step workload (64; smaller for "
                                                          "profiling captures)")
+    p.add_argument("--no-learned", action="store_true",
+                   help="skip the learned higher-order proposal measurement (training and converged steps)")
+    p.add_argument("--learned-cells", default="24,24,16",
+                   help="cells of the learned-proposal workload (rows,cols,slices; 96,96,64 is the full size)")
+    p.add_argument("--learned-phantoms", type=int, default=64, help="training phantoms (two views each)")
+    p.add_argument("--learned-epochs", type=int, default=60)
+    p.add_argument("--learned-views", type=int, default=6, help="unseen phantom views of the evaluation")
     return p.parse_args()
 
 
@@ -553,6 +560,99 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
             "spr_error": spr_error(w, mixed, angles[:2], device)}
 
 
+def learned_measurement(args, device) -> dict:
+    """The learned higher-order proposal on the learned-proposal workload (random ellipsoid phantoms, 12 groups, P5,
+    6 x 28 directions, cone 16 x 32, curved 256 x 192 panel) at ``--learned-cells``: the solver generates the
+    training triples, the network (4 levels, 32 base channels) trains on the GPU, and on unseen phantom views the
+    scatter signal is converged per sweep to an SPR change of 0.5 % from the proposal and from the cold start (the
+    plain source iteration). ms/view from CUDA events around each view's converged step; SPR errors against a
+    Neumann series converged to 1e-6."""
+    import numpy as np
+    import torch
+
+    from citrus_gb300 import learned
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step, project_scatter
+    from citrus_gb300.responses import ideal_counting_response, no_grid
+    from citrus_gb300.scatter_solver import ScatterSolver, SolverConfig
+    from citrus_gb300.workloads import ellipsoid_phantom, learned_proposal
+
+    cells = tuple(int(c) for c in args.learned_cells.split(","))
+    w = learned_proposal(1, cells)
+    config = SolverConfig(num_groups=w.library.num_groups, legendre_order=w.legendre_order, num_polar=w.num_polar,
+                          num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
+                          quadrature_point_spacing_cm=w.transport_cell_cm, cone_num_polar=w.cone_num_polar,
+                          cone_num_azimuthal=w.cone_num_azimuthal)
+    solver = ScatterSolver(w.library, config, w.geometry, detector=ideal_counting_response(), grid_response=no_grid(),
+                           device=device)
+    rng = np.random.default_rng(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    samples = []
+    for seed in range(args.learned_phantoms):
+        samples += learned.generate_training_data(solver, [ellipsoid_phantom(w.grid, 1000 + seed)], w.grid,
+                                                  [float(a) for a in rng.uniform(0, 2 * math.pi, 2)])
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    proposal = learned.HigherOrderProposal(w.library.num_materials, w.library.num_groups, seed=0, device=device)
+    losses = proposal.fit(samples, epochs=args.learned_epochs, batch=4, lr=1e-3, seed=0)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    steps = len(samples) // 4 * args.learned_epochs
+    results = {"plain": [], "learned": []}
+    proposal_err, first_cold = [], []
+    stream = torch.cuda.current_stream(device)
+    for k in range(args.learned_views):
+        seed = 5000 + k
+        angle = float(np.random.default_rng(seed).uniform(0, 2 * math.pi))
+        rho = torch.as_tensor(ellipsoid_phantom(w.grid, seed), dtype=torch.float32, device=device)
+        fields = solver.material_fields(rho, w.grid)
+        first, total = learned.collided_orders(solver, fields, angle, tolerance=1e-6)
+        higher = learned.scalar_flux(total) - learned.scalar_flux(first)
+        pred = proposal.predict(fields.rho_coarse, learned.scalar_flux(first))
+        proposal_err.append(float(torch.linalg.vector_norm(pred - higher) / torch.linalg.vector_norm(higher)))
+        phi_uc = solver.uncollided_fluence(fields, angle)
+        cone = solver.cone_quadrature(w.grid, angle)
+        ref = project_scatter(solver, None, w.grid, angle, phi_uc, total, fields, cone, signal_only=True)["signal"]
+        primary = solver.primary(fields, angle)["signal"]
+        mask = primary > 1e-3 * primary.max()
+
+        def spr_err(scatter):
+            return float(((scatter - ref)[mask].abs() / ref[mask].abs()).max())
+
+        cold, _, _ = citrus_view_step(solver, CitrusState(cone_quadrature=cone), fields, angle, primary=False)
+        first_cold.append(spr_err(cold))
+        for name, prop in (("plain", None), ("learned", proposal)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            judged, _ = learned.converged_view_step(solver, fields, angle, prop, primary=primary, cone=cone)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            results[name].append((e0.elapsed_time(e1), judged.sweeps, spr_err(judged.scatter), judged.accepted))
+
+    def summary(rows):
+        return {"ms_per_view": statistics.mean(r[0] for r in rows), "sweeps_mean": statistics.mean(r[1] for r in rows),
+                "spr_err_max": max(r[2] for r in rows), "accepted_in_two_sweeps": sum(bool(r[3]) for r in rows)}
+
+    return {
+        "workload": f"learned_proposal: {cells[0]}x{cells[1]}x{cells[2]} cells x {w.transport_cell_cm:.2f} cm, G=12 "
+                    f"(30-120 keV), P5, 168 sweep directions, cone 16x32, curved 256x192 panel; random ellipsoid "
+                    f"phantoms (water 8-18 cm semi-axes, 0-4 air/soft-tissue/bone inserts)",
+        "network": {"levels": 4, "base_channels": 32, "parameters": proposal.net.num_parameters(),
+                    "weights": "bf16 (float32 master copies)", "accumulate": "f32"},
+        "train": {"phantoms": args.learned_phantoms, "samples": len(samples), "epochs": args.learned_epochs,
+                  "adam_steps": steps, "data_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2),
+                  "ms_per_adam_step": round(1e3 * (t2 - t1) / max(1, steps), 3), "loss_first": losses[0],
+                  "loss_last": losses[-1]},
+        "eval_views": args.learned_views,
+        "proposal_rel_err_max": max(proposal_err),
+        "first_step_spr_err_max": {"cold_start": max(first_cold)},
+        "converged_to_spr_error_estimate": 0.005,
+        "plain": summary(results["plain"]),
+        "learned": summary(results["learned"]),
+    }
+
+
 def run_step(args):
     import torch
 
@@ -666,10 +766,20 @@ def run_step(args):
                                     for n, t in sorted(per_entry.items(), key=lambda x: -sum(x[1]))},
         "clocks": sampler.summary(),
     }
+    sweep_recs = calls.get("citrus_sweep_persistent") or []
+    if sweep_recs:
+        sweep_s = sum(per_entry["citrus_sweep_persistent"])
+        sweep_gbs = sum(info for info, _, _ in sweep_recs) / sweep_s / 1e9
+        line["sweep_roofline"] = {"bound": "hbm", "achieved": sweep_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                  "frac": sweep_gbs / peaks["hbm_gbs"], "launches": len(sweep_recs),
+                                  "kernel_ms_mean": 1e3 * sweep_s / len(sweep_recs),
+                                  "algorithmic_bytes_per_launch": statistics.mean(i for i, _, _ in sweep_recs)}
     if spr is not None:
         line["spr_error"] = spr
     if mixed is not None:
         line["mixed_precision_bf16x3"] = mixed
+    if not args.no_learned and rank == 0:
+        line["learned_proposal"] = learned_measurement(args, device)
     if rank == 0:
         line["cpu_baseline"] = None if args.no_cpu else cpu_baseline_step(cells=args.cells)
         print(json.dumps(line), flush=True)

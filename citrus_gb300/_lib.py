@@ -52,6 +52,16 @@ SIGNATURES = {
     "citrus_weighted_group_sum": [P, P, I64, I64, I64, I64, I64, P, P],
     "citrus_sum_directions": [P, I64, I64, I64, P, I32, P],
     "citrus_weighted_direction_sum": [P, I64, I64, I64, I64, I64, I64, I64, I64, P, I64, I64, P, I32, P],
+    "citrus_conv3d_forward": [P, I64, P, I64, I32, P, P, P, I64, I64, I64, I64, I64, I32, I32, P],
+    "citrus_conv3d_backward_input": [P, I64, P, P, I64, P, P, I64, I64, I64, I64, I64, I32, P],
+    "citrus_conv3d_weight_grad_splits": [I64, I64, I64, I64, I64, I64, I64, I32],
+    "citrus_conv3d_backward_weight": [P, I64, P, I64, P, I64, I32, P, P, I64, I64, I64, I64, I32, P, I64, P],
+    "citrus_avg_pool2": [P, P, I64, I64, I64, I64, P],
+    "citrus_avg_pool2_backward": [P, P, P, I32, I64, I64, I64, I64, P],
+    "citrus_upsample2_backward": [P, P, P, I64, I64, I64, I64, P],
+    "citrus_mse": [P, P, I64, P, P, I64, P],
+    "citrus_adam": [P, P, P, P, P, I64, F64, F64, F64, F64, I64, P],
+    "citrus_to_bf16": [P, P, I64, P],
 }
 
 _LIBRARY: Optional[ctypes.CDLL] = None
@@ -76,6 +86,7 @@ def library() -> ctypes.CDLL:
         lib.citrus_last_error_string.argtypes = []
         lib.citrus_last_error_string.restype = ctypes.c_char_p
         lib.citrus_launch_count.restype = ctypes.c_int64
+        lib.citrus_conv3d_weight_grad_splits.restype = ctypes.c_int64
         _LIBRARY = lib
     return _LIBRARY
 
@@ -123,6 +134,15 @@ def call(name: str, *args) -> None:
 def ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     """Device address of a tensor (None for None)."""
     return None if t is None else t.data_ptr()
+
+
+def upload(a, device, dtype=None) -> torch.Tensor:
+    """A host array on ``device`` through pinned memory, queued on the current stream without waiting for it (a copy
+    from pageable memory would block until every earlier launch on the stream has finished)."""
+    t = torch.as_tensor(a, dtype=dtype)
+    if t.device.type != "cpu" or torch.device(device).type != "cuda":
+        return t.to(device)
+    return t.contiguous().pin_memory().to(device, non_blocking=True)
 
 
 def stream_handle(device: torch.device) -> int:

@@ -41,7 +41,7 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
     Y = ctx.Y.index_select(0, index).contiguous()                  # [8 D8, N_sh]
     Yw_t = ctx.Y_weighted.index_select(0, index).t().contiguous()  # [N_sh, 8 D8]
     mu_cells = fields.mu_t_coarse.reshape(G, N).t().contiguous()
-    syncs = []
+    syncs, norms, pending = [], [], []
     for b0 in range(0, V, batch):
         views = list(range(b0, min(V, b0 + batch)))
         B = len(views)
@@ -76,14 +76,16 @@ def batched_view_steps(solver: ScatterSolver, states: Sequence[CitrusState], fie
             if primary:
                 primaries[v] = solver.primary(fields, float(angles[v]))["signal"]
             prev = previous[j]
-            if prev is None:
-                change = 1.0 if float(torch.linalg.vector_norm(new[:, 0, 0])) > 0 else 0.0
-            else:
-                norm, diff = torch.stack([torch.linalg.vector_norm(new[:, 0, 0]),
-                                          torch.linalg.vector_norm(new[:, 0, 0] - prev[:, 0, 0])]).tolist()
-                change = diff / norm if norm > 0 else 0.0
-            new_states[v] = CitrusState(angle=float(angles[v]), collided_moments=new, cone_quadrature=cone,
-                                        num_steps=states[v].num_steps + 1, history=states[v].history + [change])
+            norm = torch.linalg.vector_norm(new[:, 0, 0])
+            diff = norm if prev is None else torch.linalg.vector_norm(new[:, 0, 0] - prev[:, 0, 0])
+            norms.append(torch.stack([norm, diff]))
+            pending.append((v, new, cone, prev is None))
+    # one read-back for every view's change norm and the sweeps' barrier words, after all launches are queued
     if syncs and bool(torch.stack([w[2] for w in syncs]).ne(0).any()):
         raise kernels._lib.CitrusKernelError("batched sweep: a grid-barrier wait of the persistent sweep ran out")
+    values = torch.stack(norms).tolist() if norms else []
+    for (v, new, cone, cold), (norm, diff) in zip(pending, values):
+        change = (1.0 if norm > 0 else 0.0) if cold else (diff / norm if norm > 0 else 0.0)
+        new_states[v] = CitrusState(angle=float(angles[v]), collided_moments=new, cone_quadrature=cone,
+                                    num_steps=states[v].num_steps + 1, history=states[v].history + [change])
     return signals, primaries, new_states

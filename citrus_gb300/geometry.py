@@ -15,6 +15,8 @@ import numpy as np
 import torch
 from torch import Tensor
 
+_DEVICE_AXES: dict = {}   # (grid, device, dtype) -> axis coordinates on the device
+
 
 @dataclass(frozen=True)
 class Grid:
@@ -79,6 +81,15 @@ class Grid:
         y = dy * (np.arange(nr, dtype=np.float64) - (nr - 1) / 2)
         z = dz * (np.arange(ns, dtype=np.float64) - (ns - 1) / 2) + self.recon_slice_offset
         return tuple(torch.as_tensor(a, dtype=dtype, device=device) for a in (x, y, z))
+
+    def device_axes(self, device, dtype=torch.float32) -> tuple:
+        """``axis_coordinates`` on ``device``, copied there once per (grid, device, dtype) and kept."""
+        key = (self, str(torch.device(device)), dtype)
+        axes = _DEVICE_AXES.get(key)
+        if axes is None:
+            axes = tuple(a.to(device) for a in self.axis_coordinates(dtype=dtype))
+            _DEVICE_AXES[key] = axes
+        return axes
 
     def center_coordinates(self, device=None, dtype=torch.float32) -> Tensor:
         """[rows, cols, slices, 3] voxel-centre positions (x, y, z)."""

@@ -124,7 +124,7 @@ class GB300Projectors:
             _lib.call("citrus_trace_from_source", vol.data_ptr(), C, box, dims, host.doubles(source), pts.data_ptr(),
                       None, None, None, None, P, out.data_ptr(), _lib.stream_handle(device))
             return out
-        ax = [a.to(device) for a in point_grid.axis_coordinates(dtype=torch.float64)]
+        ax = point_grid.device_axes(device, torch.float64)
         P = point_grid.num_voxels
         out = torch.empty(C, P, device=device, dtype=torch.float32)
         _lib.call("citrus_trace_from_source", vol.data_ptr(), C, box, dims, host.doubles(source), None,
@@ -169,8 +169,8 @@ class GB300Projectors:
         device = mu.device
         omegas = omegas.to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
         K = omegas.shape[0]
-        n_hat = torch.tensor(geometry.panel_axes(angle)[2], dtype=torch.float32, device=device)
-        toward = ((omegas * (-n_hat)).sum(-1) > 0).to(torch.uint8).contiguous()
+        n = [float(v) for v in geometry.panel_axes(angle)[2]]
+        toward = ((omegas[:, 0] * -n[0] + omegas[:, 1] * -n[1] + omegas[:, 2] * -n[2]) > 0).to(torch.uint8)
         C, V = int(mu.shape[0]), grid.num_voxels
         if voxel_major:
             out = torch.empty(K, V, C, device=device, dtype=torch.float32)
@@ -216,8 +216,7 @@ class GB300Projectors:
         else:
             raise ValueError(f"field must be [C, ...] or [K={K}, C, ...], got {tuple(field.shape)}")
         Rd, Cd = geometry.image_shape
-        pixels = torch.as_tensor(np.ascontiguousarray(geometry.pixel_centers_np(angle).reshape(-1, 3)),
-                                 dtype=torch.float64).to(device)
+        pixels = _lib.upload(geometry.pixel_centers_np(angle).reshape(-1, 3), device, torch.float64)
         if out is None:
             out = torch.empty(K, C, Rd, Cd, device=device, dtype=torch.float32)
         if tuple(out.shape) != (K, C, Rd, Cd):

@@ -263,8 +263,7 @@ class ScatterSolver:
                                             sweep_context: Optional[SweepContext] = None
                                             ) -> FirstCollisionSamplingCorrection:
         ctx = self.sweep_context(fields.grid_coarse) if sweep_context is None else sweep_context
-        om = torch.as_tensor(ctx.quadrature.omega, dtype=torch.float32).to(self.device)
-        w = torch.as_tensor(ctx.quadrature.weight, dtype=torch.float32).to(self.device)
+        om, w = ctx.omega, ctx.weight
         # keep the source values for the LD moments of the sweep's source when they fit the chunk budget
         keep = om.shape[0] * self.num_groups * fields.grid_quadrature.num_voxels * 4 <= SWEEP_CHUNK_BUDGET_BYTES
         return first_collision_sampling_correction(self.library, fields.rho_quadrature, phi_uncollided,
@@ -275,7 +274,7 @@ class ScatterSolver:
                                       sweep_context: Optional[SweepContext] = None):
         """Cell-major sweep source function of the corrected first-collision source (reference ``:774-826``)."""
         ctx = self.sweep_context(fields.grid_coarse) if sweep_context is None else sweep_context
-        omega = torch.as_tensor(ctx.quadrature.omega, dtype=torch.float32).to(self.device)
+        omega = ctx.omega
         correction = self.first_collision_sampling_correction(fields, angle, phi_uncollided, ctx)
         library, geometry = self.library, self.geometry
 

@@ -97,6 +97,8 @@ class SweepContext:
     Y_weighted: Tensor
     flat_index: kernels.FlatPlaneIndex
     device: torch.device
+    omega: Tensor = None       # [8 D8, 3] float32 directions of the reordered quadrature
+    weight: Tensor = None      # [8 D8] float32 weights
 
     @property
     def num_cells(self) -> int:
@@ -116,9 +118,9 @@ class SweepContext:
 
     def direction_indices(self, start: int, stop: int) -> Tensor:
         """Octant-major reordered indices of the per-octant chunk ``start <= d < stop``: ``o * D8 + d``."""
-        d = torch.arange(start, stop, dtype=torch.int64)
-        o = torch.arange(8, dtype=torch.int64)
-        return (o[:, None] * self.directions_per_octant + d[None, :]).reshape(-1).to(self.device)
+        d = torch.arange(start, stop, dtype=torch.int64, device=self.device)
+        o = torch.arange(8, dtype=torch.int64, device=self.device)
+        return (o[:, None] * self.directions_per_octant + d[None, :]).reshape(-1)
 
 
 def make_sweep_context(grid: Grid, quadrature: Quadrature, L: int, device) -> SweepContext:
@@ -153,7 +155,9 @@ def make_sweep_context(grid: Grid, quadrature: Quadrature, L: int, device) -> Sw
     return SweepContext(shape=tuple(grid.shape), deltas=deltas, L=int(L), plan=plan, quadrature=reordered,
                         permutation=permutation, basis=basis, directions_per_octant=D8, c=to_device(c, device),
                         s=to_device(s, device), Y=to_device(basis.Y, device),
-                        Y_weighted=to_device(basis.Y_weighted, device), flat_index=flat, device=device)
+                        Y_weighted=to_device(basis.Y_weighted, device), flat_index=flat, device=device,
+                        omega=torch.as_tensor(reordered.omega, dtype=torch.float32).to(device),
+                        weight=torch.as_tensor(reordered.weight, dtype=torch.float32).to(device))
 
 
 def source_function_accepts_out(source_function) -> bool:

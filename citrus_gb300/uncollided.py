@@ -66,8 +66,7 @@ def moment_table(library: MultigroupLibrary, device) -> Tensor:
 
 def point_axes(grid: Grid, device) -> Tensor:
     """float32 x [cols], y [rows], z [slices] of a point grid, back to back (as the kernels read them)."""
-    x, y, z = grid.axis_coordinates(dtype=torch.float32)
-    return torch.cat([x, y, z]).to(device)
+    return torch.cat(grid.device_axes(device, torch.float32))
 
 
 def _eta_range(library: MultigroupLibrary) -> tuple:
@@ -84,7 +83,7 @@ def source_weight(source: SourceModel, geometry: ConeGeometry, angle: float, poi
                   divide_by_distance_squared: bool = True) -> Tensor:
     """[V] b(Omega) / |r - r0|^2 at the centres of a point grid."""
     host = HostArgs()
-    ax = [a.to(device) for a in points.axis_coordinates(dtype=torch.float64)]
+    ax = points.device_axes(device, torch.float64)
     out = torch.empty(points.num_voxels, device=device, dtype=torch.float32)
     _lib.call("citrus_source_weight", host.doubles(source.field_args(geometry, angle)), None, ax[0].data_ptr(),
               ax[1].data_ptr(), ax[2].data_ptr(), host.int64s(points.shape), points.num_voxels,

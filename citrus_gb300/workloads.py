@@ -115,6 +115,47 @@ def batched_views(seed: int = 1, cells: int = 64) -> Workload:
                     60)
 
 
+INSERT_DENSITIES = (0.0012, 1.04, 1.85)   # air, soft tissue (water material), bone
+
+
+def ellipsoid_phantom(grid: Grid, seed: int) -> np.ndarray:
+    """[2, R, C, S] float64 densities (water, bone) of one random phantom: a water ellipsoid (1.0 g/cc) in air with
+    semi-axes drawn uniformly from 8-18 cm (truncated by the volume) and 0-4 ellipsoid inserts of air, soft tissue
+    or bone, each with semi-axes of 1-4 cm and a centre inside the water ellipsoid."""
+    rng = np.random.default_rng(seed)
+    x, y, z = (a.double().numpy() for a in grid.axis_coordinates(dtype=torch.float64))
+    Y, X, Z = np.meshgrid(y, x, z, indexing="ij")
+    axes = rng.uniform(8.0, 18.0, 3)
+    inside = (X / axes[0]) ** 2 + (Y / axes[1]) ** 2 + (Z / axes[2]) ** 2 < 1.0
+    water = np.where(inside, 1.0, 0.0012)
+    bone = np.zeros_like(water)
+    for _ in range(int(rng.integers(0, 5))):
+        u = rng.standard_normal(3)
+        centre = u / np.linalg.norm(u) * rng.uniform(0.0, 0.7) * axes
+        semi = rng.uniform(1.0, 4.0, 3)
+        rho = INSERT_DENSITIES[int(rng.integers(0, 3))]
+        region = (((X - centre[0]) / semi[0]) ** 2 + ((Y - centre[1]) / semi[1]) ** 2
+                  + ((Z - centre[2]) / semi[2]) ** 2 < 1.0) & inside
+        if rho > 1.5:
+            water[region], bone[region] = 0.0, rho
+        else:
+            water[region], bone[region] = rho, 0.0
+    return np.stack([water, bone])
+
+
+def learned_proposal(seed: int = 1, cells: tuple = (96, 96, 64)) -> Workload:
+    """The learned-proposal workload: a 38.4 x 38.4 x 25.6 cm volume of ``cells`` cubic cells (96 x 96 x 64: 0.4 cm),
+    a random ellipsoid phantom of ``seed``, 12 groups from 120 to 30 keV, P5, 6 x 28 = 168 sweep directions, cone
+    16 x 32, the curved 256 x 192 panel and 120 views. Smaller ``cells`` give the same scene on coarser cells."""
+    rows, cols, slices = (int(c) for c in cells)
+    cell = 38.4 / rows
+    grid = Grid((rows, cols, slices), cell)
+    edges = np.linspace(120.0, 30.0, 13)
+    lib = spectral_library(edges, bremsstrahlung_spectrum(seed=0), [WATER, BONE], legendre_order=5)
+    geo = ConeGeometry(100.0, 150.0, 192, 256, 0.16, 0.16, use_curved_detector=True)
+    return Workload("learned_proposal", grid, geo, ellipsoid_phantom(grid, seed), lib, 6, 28, 5, cell, 120)
+
+
 # ---- sweep-only problem of the benchmark ----------------------------------------------------------------------------
 
 def config2_sweep_problem_host() -> dict:

@@ -299,6 +299,64 @@ int citrus_state_decode(const uint16_t* data, const float* scale, int64_t groups
 int citrus_attenuation_to_density(const float* X, int64_t num_voxels, const float* mu, const float* mass,
                                   const float* nominal, int64_t num_materials, int64_t slot, float* out, void* stream);
 
+/* ------------------------------------------------------------------------------------------------------------------
+ * Learned higher-order proposal: the layers of a 3D U-Net on the transport cells and their gradients. The reference
+ * has no counterpart (its cold start is an empty accumulator, citrus/citrus.py:70-87 and :192-247); these entry points
+ * train and run the network that proposes the higher collision orders of that accumulator.
+ * Volumes are NCDHW float32 [batch, C, depth, height, width]; weights bfloat16 bit patterns [C_out, C_in, k, k, k]
+ * (k = 1 or 3, zero padding k / 2); float32 accumulation.
+ * ------------------------------------------------------------------------------------------------------------------ */
+
+/* out = act(bias + w * [A, up(B)]): input channels [0, channels_a) from in_a, [channels_a, channels_a + channels_b)
+ * from in_b (at half resolution, nearest 2x upsampling, when b_upsampled); act = ReLU when relu != 0. */
+int citrus_conv3d_forward(const float* in_a, int64_t channels_a, const float* in_b, int64_t channels_b,
+                          int32_t b_upsampled, const uint16_t* weight, const float* bias, float* out,
+                          int64_t channels_out, int64_t batch, int64_t depth, int64_t height, int64_t width,
+                          int32_t kernel_size, int32_t relu, void* stream);
+
+/* Input gradient of citrus_conv3d_forward: grad_a (channels_a, times (mask_a > 0) when mask_a is set) and grad_b
+ * (channels_b, at full resolution, before the upsampling's backward pass) from grad_out (channels_out). */
+int citrus_conv3d_backward_input(const float* grad_out, int64_t channels_out, const uint16_t* weight, float* grad_a,
+                                 int64_t channels_a, const float* mask_a, float* grad_b, int64_t channels_b,
+                                 int64_t batch, int64_t depth, int64_t height, int64_t width, int32_t kernel_size,
+                                 void* stream);
+
+/* Partial sums the weight gradient uses for these sizes: it wants partial_capacity >= splits * C_out * C_in * k^3
+ * floats (fewer splits, or none, with less). */
+int64_t citrus_conv3d_weight_grad_splits(int64_t channels_out, int64_t channels_a, int64_t channels_b, int64_t batch,
+                                         int64_t depth, int64_t height, int64_t width, int32_t kernel_size);
+
+/* grad_weight [C_out, C_in, k^3] and grad_bias [C_out] (null: skipped) of citrus_conv3d_forward, reduced over the
+ * batch and the voxels in a fixed order. */
+int citrus_conv3d_backward_weight(const float* grad_out, int64_t channels_out, const float* in_a, int64_t channels_a,
+                                  const float* in_b, int64_t channels_b, int32_t b_upsampled, float* grad_weight,
+                                  float* grad_bias, int64_t batch, int64_t depth, int64_t height, int64_t width,
+                                  int32_t kernel_size, float* partial, int64_t partial_capacity, void* stream);
+
+/* 2x2x2 average pooling of [batch_channels, depth, height, width] (even sizes) and its backward pass:
+ * grad_in = ((accumulate ? grad_in : 0) + grad_out / 8 at the parent) * (mask > 0 when mask is set). */
+int citrus_avg_pool2(const float* in, float* out, int64_t batch_channels, int64_t depth, int64_t height,
+                     int64_t width, void* stream);
+int citrus_avg_pool2_backward(const float* grad_out, float* grad_in, const float* mask, int32_t accumulate,
+                              int64_t batch_channels, int64_t depth, int64_t height, int64_t width, void* stream);
+
+/* Backward pass of the nearest 2x upsampling: grad_coarse [batch_channels, depth, height, width] = sum of the eight
+ * children in grad_fine, times (mask_coarse > 0) when mask_coarse is set. */
+int citrus_upsample2_backward(const float* grad_fine, const float* mask_coarse, float* grad_coarse,
+                              int64_t batch_channels, int64_t depth, int64_t height, int64_t width, void* stream);
+
+/* grad = 2 (pred - target) / n and partial[block] = the squared errors of each block of 256 elements. */
+int citrus_mse(const float* pred, const float* target, int64_t n, float* grad, float* partial,
+               int64_t partial_capacity, void* stream);
+
+/* One Adam step (bias-corrected, step >= 1) of float32 parameters; param_bf16 (optional) receives their bfloat16
+ * rounding. */
+int citrus_adam(float* param, const float* grad, float* m, float* v, uint16_t* param_bf16, int64_t n, double lr,
+                double beta1, double beta2, double eps, int64_t step, void* stream);
+
+/* dst = bfloat16 rounding (to nearest even) of src. */
+int citrus_to_bf16(const float* src, uint16_t* dst, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
