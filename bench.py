@@ -46,10 +46,12 @@ def _parse():
                    help="arithmetic of the spherical-harmonic products (bf16x3: tcgen05 tensor cores, hi/lo split)")
     p.add_argument("--no-mixed", action="store_true",
                    help="skip the second measurement of the step with the tensor-core bf16 hi/lo products")
-    p.add_argument("--batch", type=int, default=4,
-                   help="views per persistent sweep launch (1: citrus_view_step per view)")
+    p.add_argument("--batch", type=int, default=0,
+                   help="views per persistent sweep launch (0: the autotuner's choice; 1: citrus_view_step per view)")
     p.add_argument("--cells", type=int, default=64, help="cells per axis of the step workload (64; smaller for "
                                                          "profiling captures)")
+    p.add_argument("--no-graph", dest="graph", action="store_false",
+                   help="run every step eagerly instead of replaying the outer iteration from a CUDA graph")
     p.add_argument("--no-learned", action="store_true",
                    help="skip the learned higher-order proposal measurement (training and converged steps)")
     p.add_argument("--learned-cells", default="24,24,16",
@@ -418,9 +420,13 @@ def make_step_solver(device, views: int = 0, cells: int = 64, precision: str = "
 STEP_METRIC = "scatter-step ms/view (all views of one outer iteration; cell*dir*group updates/s alongside)"
 
 
-def step_workload_name(cells: int, views: int, batch: int = 1) -> str:
-    how = ("citrus_view_step per view" if batch <= 1 else
+def step_workload_name(cells: int, views: int, batch: int = 1, graph: bool = False) -> str:
+    how = ("citrus_view_step per view" if batch == 1 else
+           "batched_view_steps, the accumulator sweeps of several views per persistent launch (views per launch "
+           "picked by the autotuner)" if batch <= 0 else
            f"batched_view_steps, the accumulator sweeps of {batch} views per persistent launch")
+    if graph:
+        how = f"GraphedOuterIteration: {how}, the outer iteration replayed from one CUDA graph"
     return (f"batched_views: {cells}^3 cells x {25.6 / cells:g} cm, G=8 (30-120 keV), P5, 120 sweep directions, cone "
             f"16x32, curved 256x192 panel, {views} views per rank per step, one accumulator sweep per view ({how}, "
             f"signal only)")
@@ -475,8 +481,9 @@ def sweep_bytes(args) -> int:
 
 STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_attenuated_emission": product_emission_bytes,
               "citrus_downstream_cumulative": downstream_bytes,
-              "citrus_sweep_persistent": sweep_bytes, "citrus_oblique_project": None, "citrus_box_blur": None,
-              "citrus_small_k_gemm": None, "citrus_small_k_gemm_bf16x3": None, "citrus_first_collision_moments": None,
+              "citrus_sweep_persistent": sweep_bytes, "citrus_sweep_persistent_config": sweep_bytes,
+              "citrus_oblique_project": None, "citrus_box_blur": None, "citrus_small_k_gemm": None,
+              "citrus_small_k_gemm_config": None, "citrus_small_k_gemm_bf16x3": None, "citrus_first_collision_moments": None,
               "citrus_first_collision_correction": None, "citrus_scattering_moments": None}
 
 
@@ -529,7 +536,7 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
 
     import torch
 
-    from citrus_gb300.batched import batched_view_steps
+    from citrus_gb300.batched import GraphedOuterIteration, batched_view_steps
     from citrus_gb300.citrus_step import CitrusState, citrus_view_step
     from citrus_gb300.scatter_solver import ScatterSolver
 
@@ -537,8 +544,12 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
                           solver.geometry, detector=solver.detector, grid_response=solver.grid_response,
                           device=device)
     states = [CitrusState() for _ in angles]
+    graphed = GraphedOuterIteration(mixed, w.grid, angles, batch=args.batch) if args.graph else None
 
     def step():
+        if graphed is not None:
+            graphed.step(rho_dev)
+            return
         fields = mixed.material_fields(rho_dev, w.grid)
         if args.batch > 1:
             _, _, new = batched_view_steps(mixed, states, fields, [float(a) for a in angles], batch=args.batch)
@@ -547,7 +558,8 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
             for v, a in enumerate(angles):
                 _, _, states[v] = citrus_view_step(mixed, states[v], fields, float(a), primary=False)
 
-    step()
+    for _ in range(2 if graphed is not None else 1):   # the cold start, then the warm step and its capture
+        step()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(device)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -556,7 +568,10 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
         step()
     e1.record(stream)
     torch.cuda.synchronize()
-    return {"value": e0.elapsed_time(e1) / (args.steps * len(angles)), "unit": "ms/view", "steps": args.steps,
+    value = e0.elapsed_time(e1) / (args.steps * len(angles))
+    del graphed, states
+    torch.cuda.empty_cache()
+    return {"value": value, "unit": "ms/view", "steps": args.steps, "cuda_graph": bool(args.graph),
             "spr_error": spr_error(w, mixed, angles[:2], device)}
 
 
@@ -657,7 +672,7 @@ def run_step(args):
     import torch
 
     from citrus_gb300 import _lib
-    from citrus_gb300.batched import batched_view_steps
+    from citrus_gb300.batched import GraphedOuterIteration, batched_view_steps, resolve_batch
     from citrus_gb300.citrus_step import CitrusState, citrus_view_step
 
     rank = int(os.environ.get("RANK", "0"))
@@ -675,10 +690,14 @@ def run_step(args):
     V = len(angles)
     rho_host = torch.as_tensor(w.rho, dtype=torch.float32).pin_memory()
     rho_dev = rho_host.to(device)
+    requested_batch = args.batch
+    if args.batch <= 0:
+        args.batch = resolve_batch(solver, solver.material_fields(rho_dev, w.grid), V, 0)
     states = [CitrusState() for _ in angles]
     stream = torch.cuda.current_stream(device)
+    graphed = GraphedOuterIteration(solver, w.grid, angles, batch=args.batch) if args.graph else None
 
-    def one_step(rho, signals=None):
+    def eager_step(rho, signals=None):
         fields = solver.material_fields(rho, w.grid)
         if args.batch > 1:
             out, _, new_states = batched_view_steps(solver, states, fields, [float(a) for a in angles],
@@ -692,6 +711,13 @@ def run_step(args):
             if signals is not None:
                 signals[v].copy_(scatter, non_blocking=True)
 
+    def one_step(rho, signals=None):
+        if graphed is None:
+            return eager_step(rho, signals)
+        out, _ = graphed.step(rho)
+        if signals is not None:
+            signals.copy_(out, non_blocking=True)
+
     sampler = ClockSampler(local)  # started before the warm-up: its first nvidia-smi call is slow
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with sampler:
@@ -701,28 +727,17 @@ def run_step(args):
         if dist:
             dist.barrier()
         t_start = time.monotonic()
-        with _lib.timed_calls(*STEP_TIMED, capture={n: f for n, f in STEP_TIMED.items() if f}) as calls:
-            start.record(stream)
-            for _ in range(args.steps):
-                one_step(rho_dev)
-            end.record(stream)
-            torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            one_step(rho_dev)
+        end.record(stream)
+        torch.cuda.synchronize()
         sampler.mark(t_start, time.monotonic())
     elapsed = start.elapsed_time(end) / 1e3
     if dist:
         t = torch.tensor([elapsed], device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t)
-    # entry points timed inside the timed region (CUDA events on the launch stream); the roofline is reported for
-    # the one with the largest share among those with an algorithmic byte count
-    per_entry = {}
-    for name, recs in calls.items():
-        if recs:
-            per_entry[name] = [a.elapsed_time(b) / 1e3 for _, a, b in recs]
-    ranked = sorted((n for n in per_entry if STEP_TIMED[n] is not None), key=lambda n: -sum(per_entry[n]))
-    top = ranked[0] if ranked else None
-    top_s = per_entry[top] if top else []
-    top_bytes = [info for info, _, _ in calls[top]] if top else []
     # e2e: the densities in from pinned host memory, every view's scatter signal out to pinned host memory
     Rd, Cd = w.geometry.image_shape
     host_signals = torch.empty(V, Rd, Cd, dtype=torch.float32).pin_memory()
@@ -734,7 +749,31 @@ def run_step(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e = e0.elapsed_time(e1) / 1e3
-    launches = count_launches(lambda: one_step(rho_dev))
+    graph_replays = 0 if graphed is None else graphed.replays
+    del graphed, one_step
+    torch.cuda.empty_cache()
+    # the entry points of one eager step of the same views (CUDA events on the launch stream around every call;
+    # a graph replay has no calls to time), outside the timed region
+    if args.graph:
+        for _ in range(2):
+            eager_step(rho_dev)
+    torch.cuda.synchronize()
+    with _lib.timed_calls(*STEP_TIMED, capture={n: f for n, f in STEP_TIMED.items() if f}) as calls:
+        eager_step(rho_dev)
+        torch.cuda.synchronize()
+    breakdown_steps = 1
+    per_entry = {}
+    for name, recs in calls.items():
+        if recs:
+            per_entry[name] = [a.elapsed_time(b) / 1e3 for _, a, b in recs]
+    # the roofline is reported for the entry point with the largest share among those with an algorithmic byte count
+    ranked = sorted((n for n in per_entry if STEP_TIMED[n] is not None), key=lambda n: -sum(per_entry[n]))
+    top = ranked[0] if ranked else None
+    top_s = per_entry[top] if top else []
+    top_bytes = [info for info, _, _ in calls[top]] if top else []
+    launches = count_launches(lambda: eager_step(rho_dev))   # a replay launches the same kernels as the eager step
+    states.clear()
+    torch.cuda.empty_cache()
     spr = spr_error(w, solver, angles[:2], device) if args.precision != "fp32" else None
     mixed = None
     if args.precision == "fp32" and not args.no_mixed:
@@ -749,26 +788,30 @@ def run_step(args):
         "value": ms_per_view / max(1, world), "unit": "ms/view", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom and library)",
-        "config": {"workload": step_workload_name(args.cells, V, args.batch),
+        "config": {"workload": step_workload_name(args.cells, V, requested_batch, args.graph),
                    "l2": "inputs larger than L2 (4 GB sweep store per view)",
-                   "moment_precision": args.precision, "views_per_sweep_launch": args.batch},
+                   "moment_precision": args.precision, "views_per_sweep_launch": args.batch,
+                   "views_per_sweep_launch_autotuned": requested_batch <= 0},
         "updates_per_s": updates * V * args.steps * world / elapsed,
         "e2e": {"value": e2e * 1e3 / (args.steps * V) / max(1, world), "unit": "ms/view",
                 "h2d_bytes_per_step": rho_host.numel() * 4, "d2h_bytes_per_step": host_signals.numel() * 4},
         "gpu_launches": launches["citrus"] * args.steps,
+        "cuda_graph": {"outer_iteration_replayed": bool(args.graph), "replays": graph_replays},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": None if achieved is None else achieved / peaks["hbm_gbs"], "traffic": None,
                      "peak_source": peaks["source"],
                      "entry_point": top, "launches": len(top_s),
                      "kernel_ms_mean": 1e3 * statistics.mean(top_s) if top_s else None,
                      "algorithmic_bytes_per_launch": statistics.mean(top_bytes) if top_bytes else None},
-        "entry_point_ms_per_view": {n: round(1e3 * sum(t) / (args.steps * V), 3)
+        "entry_point_ms_per_view": {n: round(1e3 * sum(t) / (breakdown_steps * V), 3)
                                     for n, t in sorted(per_entry.items(), key=lambda x: -sum(x[1]))},
         "clocks": sampler.summary(),
     }
-    sweep_recs = calls.get("citrus_sweep_persistent") or []
+    sweep_name = "citrus_sweep_persistent_config" if calls.get("citrus_sweep_persistent_config") else \
+        "citrus_sweep_persistent"
+    sweep_recs = calls.get(sweep_name) or []
     if sweep_recs:
-        sweep_s = sum(per_entry["citrus_sweep_persistent"])
+        sweep_s = sum(per_entry[sweep_name])
         sweep_gbs = sum(info for info, _, _ in sweep_recs) / sweep_s / 1e9
         line["sweep_roofline"] = {"bound": "hbm", "achieved": sweep_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                   "frac": sweep_gbs / peaks["hbm_gbs"], "launches": len(sweep_recs),

@@ -26,8 +26,10 @@ SIGNATURES = {
     "citrus_launch_count": [],
     "citrus_sweep_planes": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P],
     "citrus_sweep_persistent": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, I64, I64, P],
+    "citrus_sweep_persistent_config": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, I32, I64, I64, P],
     "citrus_sweep_persistent_static": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, P],
     "citrus_small_k_gemm": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P],
+    "citrus_small_k_gemm_config": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, I32, I32, P],
     "citrus_small_k_gemm_bf16x3": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P, P],
     "citrus_state_encode": [P, I64, I64, I64, I64, I64, I64, P, P, P],
     "citrus_state_decode": [P, P, I64, I64, I64, P, I64, I64, I64, I64, P],

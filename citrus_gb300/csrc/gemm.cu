@@ -337,9 +337,32 @@ int launch(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, i
 
 using namespace citrus;
 
-extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
-                                   int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
-                                   int32_t accumulate, void* stream) {
+namespace {
+
+int launch_tiled(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int m, int k,
+                 int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int accumulate, int tile_rows,
+                 cudaStream_t s) {
+  switch (tile_rows) {
+    case 1: return launch<1>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 2: return launch<2>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 3: return launch<3>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 4: return launch<4>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 5: return launch<5>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 6: return launch<6>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 8: return launch<8>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 12: return launch<12>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    case 16: return launch<16>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+    default: return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: tile of %d row groups (1-6, 8, 12 or 16)",
+                              tile_rows);
+  }
+}
+
+}  // namespace
+
+extern "C" int citrus_small_k_gemm_config(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                                          int64_t ldc, int64_t M, int64_t K, int64_t J, int64_t batch,
+                                          int64_t stride_b, int64_t stride_c, int32_t accumulate, int32_t variant,
+                                          int32_t tile_rows, void* stream) {
   CITRUS_REQUIRE(A && B && C, "citrus_small_k_gemm: null pointer argument");
   CITRUS_REQUIRE(M >= 1 && K >= 1 && J >= 0 && batch >= 1 && batch <= 65535,
                  "citrus_small_k_gemm: bad sizes M %lld K %lld J %lld batch %lld", (long long)M, (long long)K,
@@ -347,11 +370,16 @@ extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, 
   CITRUS_REQUIRE(K <= 1024 && M <= (1 << 20), "citrus_small_k_gemm: K %lld or M %lld too large", (long long)K,
                  (long long)M);
   CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "citrus_small_k_gemm: leading dimensions too small");
+  CITRUS_REQUIRE(variant >= 0 && variant <= 2, "citrus_small_k_gemm: variant %d (0 auto, 1 streaming, 2 tiled)",
+                 variant);
   if (J == 0) return CITRUS_OK;
   const int m = (int)M, k = (int)K;
   const int rows = (m + 7) / 8;
   cudaStream_t s = as_stream(stream);
-  if (K <= 64 || (M <= 64 && K * 64 * 4 <= 200 * 1024)) {  // the streaming forms
+  const bool streaming_fits = K <= 64 || (M <= 64 && K * 64 * 4 <= 200 * 1024);
+  CITRUS_REQUIRE(variant != 1 || streaming_fits,
+                 "citrus_small_k_gemm: the streaming forms need K <= 64, or M <= 64 with K <= 800");
+  if (variant == 1 || (variant == 0 && streaming_fits)) {
     const bool pair = J % 2 == 0 && ldb % 2 == 0 && ldc % 2 == 0 && stride_b % 2 == 0 && stride_c % 2 == 0 &&
                       ((uintptr_t)B % 8) == 0 && ((uintptr_t)C % 8) == 0;
     if (pair && accumulate)
@@ -360,15 +388,25 @@ extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, 
     if (accumulate) return launch_stream<false, true>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s);
     return launch_stream<false, false>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s);
   }
-  if (8ll * 16 * K * 4 + kChunk * kCols * 4 > 200 * 1024)
-    return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: K %lld too large for the shared-memory tile", (long long)K);
-  if (rows <= 1) return launch<1>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 2) return launch<2>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 3) return launch<3>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 4) return launch<4>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 5) return launch<5>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 6) return launch<6>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 8) return launch<8>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  if (rows <= 12) return launch<12>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
-  return launch<16>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, s);
+  int tile = tile_rows;
+  if (tile == 0) {
+    static const int kTiles[] = {1, 2, 3, 4, 5, 6, 8, 12, 16};
+    tile = 16;
+    for (int t : kTiles)
+      if (rows <= t) {
+        tile = t;
+        break;
+      }
+  }
+  if (8ll * tile * K * 4 + kChunk * kCols * 4 > 200 * 1024)
+    return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: K %lld too large for a shared-memory tile of %d row groups",
+                     (long long)K, tile);
+  return launch_tiled(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, tile, s);
+}
+
+extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                                   int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
+                                   int32_t accumulate, void* stream) {
+  return citrus_small_k_gemm_config(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, accumulate, 0, 0,
+                                    stream);
 }

@@ -20,14 +20,21 @@ __device__ __forceinline__ float4 load4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
 }
 
-// One lane: entry e of the plane, direction d of the chunk, group g, view v. Upstream neighbours lie on the previous
-// plane (already swept); an upstream index N is a vacuum face and reads zeros.
+// The inputs of one lane: entry e of the plane, direction d of the chunk, group g, view v. Upstream neighbours lie on
+// the previous plane (already swept); an upstream index N is a vacuum face and reads zeros.
+struct LaneIn {
+  float4 s, X, Y, Z;  // source moments, and (psi0, psi_x, psi_y, psi_z) of the x, y, z upstream neighbours
+  float cx, cy, cz, m;
+  int o;
+  float* dst;
+};
+
 template <int kG, bool kCoherent>
-__device__ __forceinline__ void solve_lane(int64_t lane, float* __restrict__ store, const float* __restrict__ mu,
-                                           const float* __restrict__ c, const int* __restrict__ octant,
-                                           const int* __restrict__ cell, const int* __restrict__ upstream,
-                                           int64_t start, int64_t E, int64_t N, int G_runtime, int64_t Dc,
-                                           int64_t view_stride) {
+__device__ __forceinline__ void gather_lane(int64_t lane, LaneIn& in, float* __restrict__ store,
+                                            const float* __restrict__ mu, const float* __restrict__ c,
+                                            const int* __restrict__ octant, const int* __restrict__ cell,
+                                            const int* __restrict__ upstream, int64_t start, int64_t E, int64_t N,
+                                            int G_runtime, int64_t Dc, int64_t view_stride) {
   const int G = kG > 0 ? kG : G_runtime;
   const int g = (int)(lane % G);
   int64_t t = lane / G;
@@ -39,16 +46,26 @@ __device__ __forceinline__ void solve_lane(int64_t lane, float* __restrict__ sto
   const int64_t n = __ldg(cell + e);
   const int64_t ux = __ldg(upstream + 3 * e), uy = __ldg(upstream + 3 * e + 1), uz = __ldg(upstream + 3 * e + 2);
   const int64_t od = (int64_t)o * Dc + d;
-  const float cx = __ldg(c + 3 * od), cy = __ldg(c + 3 * od + 1), cz = __ldg(c + 3 * od + 2);
-  const float sx = (o & 4) ? -1.f : 1.f, sy = (o & 2) ? -1.f : 1.f, sz = (o & 1) ? -1.f : 1.f;
-  const float m = __ldg(mu + n * G + g);
+  in.o = o;
+  in.cx = __ldg(c + 3 * od);
+  in.cy = __ldg(c + 3 * od + 1);
+  in.cz = __ldg(c + 3 * od + 2);
+  in.m = __ldg(mu + n * G + g);
   const int64_t Q = 4 * (int64_t)G;
   float* base = store + v * view_stride + od * N * Q + 4 * g;
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 s = load4<kCoherent>(base + n * Q);
-  const float4 X = ux < N ? load4<kCoherent>(base + ux * Q) : zero;  // (psi0, psi_x, psi_y, psi_z) of the x neighbour
-  const float4 Y = uy < N ? load4<kCoherent>(base + uy * Q) : zero;
-  const float4 Z = uz < N ? load4<kCoherent>(base + uz * Q) : zero;
+  in.dst = base + n * Q;
+  in.s = load4<kCoherent>(in.dst);
+  in.X = ux < N ? load4<kCoherent>(base + ux * Q) : zero;
+  in.Y = uy < N ? load4<kCoherent>(base + uy * Q) : zero;
+  in.Z = uz < N ? load4<kCoherent>(base + uz * Q) : zero;
+}
+
+// The closed-form cell solve of one lane and its store over the source.
+__device__ __forceinline__ void finish_lane(const LaneIn& in) {
+  const float sx = (in.o & 4) ? -1.f : 1.f, sy = (in.o & 2) ? -1.f : 1.f, sz = (in.o & 1) ? -1.f : 1.f;
+  const float cx = in.cx, cy = in.cy, cz = in.cz, m = in.m;
+  const float4 s = in.s, X = in.X, Y = in.Y, Z = in.Z;
   // face-averaged inflow psibar_a = psi_0[N_a] + s_a psi_a[N_a]
   const float pbx = X.x + sx * X.y;
   const float pby = Y.x + sy * Y.z;
@@ -70,7 +87,19 @@ __device__ __forceinline__ void solve_lane(int64_t lane, float* __restrict__ sto
   out.y = (rx + 3.f * sx * cx * p0) / dx;
   out.z = (ry + 3.f * sy * cy * p0) / dy;
   out.w = (rz + 3.f * sz * cz * p0) / dz;
-  *reinterpret_cast<float4*>(base + n * Q) = out;
+  *reinterpret_cast<float4*>(in.dst) = out;
+}
+
+template <int kG, bool kCoherent>
+__device__ __forceinline__ void solve_lane(int64_t lane, float* __restrict__ store, const float* __restrict__ mu,
+                                           const float* __restrict__ c, const int* __restrict__ octant,
+                                           const int* __restrict__ cell, const int* __restrict__ upstream,
+                                           int64_t start, int64_t E, int64_t N, int G_runtime, int64_t Dc,
+                                           int64_t view_stride) {
+  LaneIn in;
+  gather_lane<kG, kCoherent>(lane, in, store, mu, c, octant, cell, upstream, start, E, N, G_runtime, Dc,
+                             view_stride);
+  finish_lane(in);
 }
 
 template <int kG>
@@ -85,7 +114,10 @@ __global__ void __launch_bounds__(kThreads) plane_kernel(float* __restrict__ sto
   solve_lane<kG, false>(lane, store, mu, c, octant, cell, upstream, start, E, N, G, Dc, view_stride);
 }
 
-template <int kG>
+// All planes in one cooperative launch. A thread takes kU lanes of a plane at a time (stride apart, so every warp
+// still reads whole cells): all their loads are issued before the first solve and store, which a plain loop cannot
+// do (the stores might alias the next lane's loads as far as the compiler knows; within a plane they never do).
+template <int kG, int kU>
 __global__ void __launch_bounds__(kThreads) persistent_kernel(
     float* __restrict__ store, const float* __restrict__ mu, const float* __restrict__ c,
     const int* __restrict__ octant, const int* __restrict__ cell, const int* __restrict__ upstream,
@@ -97,8 +129,17 @@ __global__ void __launch_bounds__(kThreads) persistent_kernel(
     const int64_t start = __ldg(offsets + p);
     const int64_t E = __ldg(offsets + p + 1) - start;
     const int64_t total = E * per_entry;
-    for (int64_t lane = (int64_t)blockIdx.x * kThreads + threadIdx.x; lane < total; lane += stride)
-      solve_lane<kG, true>(lane, store, mu, c, octant, cell, upstream, start, E, N, G, Dc, view_stride);
+    for (int64_t lane0 = (int64_t)blockIdx.x * kThreads + threadIdx.x; lane0 < total; lane0 += stride * kU) {
+      LaneIn in[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+        if (lane0 + u * stride < total)
+          gather_lane<kG, true>(lane0 + u * stride, in[u], store, mu, c, octant, cell, upstream, start, E, N, G, Dc,
+                                view_stride);
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+        if (lane0 + u * stride < total) finish_lane(in[u]);
+    }
     if (p + 1 < num_planes && !grid_barrier(sync, gridDim.x, timeout_ns, skip)) return;
   }
 }
@@ -119,13 +160,13 @@ int launch_planes(float* store, const float* mu, const float* c, const int* octa
   return launch_status("citrus_sweep_planes");
 }
 
-template <int kG>
-int launch_persistent(float* store, const float* mu, const float* c, const int* octant, const int* cell,
-                      const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
-                      int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
-                      cudaStream_t stream) {
+template <int kG, int kU>
+int launch_persistent_u(float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                        const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
+                        int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
+                        cudaStream_t stream) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG>, kThreads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG, kU>, kThreads, 0);
   if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: occupancy query failed");
   int64_t blocks = (int64_t)per_sm * num_sms();
   if (max_blocks > 0 && max_blocks < blocks) blocks = max_blocks;
@@ -135,11 +176,29 @@ int launch_persistent(float* store, const float* mu, const float* c, const int* 
   if (z != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: %s", cudaGetErrorString(z));
   void* args[] = {&store, &mu, &c, &octant, &cell, &upstream, &offsets, &num_planes, &N, &G, &Dc, &views,
                   &view_stride, &sync, &timeout_ns, &skip};
-  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG>, dim3((unsigned)blocks), dim3(kThreads), args, 0,
-                                  stream);
+  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG, kU>, dim3((unsigned)blocks), dim3(kThreads), args,
+                                  0, stream);
   if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_persistent: %s", cudaGetErrorString(e));
   note_launches();
   return CITRUS_OK;
+}
+
+constexpr int kDefaultUnroll = 2;
+
+template <int kG>
+int launch_persistent(float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                      const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
+                      int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
+                      cudaStream_t stream, int unroll = kDefaultUnroll) {
+  switch (unroll) {
+    case 1: return launch_persistent_u<kG, 1>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                              views, sync, max_blocks, timeout_ns, skip, stream);
+    case 2: return launch_persistent_u<kG, 2>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                              views, sync, max_blocks, timeout_ns, skip, stream);
+    case 4: return launch_persistent_u<kG, 4>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                              views, sync, max_blocks, timeout_ns, skip, stream);
+    default: return set_error(CITRUS_EINVAL, "citrus_sweep_persistent: lanes per thread %d (1, 2 or 4)", unroll);
+  }
 }
 
 int check_sweep_args(const float* store, const float* mu, const float* c, const int* octant, const int* cell,
@@ -185,11 +244,12 @@ extern "C" int citrus_sweep_planes(float* store, const float* mu_cells, const fl
   }
 }
 
-extern "C" int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c, const int32_t* octant,
-                                       const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_dev,
-                                       int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
-                                       int64_t views, uint32_t* sync, int64_t max_blocks, int64_t timeout_ns,
-                                       int64_t skip_block, void* stream) {
+extern "C" int citrus_sweep_persistent_config(float* store, const float* mu_cells, const float* c,
+                                              const int32_t* octant, const int32_t* cell, const int32_t* upstream,
+                                              const int32_t* plane_offsets_dev, int64_t num_planes, int64_t num_cells,
+                                              int64_t num_groups, int64_t dc, int64_t views, uint32_t* sync,
+                                              int64_t max_blocks, int32_t lanes_per_thread, int64_t timeout_ns,
+                                              int64_t skip_block, void* stream) {
   int status = check_sweep_args(store, mu_cells, c, octant, cell, upstream, num_planes, num_cells, num_groups, dc,
                                 views);
   if (status) return status;
@@ -198,22 +258,33 @@ extern "C" int citrus_sweep_persistent(float* store, const float* mu_cells, cons
   CITRUS_REQUIRE(timeout_ns > 0, "citrus_sweep_persistent: timeout_ns must be positive");
   const int G = (int)num_groups, P = (int)num_planes, skip = skip_block < 0 ? -1 : (int)skip_block;
   const uint64_t t = (uint64_t)timeout_ns;
+  const int u = lanes_per_thread <= 0 ? kDefaultUnroll : lanes_per_thread;
   unsigned* sy = reinterpret_cast<unsigned*>(sync);
   cudaStream_t s = as_stream(stream);
   switch (G) {
     case 1: return launch_persistent<1>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
-                                        G, dc, views, sy, max_blocks, t, skip, s);
+                                        G, dc, views, sy, max_blocks, t, skip, s, u);
     case 2: return launch_persistent<2>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
-                                        G, dc, views, sy, max_blocks, t, skip, s);
+                                        G, dc, views, sy, max_blocks, t, skip, s, u);
     case 4: return launch_persistent<4>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
-                                        G, dc, views, sy, max_blocks, t, skip, s);
+                                        G, dc, views, sy, max_blocks, t, skip, s, u);
     case 8: return launch_persistent<8>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
-                                        G, dc, views, sy, max_blocks, t, skip, s);
+                                        G, dc, views, sy, max_blocks, t, skip, s, u);
     case 16: return launch_persistent<16>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P,
-                                          num_cells, G, dc, views, sy, max_blocks, t, skip, s);
+                                          num_cells, G, dc, views, sy, max_blocks, t, skip, s, u);
     default: return launch_persistent<0>(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, P, num_cells,
-                                         G, dc, views, sy, max_blocks, t, skip, s);
+                                         G, dc, views, sy, max_blocks, t, skip, s, u);
   }
+}
+
+extern "C" int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c, const int32_t* octant,
+                                       const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_dev,
+                                       int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
+                                       int64_t views, uint32_t* sync, int64_t max_blocks, int64_t timeout_ns,
+                                       int64_t skip_block, void* stream) {
+  return citrus_sweep_persistent_config(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, num_planes,
+                                        num_cells, num_groups, dc, views, sync, max_blocks, 0, timeout_ns, skip_block,
+                                        stream);
 }
 
 // ---- allocation-free persistent sweep ----------------------------------------------------------------------------

@@ -73,7 +73,8 @@ class FlatPlaneIndex:
 
 def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tensor, *, method: str = "persistent",
                  sync: Optional[Tensor] = None, max_blocks: int = 0,
-                 timeout_ns: int = DEFAULT_BARRIER_TIMEOUT_NS, skip_block: int = -1) -> Optional[Tensor]:
+                 timeout_ns: int = DEFAULT_BARRIER_TIMEOUT_NS, skip_block: int = -1,
+                 lanes_per_thread: int = 0) -> Optional[Tensor]:
     """Sweep one direction chunk in place (reference ``sweep_kernels.py:265-290``).
 
     Args:
@@ -87,6 +88,7 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
         max_blocks: cap on the persistent grid (0: as many blocks as fit).
         timeout_ns: bound of every barrier wait of the persistent launch.
         skip_block: test hook forcing a barrier timeout (-1 in normal use).
+        lanes_per_thread: lanes a thread of the persistent launch loads before it solves them (1, 2 or 4; 0: 2).
 
     Returns:
         The sync words of the persistent launch (``sync[2] != 0`` means a barrier wait ran out), or None.
@@ -119,9 +121,10 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
         raise ValueError(f"method must be 'persistent' or 'planes', got {method!r}")
     if sync is None:
         sync = torch.empty(4, dtype=torch.int32, device=store.device)
-    _lib.call("citrus_sweep_persistent", store.data_ptr(), mu_cells.data_ptr(), c.data_ptr(), index.octant.data_ptr(),
-              index.cell.data_ptr(), index.upstream.data_ptr(), index.offsets_device.data_ptr(), index.num_planes, N,
-              G, Dc, views, sync.data_ptr(), int(max_blocks), int(timeout_ns), int(skip_block), stream)
+    _lib.call("citrus_sweep_persistent_config", store.data_ptr(), mu_cells.data_ptr(), c.data_ptr(),
+              index.octant.data_ptr(), index.cell.data_ptr(), index.upstream.data_ptr(), index.offsets_device.data_ptr(),
+              index.num_planes, N, G, Dc, views, sync.data_ptr(), int(max_blocks), int(lanes_per_thread),
+              int(timeout_ns), int(skip_block), stream)
     return sync
 
 
@@ -161,8 +164,11 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, prec
     sb, sc = (B.stride(0), C.stride(0)) if batch > 1 else (0, 0)
     stream = _lib.stream_handle(A.device)
     if precision == "fp32":
-        _lib.call("citrus_small_k_gemm", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
-                  C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), stream)
+        from .autotune import small_k_gemm_config
+
+        variant, tile = small_k_gemm_config(A, B, C, M, K, J, batch, sb, sc, accumulate)
+        _lib.call("citrus_small_k_gemm_config", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
+                  C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), int(variant), int(tile), stream)
         return C
     # the tensor-core product takes at most 128 rows and 128 inner terms per call; inner dimensions above 64 go in
     # steps of 64 (partial sums added), which keeps the split operands of a CTA small enough for three per SM

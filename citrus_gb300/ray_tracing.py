@@ -19,6 +19,22 @@ from torch import Tensor
 from . import _lib
 from .geometry import ConeGeometry, Grid
 
+_PIXELS: dict = {}   # (geometry, angle, device) -> float64 [Rd Cd, 3] pixel centres on the device
+_PIXELS_MAX = 512
+
+
+def _pixel_centers(geometry: ConeGeometry, angle: float, device) -> Tensor:
+    """The panel's pixel centres at ``angle`` on ``device``, uploaded once per (geometry, angle) and kept (so that a
+    captured CUDA graph reads a buffer that stays put)."""
+    key = (geometry, float(angle), str(torch.device(device)))
+    t = _PIXELS.get(key)
+    if t is None:
+        if len(_PIXELS) >= _PIXELS_MAX:
+            _PIXELS.pop(next(iter(_PIXELS)))
+        t = _lib.upload(geometry.pixel_centers_np(angle).reshape(-1, 3), device, torch.float64)
+        _PIXELS[key] = t
+    return t
+
 
 class Projectors(Protocol):
     """The five ray operations of the scatter solver (reference ``ray_tracing.py:27-115``)."""
@@ -216,7 +232,7 @@ class GB300Projectors:
         else:
             raise ValueError(f"field must be [C, ...] or [K={K}, C, ...], got {tuple(field.shape)}")
         Rd, Cd = geometry.image_shape
-        pixels = _lib.upload(geometry.pixel_centers_np(angle).reshape(-1, 3), device, torch.float64)
+        pixels = _pixel_centers(geometry, angle, device)
         if out is None:
             out = torch.empty(K, C, Rd, Cd, device=device, dtype=torch.float32)
         if tuple(out.shape) != (K, C, Rd, Cd):

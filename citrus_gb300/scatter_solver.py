@@ -121,7 +121,7 @@ class ScatterSolver:
 
     def __init__(self, library: MultigroupLibrary, config: SolverConfig, geometry: ConeGeometry, projectors=None,
                  detector: Optional[DetectorResponse] = None, grid_response: Optional[GridResponse] = None,
-                 source: Optional[SourceModel] = None, device="cuda", direction_context_cache_size: int = 8):
+                 source: Optional[SourceModel] = None, device="cuda", direction_context_cache_size: int = 128):
         if detector is None or grid_response is None:
             raise TypeError("ScatterSolver needs a detector and a grid_response")
         config.validate()

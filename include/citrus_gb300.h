@@ -64,6 +64,14 @@ int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c,
                             int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc, int64_t views,
                             uint32_t* sync, int64_t max_blocks, int64_t timeout_ns, int64_t skip_block, void* stream);
 
+/* citrus_sweep_persistent with the lanes a thread takes at a time chosen by the caller (the autotuner):
+ * lanes_per_thread 1, 2 or 4 (0: 2); a thread issues the loads of all its lanes before their solves. */
+int citrus_sweep_persistent_config(float* store, const float* mu_cells, const float* c, const int32_t* octant,
+                                   const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_dev,
+                                   int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
+                                   int64_t views, uint32_t* sync, int64_t max_blocks, int32_t lanes_per_thread,
+                                   int64_t timeout_ns, int64_t skip_block, void* stream);
+
 /* The persistent sweep without any allocation: no counterpart in the reference, which always runs the sweep through
  * torch's allocator. The barrier words and the plane offsets live in a static device array of this library (33 KB
  * per device, at most 8191 planes, i.e. R + C + S - 2 <= 8191; more planes return CITRUS_EINVAL). The call clears
@@ -89,6 +97,13 @@ int citrus_sweep_persistent_static(float* store, const float* mu_cells, const fl
 int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t M,
                         int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, int32_t accumulate,
                         void* stream);
+
+/* The same product with its kernel chosen by the caller (the autotuner): variant 0 = the shape rule of
+ * citrus_small_k_gemm, 1 = the streaming forms (columns of B in registers for K <= 64, rows of C in registers for
+ * M <= 64), 2 = the shared-memory tiled kernel with tile_rows groups of 8 rows per CTA (1-6, 8, 12, 16; 0 = fit M). */
+int citrus_small_k_gemm_config(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                               int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
+                               int32_t accumulate, int32_t variant, int32_t tile_rows, void* stream);
 
 /* The same product on the tcgen05 tensor cores, M <= 128 and K <= 128: each float32 operand is split into a bfloat16
  * high part and a bfloat16 low part (x - hi), the product accumulated in float32 as A_hi B_hi + A_hi B_lo + A_lo B_hi

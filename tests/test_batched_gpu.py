@@ -6,7 +6,7 @@ import pytest
 import torch
 
 from conftest import rel_err
-from citrus_gb300.batched import batched_view_steps
+from citrus_gb300.batched import GraphedOuterIteration, batched_view_steps
 from citrus_gb300.citrus_step import CitrusState, citrus_view_step
 from citrus_gb300.geometry import Grid
 from test_citrus_step_gpu import _solver
@@ -32,3 +32,25 @@ def test_batched_steps_equal_per_view_steps(cuda_device, name):
             assert rel_err(signals[v], ref[v]) < 1e-6
             assert rel_err(batched[v].collided_moments, single[v].collided_moments) < 1e-6
             assert abs(batched[v].history[-1] - single[v].history[-1]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
+def test_graphed_outer_iterations_equal_batched_steps(cuda_device, name):
+    """The outer iteration recorded into a CUDA graph (accumulators updated in place) gives the eager batched steps'
+    results on every replay, including after the densities change."""
+    g, solver = _solver(name, cuda_device)
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device)
+    angles = [0.3, 1.7, 4.0]
+    graphed = GraphedOuterIteration(solver, grid, angles, batch=2)
+    eager = [CitrusState() for _ in angles]
+    for step in range(5):
+        rho_step = rho * (1.0 + 0.05 * step)          # the densities move between outer iterations
+        signals, states = graphed.step(rho_step)
+        fields = solver.material_fields(rho_step, grid)
+        ref, _, eager = batched_view_steps(solver, eager, fields, angles, batch=2)
+        for v in range(len(angles)):
+            assert rel_err(signals[v], ref[v]) < 1e-6, (step, v)
+            assert rel_err(states[v].collided_moments, eager[v].collided_moments) < 1e-6, (step, v)
+            assert abs(states[v].history[-1] - eager[v].history[-1]) < 1e-6
+    assert graphed.replays == 3

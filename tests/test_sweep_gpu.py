@@ -75,9 +75,11 @@ def test_batched_views_sweep_matches_single_views(cuda_device):
     single = stores.clone()
     for v in range(V):
         kernels.sweep_planes(ctx.flat_index, single[v], mu, c, method="planes")
-    batched = stores.clone()
-    kernels.sweep_planes(ctx.flat_index, batched, mu, c, method="persistent")
-    assert torch.equal(single, batched)
+    for lanes in (1, 2, 4):   # every lanes-per-thread form the autotuner chooses between
+        batched = stores.clone()
+        sync = kernels.sweep_planes(ctx.flat_index, batched, mu, c, method="persistent", lanes_per_thread=lanes)
+        assert torch.equal(single, batched), lanes
+        assert int(sync[2]) == 0
 
 
 def test_persistent_barrier_timeout_is_reported(cuda_device):
@@ -176,3 +178,39 @@ def test_source_iteration_matches_oracle(cuda_device):
     expected = osweep.scatter_source(real_spherical_harmonics(L, ctx.quadrature.omega),
                                      osweep.scatter_moments(transfer, result.phi_total.double().cpu().numpy()))
     assert rel_err(got, expected) < 1e-5
+
+
+@pytest.mark.parametrize("M,K,acc", [(120, 36, True), (36, 120, False), (64, 36, False), (20, 36, True)])
+def test_every_small_k_gemm_variant_matches(cuda_device, tmp_path, M, K, acc):
+    """Each kernel the autotuner chooses between gives the product (float64 reference), and the tuned call too."""
+    from citrus_gb300 import _lib
+    from citrus_gb300.autotune import GEMM_CANDIDATES, Autotuner
+    import citrus_gb300.autotune as autotune
+
+    gen = torch.Generator().manual_seed(M + K)
+    batch, J = 2, 4096 + 8
+    A = torch.randn(M, K, generator=gen).to(cuda_device)
+    B = torch.randn(batch, K, J, generator=gen).to(cuda_device)
+    C0 = torch.randn(batch, M, J, generator=gen).to(cuda_device)
+    ref = torch.einsum("mk,bkj->bmj", A.double(), B.double()) + (C0.double() if acc else 0)
+    stream = _lib.stream_handle(cuda_device)
+    ran = 0
+    for variant, tile in GEMM_CANDIDATES:
+        C = C0.clone()
+        try:
+            _lib.call("citrus_small_k_gemm_config", A.data_ptr(), K, B.data_ptr(), J, C.data_ptr(), J, M, K, J,
+                      batch, K * J, M * J, int(acc), variant, tile, stream)
+        except _lib.CitrusKernelError:
+            continue        # a tile the shape does not admit (shared memory)
+        ran += 1
+        assert float((C.double() - ref).abs().max() / ref.abs().max()) < 1e-5, (variant, tile)
+    assert ran >= 3
+    saved = autotune._TUNER
+    autotune._TUNER = Autotuner(path=tmp_path / "tuning.json", enabled=True)
+    try:
+        C = C0.clone()
+        kernels.small_k_gemm(A, B, C, accumulate=acc)
+        assert float((C.double() - ref).abs().max() / ref.abs().max()) < 1e-5
+        assert len(autotune._TUNER.table) == 1
+    finally:
+        autotune._TUNER = saved
