@@ -56,6 +56,8 @@ SIGNATURES = {
     "citrus_weighted_direction_sum": [P, I64, I64, I64, I64, I64, I64, I64, I64, P, I64, I64, P, I32, P],
     "citrus_conv3d_forward": [P, I64, P, I64, I32, P, P, P, I64, I64, I64, I64, I64, I32, I32, P],
     "citrus_conv3d_backward_input": [P, I64, P, P, I64, P, P, I64, I64, I64, I64, I64, I32, P],
+    "citrus_conv3d_forward_config": [P, I64, P, I64, I32, P, P, P, I64, I64, I64, I64, I64, I32, I32, I32, P, P],
+    "citrus_conv3d_backward_input_config": [P, I64, P, P, I64, P, P, I64, I64, I64, I64, I64, I32, I32, P, P],
     "citrus_conv3d_weight_grad_splits": [I64, I64, I64, I64, I64, I64, I64, I32],
     "citrus_conv3d_backward_weight": [P, I64, P, I64, P, I64, I32, P, P, I64, I64, I64, I64, I32, P, I64, P],
     "citrus_avg_pool2": [P, P, I64, I64, I64, I64, P],

@@ -16,7 +16,9 @@
 //   * pooling (2x average), the upsampling's backward pass, MSE and Adam.
 #include <cuda_bf16.h>
 
-#include "common.cuh"
+#include <algorithm>
+
+#include "tcgen05.cuh"
 
 namespace citrus {
 namespace {
@@ -129,6 +131,236 @@ __global__ void __launch_bounds__(kConvThreads) conv_kernel(const ConvArgs a) {
       a.out_b[((int64_t)b * a.ob + (o - a.oa)) * V + vox] = r;
     }
   }
+}
+
+// The same convolution as an implicit GEMM on the tcgen05 tensor cores: D[voxel, o] = sum_k A[voxel, k] B[o, k] with
+// k = (input channel, tap). A CTA takes a tile of 128 consecutive voxels (the MMA's M) x n_tile output channels (its
+// N, a multiple of 16 up to 256) and walks k in chunks of 64 through two shared-memory stages:
+//   * every thread gathers its voxel's 64 inputs of the chunk (the concatenation and the upsampling read in place,
+//     zero padding outside the volume), splits each float32 value into bfloat16 high and low parts and writes them in
+//     the K-major canonical layout (8-row x 16-byte core matrices, no swizzle);
+//   * the chunk's weights, already bfloat16, fill the B operand as they are;
+//   * one thread issues 2 x 4 MMAs (M = 128, N = n_tile, K = 16, kind::f16: A_hi B + A_lo B, exact weights, so the
+//     product keeps about sixteen bits of every input) into a float32 accumulator in tensor memory and commits them
+//     to the stage's mbarrier, while the threads build the other stage;
+//   * every wait on an mbarrier is bounded by a wall-clock limit (the CTA records the error and leaves).
+// The epilogue reads the accumulator (lane = voxel, column = output channel) and stores 32 consecutive voxels of one
+// channel per warp instruction, with the bias, the ReLU and the mask applied.
+constexpr int kCvThreads = 128;
+constexpr int kCvKC = 64;                     // inner dimension of one stage (four MMA K-steps)
+constexpr uint32_t kCvAStep = kTcM * 16 * 2;  // bytes of one K-step of A: 128 rows x 16 bfloat16
+
+inline uint32_t tc_columns(int n_tile) {
+  uint32_t c = 32;
+  while (c < (uint32_t)n_tile) c <<= 1;
+  return c;
+}
+
+inline size_t tc_stage_bytes(int n_tile) { return 2 * 4 * (size_t)kCvAStep + 4 * (size_t)n_tile * 32; }
+
+template <int kK>
+__global__ void __launch_bounds__(kCvThreads) conv_tc_kernel(const ConvArgs a, int n_tile, int co_tiles,
+                                                            int vox_tiles, int64_t num_tiles,
+                                                            uint32_t* __restrict__ error_word) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr int K3 = kK * kK * kK;
+  constexpr int kH = kK / 2;
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid / 32;
+  const int O = a.oa + a.ob, Ci = a.ca + a.cb;
+  const int Ktot = Ci * K3;
+  const int nchunks = (Ktot + kCvKC - 1) / kCvKC;
+  const int64_t V = (int64_t)a.D * a.H * a.W;
+  const int Dc = a.D >> 1, Hc = a.H >> 1, Wc = a.W >> 1;
+  const uint32_t a_bytes = 4 * kCvAStep;
+  const uint32_t b_step = (uint32_t)n_tile * 32;
+  const uint32_t stage_bytes = 2 * a_bytes + 4 * b_step;
+  const uint32_t cols = n_tile <= 32 ? 32u : n_tile <= 64 ? 64u : n_tile <= 128 ? 128u : 256u;
+  const uint32_t idesc = idesc_bf16(n_tile);
+
+  if (tid == 0) {
+    abort_flag = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  uint32_t phase0 = 0, phase1 = 0;
+  bool pending0 = false, pending1 = false;
+  bool failed = false;
+
+  for (int64_t tile = blockIdx.x; tile < num_tiles && !failed; tile += gridDim.x) {
+    const int vt = (int)(tile % vox_tiles);
+    const int64_t rest = tile / vox_tiles;
+    const int ct = (int)(rest % co_tiles);
+    const int b = (int)(rest / co_tiles);
+    const int co0 = ct * n_tile;
+    const int64_t vox = (int64_t)vt * kTcM + tid;
+    const bool vvalid = vox < V;
+    const int x = vvalid ? (int)(vox % a.W) : 0;
+    const int y = vvalid ? (int)((vox / a.W) % a.H) : 0;
+    const int z = vvalid ? (int)(vox / ((int64_t)a.W * a.H)) : 0;
+    for (int c = 0; c < nchunks; ++c) {
+      const int st = c & 1;
+      uint8_t* sa_hi = smem + st * stage_bytes;
+      uint8_t* sa_lo = sa_hi + a_bytes;
+      uint8_t* sb = sa_lo + a_bytes;
+      // the stage's previous MMAs must be done before its operands are overwritten
+      if (st == 0 ? pending0 : pending1) {
+        const bool ok = mbar_wait(smem_u32(&mbar[st]), st == 0 ? phase0 : phase1, global_timer_ns());
+        if (st == 0) { phase0 ^= 1u; pending0 = false; } else { phase1 ^= 1u; pending1 = false; }
+        if (!ok) abort_flag = 1;
+      }
+      // A: this thread's voxel row, the chunk's 64 inputs, split into bfloat16 high and low parts
+      int k = c * kCvKC;
+      int ci = k / K3, tap = k - ci * K3;
+#pragma unroll 1
+      for (int kk8 = 0; kk8 < kCvKC; kk8 += 8) {
+        float xv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          float v = 0.f;
+          if (vvalid && ci < Ci) {
+            const int gz = z + tap / (kK * kK) - kH, gy = y + (tap / kK) % kK - kH, gx = x + tap % kK - kH;
+            if (gz >= 0 && gz < a.D && gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+              if (ci < a.ca)
+                v = __ldg(a.in_a + ((int64_t)b * a.ca + ci) * V + ((int64_t)gz * a.H + gy) * a.W + gx);
+              else if (a.b_up)
+                v = __ldg(a.in_b + (((int64_t)b * a.cb + (ci - a.ca)) * Dc + (gz >> 1)) * Hc * Wc +
+                          (int64_t)(gy >> 1) * Wc + (gx >> 1));
+              else
+                v = __ldg(a.in_b + ((int64_t)b * a.cb + (ci - a.ca)) * V + ((int64_t)gz * a.H + gy) * a.W + gx);
+            }
+          }
+          xv[q] = v;
+          if (++tap == K3) {
+            tap = 0;
+            ++ci;
+          }
+        }
+        uint4 hi, lo;
+        split_pair(xv[0], xv[1], hi.x, lo.x);
+        split_pair(xv[2], xv[3], hi.y, lo.y);
+        split_pair(xv[4], xv[5], hi.z, lo.z);
+        split_pair(xv[6], xv[7], hi.w, lo.w);
+        const uint32_t off = (uint32_t)(kk8 >> 4) * kCvAStep + core_offset(tid, kk8 & 15);
+        *reinterpret_cast<uint4*>(sa_hi + off) = hi;
+        *reinterpret_cast<uint4*>(sa_lo + off) = lo;
+      }
+      // B: n_tile output channels x the chunk's 64 weights, 8 at a time
+      for (int u = tid; u < n_tile * 8; u += kCvThreads) {
+        const int row = u >> 3, g8 = u & 7;
+        const int o = co0 + row;
+        uint32_t w2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint32_t pair = 0;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int kq = c * kCvKC + g8 * 8 + 2 * q + h;
+            uint32_t bits = 0;
+            if (o < O && kq < Ktot) {
+              const int i = kq / K3, t = kq - (kq / K3) * K3;
+              bits = a.w[a.w_base + o * a.w_o + i * a.w_i + t * a.w_t];
+            }
+            pair |= bits << (16 * h);
+          }
+          w2[q] = pair;
+        }
+        const uint32_t off = (uint32_t)(g8 >> 1) * b_step + core_offset(row, (g8 & 1) * 8);
+        *reinterpret_cast<uint4*>(sb + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (abort_flag) {
+        failed = true;
+        break;
+      }
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const uint64_t ah = smem_desc(smem_u32(sa_hi + s * kCvAStep), 128, 256);
+          const uint64_t al = smem_desc(smem_u32(sa_lo + s * kCvAStep), 128, 256);
+          const uint64_t bd = smem_desc(smem_u32(sb + s * b_step), 128, 256);
+          mma_bf16(tmem, ah, bd, idesc, (c > 0 || s > 0) ? 1u : 0u);
+          mma_bf16(tmem, al, bd, idesc, 1u);
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&mbar[st]))
+                     : "memory");
+      }
+      if (st == 0) pending0 = true; else pending1 = true;
+    }
+    // every MMA of the tile done (both stages drained)
+    if (pending0) {
+      if (!mbar_wait(smem_u32(&mbar[0]), phase0, global_timer_ns())) abort_flag = 1;
+      phase0 ^= 1u;
+      pending0 = false;
+    }
+    if (pending1) {
+      if (!mbar_wait(smem_u32(&mbar[1]), phase1, global_timer_ns())) abort_flag = 1;
+      phase1 ^= 1u;
+      pending1 = false;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (abort_flag || failed) {
+      failed = true;
+      break;
+    }
+    // epilogue: accumulator lane tid = this thread's voxel, columns = output channels co0 ..
+#pragma unroll 1
+    for (int j0 = 0; j0 < n_tile; j0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)j0)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (vvalid) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int o = co0 + j0 + q;
+          if (o < O) {
+            float val = __uint_as_float(r[q]) + (a.bias != nullptr ? a.bias[o] : 0.f);
+            if (a.relu) val = fmaxf(val, 0.f);
+            if (o < a.oa) {
+              const int64_t idx = ((int64_t)b * a.oa + o) * V + vox;
+              if (a.mask_a != nullptr && !(a.mask_a[idx] > 0.f)) val = 0.f;
+              a.out_a[idx] = val;
+            } else {
+              a.out_b[((int64_t)b * a.ob + (o - a.oa)) * V + vox] = val;
+            }
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // the accumulator is free for the next tile
+  }
+  if (failed && tid == 0 && error_word != nullptr) atomicExch(error_word, 1u);
+  // leave only after the tensor cores are done with this CTA's shared memory and tensor memory
+  if (pending0) mbar_wait(smem_u32(&mbar[0]), phase0, global_timer_ns());
+  if (pending1) mbar_wait(smem_u32(&mbar[1]), phase1, global_timer_ns());
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(cols) : "memory");
 }
 
 // grad_w[o, i, t] partial sums over the bricks s, s + S, s + 2S, ... of (batch x voxel bricks):
@@ -345,7 +577,35 @@ int check_volume(int64_t batch, int64_t depth, int64_t height, int64_t width, co
   return CITRUS_OK;
 }
 
-int launch_conv(const ConvArgs& a, int kernel_size, cudaStream_t s) {
+template <int kK>
+int launch_conv_tc_k(const ConvArgs& a, uint32_t* error_word, cudaStream_t s) {
+  const int O = a.oa + a.ob;
+  const int co_tiles = (int)cdiv(O, 256);
+  const int n_tile = (int)(cdiv(cdiv(O, co_tiles), 16) * 16);
+  const int64_t V = (int64_t)a.D * a.H * a.W;
+  const int64_t vox_tiles = cdiv(V, kTcM);
+  CITRUS_REQUIRE(vox_tiles < (1ll << 30), "conv3d: too many voxel tiles");
+  const int64_t num_tiles = vox_tiles * co_tiles * a.B;
+  const size_t smem = 2 * tc_stage_bytes(n_tile);
+  cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<kK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "conv3d (tensor cores): %s", cudaGetErrorString(e));
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_tc_kernel<kK>, kCvThreads, smem);
+  if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "conv3d (tensor cores): occupancy query failed");
+  const int by_tmem = (int)(512 / tc_columns(n_tile));  // tensor-memory columns of the SM
+  if (per_sm > by_tmem) per_sm = by_tmem;
+  const int64_t grid = std::min<int64_t>(num_tiles, (int64_t)per_sm * num_sms());
+  conv_tc_kernel<kK><<<(unsigned)grid, kCvThreads, smem, s>>>(a, n_tile, co_tiles, (int)vox_tiles, num_tiles,
+                                                               error_word);
+  note_launches();
+  return CITRUS_OK;
+}
+
+// variant 1: the FP32 SIMT kernel; variant 2 (and 0): the tcgen05 implicit GEMM
+int launch_conv(const ConvArgs& a, int kernel_size, int variant, uint32_t* error_word, cudaStream_t s) {
+  if (variant != 1) {
+    return kernel_size == 3 ? launch_conv_tc_k<3>(a, error_word, s) : launch_conv_tc_k<1>(a, error_word, s);
+  }
   const int64_t tiles = cdiv(a.W, kTX) * cdiv(a.H, kTY) * cdiv(a.D, kTZ);
   CITRUS_REQUIRE(tiles < (1ll << 31), "conv3d: too many voxel bricks");
   dim3 grid((unsigned)tiles, (unsigned)cdiv(a.oa + a.ob, kCoT), (unsigned)a.B);
@@ -360,10 +620,11 @@ int launch_conv(const ConvArgs& a, int kernel_size, cudaStream_t s) {
 
 using namespace citrus;
 
-extern "C" int citrus_conv3d_forward(const float* in_a, int64_t channels_a, const float* in_b, int64_t channels_b,
-                                     int32_t b_upsampled, const uint16_t* weight, const float* bias, float* out,
-                                     int64_t channels_out, int64_t batch, int64_t depth, int64_t height,
-                                     int64_t width, int32_t kernel_size, int32_t relu, void* stream) {
+extern "C" int citrus_conv3d_forward_config(const float* in_a, int64_t channels_a, const float* in_b,
+                                            int64_t channels_b, int32_t b_upsampled, const uint16_t* weight,
+                                            const float* bias, float* out, int64_t channels_out, int64_t batch,
+                                            int64_t depth, int64_t height, int64_t width, int32_t kernel_size,
+                                            int32_t relu, int32_t variant, uint32_t* error_word, void* stream) {
   int st = check_volume(batch, depth, height, width, "citrus_conv3d_forward");
   if (st) return st;
   CITRUS_REQUIRE(in_a && weight && out, "citrus_conv3d_forward: null pointer argument");
@@ -379,15 +640,28 @@ extern "C" int citrus_conv3d_forward(const float* in_a, int64_t channels_a, cons
              weight, (channels_a + channels_b) * k3, k3, 1, 0,
              bias, out, nullptr, (int)channels_out, 0, nullptr, relu ? 1 : 0,
              (int)batch, (int)depth, (int)height, (int)width};
-  st = launch_conv(a, kernel_size, as_stream(stream));
+  CITRUS_REQUIRE(variant >= 0 && variant <= 2, "citrus_conv3d_forward: variant %d (0 auto, 1 SIMT, 2 tensor cores)",
+                 variant);
+  st = launch_conv(a, kernel_size, variant, error_word, as_stream(stream));
   if (st) return st;
   return launch_status("citrus_conv3d_forward");
 }
 
-extern "C" int citrus_conv3d_backward_input(const float* grad_out, int64_t channels_out, const uint16_t* weight,
-                                            float* grad_a, int64_t channels_a, const float* mask_a, float* grad_b,
-                                            int64_t channels_b, int64_t batch, int64_t depth, int64_t height,
-                                            int64_t width, int32_t kernel_size, void* stream) {
+extern "C" int citrus_conv3d_forward(const float* in_a, int64_t channels_a, const float* in_b, int64_t channels_b,
+                                     int32_t b_upsampled, const uint16_t* weight, const float* bias, float* out,
+                                     int64_t channels_out, int64_t batch, int64_t depth, int64_t height,
+                                     int64_t width, int32_t kernel_size, int32_t relu, void* stream) {
+  return citrus_conv3d_forward_config(in_a, channels_a, in_b, channels_b, b_upsampled, weight, bias, out,
+                                      channels_out, batch, depth, height, width, kernel_size, relu, 0, nullptr,
+                                      stream);
+}
+
+extern "C" int citrus_conv3d_backward_input_config(const float* grad_out, int64_t channels_out,
+                                                   const uint16_t* weight, float* grad_a, int64_t channels_a,
+                                                   const float* mask_a, float* grad_b, int64_t channels_b,
+                                                   int64_t batch, int64_t depth, int64_t height, int64_t width,
+                                                   int32_t kernel_size, int32_t variant, uint32_t* error_word,
+                                                   void* stream) {
   int st = check_volume(batch, depth, height, width, "citrus_conv3d_backward_input");
   if (st) return st;
   CITRUS_REQUIRE(grad_out && weight && grad_a, "citrus_conv3d_backward_input: null pointer argument");
@@ -405,9 +679,20 @@ extern "C" int citrus_conv3d_backward_input(const float* grad_out, int64_t chann
              weight, k3, ci * k3, -1, k3 - 1,
              nullptr, grad_a, grad_b, (int)channels_a, (int)channels_b, mask_a, 0,
              (int)batch, (int)depth, (int)height, (int)width};
-  st = launch_conv(a, kernel_size, as_stream(stream));
+  CITRUS_REQUIRE(variant >= 0 && variant <= 2,
+                 "citrus_conv3d_backward_input: variant %d (0 auto, 1 SIMT, 2 tensor cores)", variant);
+  st = launch_conv(a, kernel_size, variant, error_word, as_stream(stream));
   if (st) return st;
   return launch_status("citrus_conv3d_backward_input");
+}
+
+extern "C" int citrus_conv3d_backward_input(const float* grad_out, int64_t channels_out, const uint16_t* weight,
+                                            float* grad_a, int64_t channels_a, const float* mask_a, float* grad_b,
+                                            int64_t channels_b, int64_t batch, int64_t depth, int64_t height,
+                                            int64_t width, int32_t kernel_size, void* stream) {
+  return citrus_conv3d_backward_input_config(grad_out, channels_out, weight, grad_a, channels_a, mask_a, grad_b,
+                                             channels_b, batch, depth, height, width, kernel_size, 0, nullptr,
+                                             stream);
 }
 
 extern "C" int64_t citrus_conv3d_weight_grad_splits(int64_t channels_out, int64_t channels_a, int64_t channels_b,

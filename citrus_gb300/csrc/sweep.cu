@@ -61,32 +61,39 @@ __device__ __forceinline__ void gather_lane(int64_t lane, LaneIn& in, float* __r
   in.Z = uz < N ? load4<kCoherent>(base + uz * Q) : zero;
 }
 
-// The closed-form cell solve of one lane and its store over the source.
+// The closed-form cell solve of one lane and its store over the source. Every operation is rounded on its own (no
+// multiply-add contraction), so every kernel that inlines it computes the same bits.
 __device__ __forceinline__ void finish_lane(const LaneIn& in) {
   const float sx = (in.o & 4) ? -1.f : 1.f, sy = (in.o & 2) ? -1.f : 1.f, sz = (in.o & 1) ? -1.f : 1.f;
   const float cx = in.cx, cy = in.cy, cz = in.cz, m = in.m;
   const float4 s = in.s, X = in.X, Y = in.Y, Z = in.Z;
   // face-averaged inflow psibar_a = psi_0[N_a] + s_a psi_a[N_a]
-  const float pbx = X.x + sx * X.y;
-  const float pby = Y.x + sy * Y.z;
-  const float pbz = Z.x + sz * Z.w;
-  const float r0 = s.x + (cx * pbx + cy * pby + cz * pbz);
+  const float pbx = __fadd_rn(X.x, __fmul_rn(sx, X.y));
+  const float pby = __fadd_rn(Y.x, __fmul_rn(sy, Y.z));
+  const float pbz = __fadd_rn(Z.x, __fmul_rn(sz, Z.w));
+  const float r0 = __fadd_rn(s.x, __fadd_rn(__fadd_rn(__fmul_rn(cx, pbx), __fmul_rn(cy, pby)), __fmul_rn(cz, pbz)));
   // R_a = S_a - 3 s_a c_a psibar_a + sum_{b != a} c_b psi_a[N_b]
-  const float rx = s.y - 3.f * sx * cx * pbx + (cy * Y.y + cz * Z.y);
-  const float ry = s.z - 3.f * sy * cy * pby + (cx * X.z + cz * Z.z);
-  const float rz = s.w - 3.f * sz * cz * pbz + (cx * X.w + cy * Y.w);
-  const float csum = cx + cy + cz;
-  const float dx = 3.f * cx + (csum - cx) + m;
-  const float dy = 3.f * cy + (csum - cy) + m;
-  const float dz = 3.f * cz + (csum - cz) + m;
-  const float qx = cx / dx, qy = cy / dy, qz = cz / dz;
-  const float denom = csum + m + 3.f * (cx * qx + cy * qy + cz * qz);
-  const float p0 = (r0 - (sx * qx * rx + sy * qy * ry + sz * qz * rz)) / denom;
+  const float tx = __fmul_rn(__fmul_rn(__fmul_rn(3.f, sx), cx), pbx);
+  const float ty = __fmul_rn(__fmul_rn(__fmul_rn(3.f, sy), cy), pby);
+  const float tz = __fmul_rn(__fmul_rn(__fmul_rn(3.f, sz), cz), pbz);
+  const float rx = __fadd_rn(__fsub_rn(s.y, tx), __fadd_rn(__fmul_rn(cy, Y.y), __fmul_rn(cz, Z.y)));
+  const float ry = __fadd_rn(__fsub_rn(s.z, ty), __fadd_rn(__fmul_rn(cx, X.z), __fmul_rn(cz, Z.z)));
+  const float rz = __fadd_rn(__fsub_rn(s.w, tz), __fadd_rn(__fmul_rn(cx, X.w), __fmul_rn(cy, Y.w)));
+  const float csum = __fadd_rn(__fadd_rn(cx, cy), cz);
+  const float dx = __fadd_rn(__fadd_rn(__fmul_rn(3.f, cx), __fsub_rn(csum, cx)), m);
+  const float dy = __fadd_rn(__fadd_rn(__fmul_rn(3.f, cy), __fsub_rn(csum, cy)), m);
+  const float dz = __fadd_rn(__fadd_rn(__fmul_rn(3.f, cz), __fsub_rn(csum, cz)), m);
+  const float qx = __fdiv_rn(cx, dx), qy = __fdiv_rn(cy, dy), qz = __fdiv_rn(cz, dz);
+  const float qsum = __fadd_rn(__fadd_rn(__fmul_rn(cx, qx), __fmul_rn(cy, qy)), __fmul_rn(cz, qz));
+  const float denom = __fadd_rn(__fadd_rn(csum, m), __fmul_rn(3.f, qsum));
+  const float corr = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(sx, qx), rx), __fmul_rn(__fmul_rn(sy, qy), ry)),
+                               __fmul_rn(__fmul_rn(sz, qz), rz));
+  const float p0 = __fdiv_rn(__fsub_rn(r0, corr), denom);
   float4 out;
   out.x = p0;
-  out.y = (rx + 3.f * sx * cx * p0) / dx;
-  out.z = (ry + 3.f * sy * cy * p0) / dy;
-  out.w = (rz + 3.f * sz * cz * p0) / dz;
+  out.y = __fdiv_rn(__fadd_rn(rx, __fmul_rn(__fmul_rn(__fmul_rn(3.f, sx), cx), p0)), dx);
+  out.z = __fdiv_rn(__fadd_rn(ry, __fmul_rn(__fmul_rn(__fmul_rn(3.f, sy), cy), p0)), dy);
+  out.w = __fdiv_rn(__fadd_rn(rz, __fmul_rn(__fmul_rn(__fmul_rn(3.f, sz), cz), p0)), dz);
   *reinterpret_cast<float4*>(in.dst) = out;
 }
 

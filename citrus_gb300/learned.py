@@ -104,6 +104,8 @@ class ConvNet3D:
             layer.weight_bf16 = torch.empty(layer.weight.shape, dtype=torch.int16, device=self.device)
             self._refresh_bf16(layer)
         self._cache: dict = {}
+        self.variant = 0          # 0: the autotuner picks each layer's kernel; 1 SIMT; 2 tensor cores
+        self._error = torch.zeros(1, dtype=torch.int32, device=self.device)
 
     # -- parameters --------------------------------------------------------------------------------------------------
     def _refresh_bf16(self, layer: ConvLayer) -> None:
@@ -142,12 +144,36 @@ class ConvNet3D:
             raise ValueError(f"spatial sizes {tuple(x.shape[2:])} must be divisible by {step}")
 
     # -- kernels -----------------------------------------------------------------------------------------------------
+    def _variant(self, op: str, layer: ConvLayer, shape: tuple, run) -> int:
+        """The convolution kernel of this layer and shape: ``self.variant`` when set (1 SIMT, 2 tensor cores), else
+        the autotuner's choice between them."""
+        if self.variant:
+            return self.variant
+        from .autotune import Autotuner, tuner
+
+        B, D, H, W = shape
+        key = Autotuner.key(op, self.device, B=B, D=D, H=H, W=W, ca=layer.c_a, cb=layer.c_b, co=layer.c_out,
+                            k=layer.k, up=int(layer.b_up))
+        return int(tuner().choose(key, [2, 1], run, 2))
+
+    def check_errors(self) -> None:
+        """Raise if a wait for the tensor cores ran out in any convolution so far (reads a device word)."""
+        if int(self._error.item()) != 0:
+            self._error.zero_()
+            raise _lib.CitrusKernelError("conv3d: a wait for the tensor cores ran out; the results are invalid")
+
     def _conv(self, layer: ConvLayer, a: Tensor, b: Optional[Tensor] = None) -> Tensor:
         B, _, D, H, W = a.shape
         out = torch.empty((B, layer.c_out, D, H, W), device=self.device, dtype=torch.float32)
-        _lib.call("citrus_conv3d_forward", a.data_ptr(), layer.c_a, _lib.ptr(b), layer.c_b, int(layer.b_up),
-                  layer.weight_bf16.data_ptr(), layer.bias.data_ptr(), out.data_ptr(), layer.c_out, B, D, H, W,
-                  layer.k, int(layer.relu), _lib.stream_handle(self.device))
+        stream = _lib.stream_handle(self.device)
+
+        def run(variant):
+            _lib.call("citrus_conv3d_forward_config", a.data_ptr(), layer.c_a, _lib.ptr(b), layer.c_b,
+                      int(layer.b_up), layer.weight_bf16.data_ptr(), layer.bias.data_ptr(), out.data_ptr(),
+                      layer.c_out, B, D, H, W, layer.k, int(layer.relu), int(variant), self._error.data_ptr(),
+                      stream)
+
+        run(self._variant("conv3d_forward", layer, (B, D, H, W), run))
         return out
 
     def _pool(self, x: Tensor) -> Tensor:
@@ -160,9 +186,14 @@ class ConvNet3D:
         B, _, D, H, W = g.shape
         ga = torch.empty((B, layer.c_a, D, H, W), device=self.device, dtype=torch.float32)
         gb = torch.empty((B, layer.c_b, D, H, W), device=self.device, dtype=torch.float32) if want_b else None
-        _lib.call("citrus_conv3d_backward_input", g.data_ptr(), layer.c_out, layer.weight_bf16.data_ptr(),
-                  ga.data_ptr(), layer.c_a, _lib.ptr(mask_a), _lib.ptr(gb), layer.c_b if want_b else 0, B, D, H, W,
-                  layer.k, _lib.stream_handle(self.device))
+        stream = _lib.stream_handle(self.device)
+
+        def run(variant):
+            _lib.call("citrus_conv3d_backward_input_config", g.data_ptr(), layer.c_out, layer.weight_bf16.data_ptr(),
+                      ga.data_ptr(), layer.c_a, _lib.ptr(mask_a), _lib.ptr(gb), layer.c_b if want_b else 0, B, D, H,
+                      W, layer.k, int(variant), self._error.data_ptr(), stream)
+
+        run(self._variant("conv3d_backward_input" + ("_b" if want_b else ""), layer, (B, D, H, W), run))
         return ga, gb
 
     def _backward_weight(self, layer: ConvLayer, g: Tensor, a: Tensor, b: Optional[Tensor]) -> None:
@@ -331,7 +362,9 @@ class HigherOrderProposal:
     def predict(self, rho_coarse: Tensor, first: Tensor) -> Tensor:
         """Phi_{>1} scalar flux [G, R, C, S] of one view."""
         x, s = features(rho_coarse.to(self.device), first.to(self.device))
-        return self.net.forward(x)[0] * s
+        y = self.net.forward(x)[0] * s
+        self.net.check_errors()
+        return y
 
     def propose(self, rho_coarse: Tensor, first_collided: Tensor) -> Tensor:
         """The proposed accumulator: phi^(1) with Phi_{>1} added to its cell-mean scalar moment."""
@@ -366,6 +399,7 @@ class HigherOrderProposal:
                 self.net.backward(grad)
                 opt.step()
                 total += loss
+            self.net.check_errors()
             losses.append(float(total) / max(1, n // batch))
             if log_every and (epoch + 1) % log_every == 0:
                 print(f"epoch {epoch + 1}: loss {losses[-1]:.4e}")

@@ -329,12 +329,30 @@ int citrus_conv3d_forward(const float* in_a, int64_t channels_a, const float* in
                           int64_t channels_out, int64_t batch, int64_t depth, int64_t height, int64_t width,
                           int32_t kernel_size, int32_t relu, void* stream);
 
+/* citrus_conv3d_forward with the kernel chosen by the caller (the autotuner): variant 1 = the FP32 SIMT kernel
+ * (a 4 x 8 x 8 voxel brick x 16 output channels per CTA), 2 (and 0) = the implicit GEMM on the tcgen05 tensor cores
+ * (128 voxels x up to 256 output channels per CTA, every input split into bfloat16 high and low parts against the
+ * exact bfloat16 weights, float32 accumulation in tensor memory). error_word (NULL: none) is set to 1 if a wait for
+ * the tensor cores ran out (the output is then invalid). */
+int citrus_conv3d_forward_config(const float* in_a, int64_t channels_a, const float* in_b, int64_t channels_b,
+                                 int32_t b_upsampled, const uint16_t* weight, const float* bias, float* out,
+                                 int64_t channels_out, int64_t batch, int64_t depth, int64_t height, int64_t width,
+                                 int32_t kernel_size, int32_t relu, int32_t variant, uint32_t* error_word,
+                                 void* stream);
+
 /* Input gradient of citrus_conv3d_forward: grad_a (channels_a, times (mask_a > 0) when mask_a is set) and grad_b
  * (channels_b, at full resolution, before the upsampling's backward pass) from grad_out (channels_out). */
 int citrus_conv3d_backward_input(const float* grad_out, int64_t channels_out, const uint16_t* weight, float* grad_a,
                                  int64_t channels_a, const float* mask_a, float* grad_b, int64_t channels_b,
                                  int64_t batch, int64_t depth, int64_t height, int64_t width, int32_t kernel_size,
                                  void* stream);
+
+/* citrus_conv3d_backward_input with the kernel chosen by the caller (variants as citrus_conv3d_forward_config). */
+int citrus_conv3d_backward_input_config(const float* grad_out, int64_t channels_out, const uint16_t* weight,
+                                        float* grad_a, int64_t channels_a, const float* mask_a, float* grad_b,
+                                        int64_t channels_b, int64_t batch, int64_t depth, int64_t height,
+                                        int64_t width, int32_t kernel_size, int32_t variant, uint32_t* error_word,
+                                        void* stream);
 
 /* Partial sums the weight gradient uses for these sizes: it wants partial_capacity >= splits * C_out * C_in * k^3
  * floats (fewer splits, or none, with less). */
