@@ -205,15 +205,20 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* 
   float c0[kMP], c1[kMP];
 #pragma unroll
   for (int r = 0; r < kMP; ++r) c0[r] = c1[r] = 0.f;
-  for (int k = 0; k < K; ++k) {
-    float x0, x1 = 0.f;
+  // the loads of kU consecutive rows of B are issued before their products, so that every warp keeps kU loads in
+  // flight instead of one (the sums still run over k in order)
+  constexpr int kU = 8;
+  auto load_b = [&](int k, float& x0, float& x1) {
     if (kPair) {
-      const float2 v = *reinterpret_cast<const float2*>(B + (int64_t)k * ldb + col);
+      const float2 v = __ldg(reinterpret_cast<const float2*>(B + (int64_t)k * ldb + col));
       x0 = v.x;
       x1 = v.y;
     } else {
-      x0 = B[(int64_t)k * ldb + col];
+      x0 = __ldg(B + (int64_t)k * ldb + col);
+      x1 = 0.f;
     }
+  };
+  auto product = [&](int k, float x0, float x1) {
     const float* at = At + k * kMP;
 #pragma unroll
     for (int r = 0; r < kMP; r += 4) {
@@ -229,6 +234,19 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* 
         c1[r + 3] = fmaf(a.w, x1, c1[r + 3]);
       }
     }
+  };
+  int k = 0;
+  for (; k + kU <= K; k += kU) {
+    float x0[kU], x1[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) load_b(k + u, x0[u], x1[u]);
+#pragma unroll
+    for (int u = 0; u < kU; ++u) product(k + u, x0[u], x1[u]);
+  }
+  for (; k < K; ++k) {
+    float x0, x1;
+    load_b(k, x0, x1);
+    product(k, x0, x1);
   }
   if (kAccumulate) {  // eight rows' loads before their stores
 #pragma unroll
@@ -245,8 +263,10 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* 
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        c0[r8 + q] += o[q].x;
-        c1[r8 + q] += o[q].y;
+        if (r8 + q < kMP) {
+          c0[r8 + q] += o[q].x;
+          c1[r8 + q] += o[q].y;
+        }
       }
     }
   }
@@ -302,6 +322,7 @@ int launch_stream(const float* A, int64_t lda, const float* B, int64_t ldb, floa
   if (K <= 64) return launch_cols<64, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (M <= 16) return launch_rows<16, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (M <= 32) return launch_rows<32, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (M <= 36) return launch_rows<36, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (M <= 48) return launch_rows<48, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   return launch_rows<64, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
 }

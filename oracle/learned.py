@@ -15,13 +15,17 @@ import torch
 import torch.nn.functional as F
 
 
-def forward(weights: dict, biases: dict, x: torch.Tensor, levels: int) -> torch.Tensor:
-    """y [B, out, D, H, W] of x [B, in, D, H, W]; weights/biases by layer name (float64 CPU tensors)."""
+def forward(weights: dict, biases: dict, x: torch.Tensor, levels: int, masks: dict = None) -> torch.Tensor:
+    """y [B, out, D, H, W] of x [B, in, D, H, W]; weights/biases by layer name (float64 CPU tensors). ``masks`` (by
+    layer name, optional) replaces each ReLU's decision by a given one: the checked kernels' own, so that a
+    pre-activation within rounding of zero takes the same side in both computations."""
 
     def conv(name, h, relu=True):
         w = weights[name]
         y = F.conv3d(h, w, biases[name], padding=w.shape[-1] // 2)
-        return F.relu(y) if relu else y
+        if not relu:
+            return y
+        return F.relu(y) if masks is None else y * masks[name].to(y.dtype)
 
     skips = []
     h = x
@@ -37,11 +41,12 @@ def forward(weights: dict, biases: dict, x: torch.Tensor, levels: int) -> torch.
     return conv("out", top, relu=False)
 
 
-def loss_and_gradients(weights: dict, biases: dict, x: torch.Tensor, target: torch.Tensor, levels: int) -> dict:
-    """Output, MSE loss and the gradient of every weight and bias, all float64."""
+def loss_and_gradients(weights: dict, biases: dict, x: torch.Tensor, target: torch.Tensor, levels: int,
+                       masks: dict = None) -> dict:
+    """Output, MSE loss and the gradient of every weight and bias, all float64 (``masks`` as in ``forward``)."""
     w = {k: v.detach().double().clone().requires_grad_(True) for k, v in weights.items()}
     b = {k: v.detach().double().clone().requires_grad_(True) for k, v in biases.items()}
-    y = forward(w, b, x.double(), levels)
+    y = forward(w, b, x.double(), levels, masks)
     loss = ((y - target.double()) ** 2).mean()
     loss.backward()
     out = {"y": y.detach(), "loss": float(loss.detach())}
