@@ -17,6 +17,7 @@
 // warp reads and writes 32 consecutive points of one group. The transfer table is laid out [M, N_eta, G_out, G_in]
 // (downscatter only, zero above the diagonal), so the 32 B row of one outgoing group at one node is one vector load.
 #include <math.h>
+#include <stdlib.h>
 
 #include "common.cuh"
 
@@ -405,9 +406,9 @@ __device__ __forceinline__ float row_dot(const float* __restrict__ row, const fl
 constexpr int kWindowBytes = 32 * 1024;
 
 __host__ __device__ inline int window_row_stride(int G) { return G * G + 4; }
-__host__ __device__ inline int window_nodes(int M, int G) {
-  const int n = kWindowBytes / (4 * M * window_row_stride(G));
-  return n < 64 ? n : 64;
+__host__ __device__ inline int window_nodes(int M, int G, int bytes = kWindowBytes) {
+  const int n = bytes / (4 * M * window_row_stride(G));
+  return n < 96 ? n : 96;
 }
 
 
@@ -417,7 +418,7 @@ __host__ __device__ inline int window_nodes(int M, int G) {
 // every thread of the block must call it.
 __device__ void stage_window(const Table& tb, bool valid, float ux, float uy, float uz, const float (*s_om)[3], int n,
                              int first_dir, int dir_step, int warp, int nwarps, int tid, int nthreads,
-                             int (*s_range)[32], int* s_window, float* s_tab) {
+                             int (*s_range)[32], int* s_window, float* s_tab, int window_bytes = kWindowBytes) {
   const int G = tb.G;
   int lo = 1 << 30, hi = -1;
   if (valid) {
@@ -444,7 +445,7 @@ __device__ void stage_window(const Table& tb, bool valid, float ux, float uy, fl
       lo = min(lo, s_range[0][q]);
       hi = max(hi, s_range[1][q]);
     }
-    const bool fits = hi >= lo && hi + 2 - lo <= window_nodes(tb.M, G);
+    const bool fits = hi >= lo && hi + 2 - lo <= window_nodes(tb.M, G, window_bytes);
     s_window[0] = fits ? lo : -1;
     s_window[1] = fits ? hi + 2 - lo : 0;
   }
@@ -487,7 +488,10 @@ __device__ __forceinline__ float fc_group(const Table& tb, const float* s_tab, i
   return src;
 }
 
-template <int kGP, int kMM, bool kFused>
+// window bytes of an emission block with kDirs directions (more directions span more table nodes)
+__host__ __device__ constexpr int emission_window_bytes(int dirs) { return dirs > 16 ? 48 * 1024 : kWindowBytes; }
+
+template <int kGP, int kMM, bool kFused, int kDirs>
 __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
     FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, int K,
     const float* __restrict__ tau /*[K, NC, G], or [K, NC, TM] path lengths with tau_mu*/,
@@ -500,27 +504,27 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
   constexpr int kWarps = kEmitPoints / kPW;     // = kGP
   extern __shared__ float4 s_dyn4[];
   float* s_tab = reinterpret_cast<float*>(s_dyn4);  // the table window (dynamic, kWindowBytes)
-  __shared__ float s_om[kEmitDirs][3];
-  __shared__ float s_sw[kEmitDirs][kGP];          // signal weights of the block's directions
-  __shared__ __align__(16) float s_y[kFused ? kEmitDirs : 1][kFused ? kMaxMoments : 4];
-  __shared__ float s_sum[kEmitDirs][kWarps][2];   // per-direction, per-warp sums of e and e h
+  __shared__ float s_om[kDirs][3];
+  __shared__ float s_sw[kDirs][kGP];          // signal weights of the block's directions
+  __shared__ __align__(16) float s_y[kFused ? kDirs : 1][kFused ? kMaxMoments : 4];
+  __shared__ float s_sum[kDirs][kWarps][2];   // per-direction, per-warp sums of e and e h
   __shared__ int s_range[2][32];
   __shared__ int s_window[2];
   const int G = tb.G;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
   const int g = lane % kGP, p = warp * kPW + lane / kGP;   // the thread's group and point of the block
   const bool gvalid = g < G;
-  const int d0 = blockIdx.y * kEmitDirs;
-  const int nd = min(kEmitDirs, K - d0);
+  const int d0 = blockIdx.y * kDirs;
+  const int nd = min(kDirs, K - d0);
   constexpr int nthreads = kEmitPoints * kGP;
-  for (int i = tid; i < kEmitDirs * 3; i += nthreads) s_om[i / 3][i % 3] = i < nd * 3 ? omegas[3 * d0 + i] : 0.f;
+  for (int i = tid; i < kDirs * 3; i += nthreads) s_om[i / 3][i % 3] = i < nd * 3 ? omegas[3 * d0 + i] : 0.f;
   if (signal_weight != nullptr)
-    for (int i = tid; i < kEmitDirs * kGP; i += nthreads) {
+    for (int i = tid; i < kDirs * kGP; i += nthreads) {
       const int dd = i / kGP, q = i % kGP;
       s_sw[dd][q] = (dd < nd && q < G) ? signal_weight[(int64_t)(d0 + dd) * G + q] : 0.f;
     }
   if (kFused)
-    for (int i = tid; i < kEmitDirs * NS; i += nthreads)
+    for (int i = tid; i < kDirs * NS; i += nthreads)
       s_y[i / NS][i % NS] = i < nd * NS ? harmonics[(int64_t)d0 * NS + i] : 0.f;
 
   const int64_t v = (int64_t)blockIdx.x * kEmitPoints + p;
@@ -562,7 +566,8 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
       tmom[n] = (valid && gvalid && n < NS) ? __ldg(moments + ((int64_t)n * NC + cell) * G + g) : 0.f;
   }
   __syncthreads();  // s_om and s_y are complete
-  stage_window(tb, valid, ux, uy, uz, s_om, nd, g, kGP, warp, kWarps, tid, nthreads, s_range, s_window, s_tab);
+  stage_window(tb, valid, ux, uy, uz, s_om, nd, g, kGP, warp, kWarps, tid, nthreads, s_range, s_window, s_tab,
+               emission_window_bytes(kDirs));
   const int win_lo = s_window[0];
 
   for (int dd = 0; dd < nd; ++dd) {
@@ -1118,20 +1123,48 @@ extern "C" int citrus_first_collision_correction(const float* rho, int64_t num_m
 namespace citrus {
 namespace {
 
+template <int kGP, int kMM, bool kFused, int kDirs>
+int launch_emission_d(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                      const float* omegas, int K, const float* tau, const float* tau_mu, int TM, const float* mu,
+                      const float* multiple, const float* harmonics, const float* moments, int NS,
+                      const float* heights, const float* signal_weight, const double* deltas, float* out,
+                      float* partial) {
+  constexpr int bytes = emission_window_bytes(kDirs);
+  cudaError_t e = cudaFuncSetAttribute(emission_kernel<kGP, kMM, kFused, kDirs>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "emission window: %s", cudaGetErrorString(e));
+  grid.y = (unsigned)cdiv(K, kDirs);
+  emission_kernel<kGP, kMM, kFused, kDirs><<<grid, kEmitPoints * kGP, bytes, s>>>(
+      in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, harmonics, moments, NS, heights, signal_weight, (float)deltas[0],
+      (float)deltas[1], (float)deltas[2], out, partial);
+  note_launches();
+  return CITRUS_OK;
+}
+
+// directions per emission block: 32 amortise the block's set-up (point geometry, table window) over twice as many
+// directions once there are enough of them; CITRUS_EMISSION_DIRS (16 or 32) overrides, for measurements
+inline int emission_dirs(int K) {
+  static const int forced = [] {
+    const char* v = getenv("CITRUS_EMISSION_DIRS");
+    return v ? atoi(v) : 0;
+  }();
+  if (forced == 16 || forced == 32) return forced;
+  return K >= 64 ? 32 : 16;
+}
+
 template <int kGP, int kMM, bool kFused>
 int launch_emission_m(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
                       const float* omegas, int K, const float* tau, const float* tau_mu, int TM, const float* mu,
                       const float* multiple, const float* harmonics, const float* moments, int NS,
                       const float* heights, const float* signal_weight, const double* deltas, float* out,
                       float* partial) {
-  cudaError_t e = cudaFuncSetAttribute(emission_kernel<kGP, kMM, kFused>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kWindowBytes);
-  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "emission window: %s", cudaGetErrorString(e));
-  emission_kernel<kGP, kMM, kFused><<<grid, kEmitPoints * kGP, kWindowBytes, s>>>(
-      in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, harmonics, moments, NS, heights, signal_weight, (float)deltas[0],
-      (float)deltas[1], (float)deltas[2], out, partial);
-  note_launches();
-  return CITRUS_OK;
+  (void)G;
+  if (emission_dirs(K) == 32)
+    return launch_emission_d<kGP, kMM, kFused, 32>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                                   harmonics, moments, NS, heights, signal_weight, deltas, out,
+                                                   partial);
+  return launch_emission_d<kGP, kMM, kFused, 16>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                                 harmonics, moments, NS, heights, signal_weight, deltas, out, partial);
 }
 
 template <int kGP, bool kFused>
@@ -1155,7 +1188,7 @@ int emission_for(int64_t V, int K, cudaStream_t s, const FCInputs& in, const Tab
                  const float* signal_weight, const double* deltas, float* out, float* partial,
                  float* height_sums) {
   const int64_t nblocks = cdiv(V, kEmitPoints);
-  dim3 grid((unsigned)nblocks, (unsigned)cdiv(K, kEmitDirs));
+  dim3 grid((unsigned)nblocks, 1u);  // grid.y: the direction blocks, set by the launcher
   const int st = moments != nullptr
                      ? launch_emission<kGP, true>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
                                                   multiple, harmonics, moments, NS, heights, signal_weight, deltas,
