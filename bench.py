@@ -54,6 +54,8 @@ def _parse():
                                                          "profiling captures)")
     p.add_argument("--no-graph", dest="graph", action="store_false",
                    help="run every step eagerly instead of replaying the outer iteration from a CUDA graph")
+    p.add_argument("--no-plain", action="store_true",
+                   help="skip the measurement of the plain form (citrus_view_step per view, eager)")
     p.add_argument("--no-learned", action="store_true",
                    help="skip the learned higher-order proposal measurement (training and converged steps)")
     p.add_argument("--learned-cells", default="24,24,16",
@@ -577,6 +579,35 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
             "spr_error": spr_error(w, mixed, angles[:2], device)}
 
 
+def plain_single_view_step(w, solver, angles, rho_dev, device) -> dict:
+    """The plain form of the same outer iteration: ``citrus_view_step`` per view, eagerly, one sweep launch per view
+    (no batching, no graph), float32 products; ms/view over one warm step after the cold start."""
+    import torch
+
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step
+
+    states = [CitrusState() for _ in angles]
+    stream = torch.cuda.current_stream(device)
+
+    def step():
+        fields = solver.material_fields(rho_dev, w.grid)
+        for v, a in enumerate(angles):
+            _, _, states[v] = citrus_view_step(solver, states[v], fields, float(a), primary=False)
+
+    step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    value = e0.elapsed_time(e1) / len(angles)
+    states.clear()
+    torch.cuda.empty_cache()
+    return {"value": value, "unit": "ms/view", "steps": 1,
+            "form": "citrus_view_step per view: one sweep launch per view, eager, float32 products"}
+
+
 def learned_measurement(args, device) -> dict:
     """The learned higher-order proposal on the learned-proposal workload (random ellipsoid phantoms, 12 groups, P5,
     6 x 28 directions, cone 16 x 32, curved 256 x 192 panel) at ``--learned-cells``: the solver generates the
@@ -778,6 +809,7 @@ def run_step(args):
     launches = count_launches(lambda: eager_step(rho_dev))   # a replay launches the same kernels as the eager step
     states.clear()
     torch.cuda.empty_cache()
+    plain = None if args.no_plain else plain_single_view_step(w, solver, angles, rho_dev, device)
     spr = spr_error(w, solver, angles[:2], device) if args.precision != "fp32" else None
     mixed = None
     if args.precision == "fp32" and not args.no_mixed:
@@ -825,6 +857,8 @@ def run_step(args):
         line["spr_error"] = spr
     if mixed is not None:
         line["mixed_precision_bf16x3"] = mixed
+    if plain is not None:
+        line["plain_single_view_step"] = plain
     if not args.no_learned and rank == 0:
         line["learned_proposal"] = learned_measurement(args, device)
     if rank == 0:

@@ -489,7 +489,9 @@ __device__ __forceinline__ float fc_group(const Table& tb, const float* s_tab, i
 }
 
 // window bytes of an emission block with kDirs directions (more directions span more table nodes)
-__host__ __device__ constexpr int emission_window_bytes(int dirs) { return dirs > 16 ? 48 * 1024 : kWindowBytes; }
+__host__ __device__ constexpr int emission_window_bytes(int dirs) {
+  return dirs > 32 ? 64 * 1024 : dirs > 16 ? 48 * 1024 : kWindowBytes;
+}
 
 template <int kGP, int kMM, bool kFused, int kDirs>
 __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
@@ -1142,13 +1144,13 @@ int launch_emission_d(dim3 grid, cudaStream_t s, const FCInputs& in, const Table
 }
 
 // directions per emission block: 32 amortise the block's set-up (point geometry, table window) over twice as many
-// directions once there are enough of them; CITRUS_EMISSION_DIRS (16 or 32) overrides, for measurements
+// directions once there are enough of them; CITRUS_EMISSION_DIRS (16, 32 or 64) overrides, for measurements
 inline int emission_dirs(int K) {
   static const int forced = [] {
     const char* v = getenv("CITRUS_EMISSION_DIRS");
     return v ? atoi(v) : 0;
   }();
-  if (forced == 16 || forced == 32) return forced;
+  if (forced == 16 || forced == 32 || forced == 64) return forced;
   return K >= 64 ? 32 : 16;
 }
 
@@ -1159,7 +1161,12 @@ int launch_emission_m(dim3 grid, int G, cudaStream_t s, const FCInputs& in, cons
                       const float* heights, const float* signal_weight, const double* deltas, float* out,
                       float* partial) {
   (void)G;
-  if (emission_dirs(K) == 32)
+  const int dirs = emission_dirs(K);
+  if (dirs == 64)
+    return launch_emission_d<kGP, kMM, kFused, 64>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                                   harmonics, moments, NS, heights, signal_weight, deltas, out,
+                                                   partial);
+  if (dirs == 32)
     return launch_emission_d<kGP, kMM, kFused, 32>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
                                                    harmonics, moments, NS, heights, signal_weight, deltas, out,
                                                    partial);
