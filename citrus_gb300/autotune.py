@@ -146,13 +146,15 @@ def small_k_gemm_config(A, B, C, M: int, K: int, J: int, batch: int, sb: int, sc
 
 
 VIEW_CANDIDATES = (1, 2, 4, 8)
-UNROLL_CANDIDATES = (1, 2, 4)
+# lanes-per-thread forms of the persistent sweep: one lane with the registers capped for 5 (form 1), 6 (form 3) or
+# 8 (form 5) blocks of 256 threads per SM, or 2 lanes loaded before they are solved (form 2)
+UNROLL_CANDIDATES = (1, 3, 5, 2)
 
 
 def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> tuple:
     """(views per persistent sweep launch, lanes per thread) for ``views`` views on this grid: the per-view time of
     the sweep on a zero store of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device
-    memory) at 1, 2 or 4 lanes per thread; fewest views, then fewest lanes, within 3 % of the fastest."""
+    memory) in each lanes-per-thread form; the first (fewest views) within 3 % of the fastest."""
     from . import kernels
 
     N, D8, Q = ctx.num_cells, ctx.directions_per_octant, 4 * num_groups

@@ -124,8 +124,8 @@ __global__ void __launch_bounds__(kThreads) plane_kernel(float* __restrict__ sto
 // All planes in one cooperative launch. A thread takes kU lanes of a plane at a time (stride apart, so every warp
 // still reads whole cells): all their loads are issued before the first solve and store, which a plain loop cannot
 // do (the stores might alias the next lane's loads as far as the compiler knows; within a plane they never do).
-template <int kG, int kU>
-__global__ void __launch_bounds__(kThreads) persistent_kernel(
+template <int kG, int kU, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_kernel(
     float* __restrict__ store, const float* __restrict__ mu, const float* __restrict__ c,
     const int* __restrict__ octant, const int* __restrict__ cell, const int* __restrict__ upstream,
     const int* __restrict__ offsets, int num_planes, int64_t N, int G, int64_t Dc, int64_t views,
@@ -167,13 +167,14 @@ int launch_planes(float* store, const float* mu, const float* c, const int* octa
   return launch_status("citrus_sweep_planes");
 }
 
-template <int kG, int kU>
+template <int kG, int kU, int kMinBlocks = 1>
 int launch_persistent_u(float* store, const float* mu, const float* c, const int* octant, const int* cell,
                         const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
                         int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
                         cudaStream_t stream) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG, kU>, kThreads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG, kU, kMinBlocks>,
+                                                                kThreads, 0);
   if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: occupancy query failed");
   int64_t blocks = (int64_t)per_sm * num_sms();
   if (max_blocks > 0 && max_blocks < blocks) blocks = max_blocks;
@@ -183,14 +184,14 @@ int launch_persistent_u(float* store, const float* mu, const float* c, const int
   if (z != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: %s", cudaGetErrorString(z));
   void* args[] = {&store, &mu, &c, &octant, &cell, &upstream, &offsets, &num_planes, &N, &G, &Dc, &views,
                   &view_stride, &sync, &timeout_ns, &skip};
-  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG, kU>, dim3((unsigned)blocks), dim3(kThreads), args,
-                                  0, stream);
+  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG, kU, kMinBlocks>, dim3((unsigned)blocks),
+                                  dim3(kThreads), args, 0, stream);
   if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_persistent: %s", cudaGetErrorString(e));
   note_launches();
   return CITRUS_OK;
 }
 
-constexpr int kDefaultUnroll = 2;
+constexpr int kDefaultUnroll = 1;
 
 template <int kG>
 int launch_persistent(float* store, const float* mu, const float* c, const int* octant, const int* cell,
@@ -198,13 +199,21 @@ int launch_persistent(float* store, const float* mu, const float* c, const int* 
                       int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
                       cudaStream_t stream, int unroll = kDefaultUnroll) {
   switch (unroll) {
-    case 1: return launch_persistent_u<kG, 1>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
-                                              views, sync, max_blocks, timeout_ns, skip, stream);
+    case 1:  // one lane per thread, five blocks of 256 threads per SM
+      return launch_persistent_u<kG, 1, 5>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                           views, sync, max_blocks, timeout_ns, skip, stream);
+    case 3:  // one lane per thread, registers capped for six blocks of 256 threads per SM
+      return launch_persistent_u<kG, 1, 6>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                           views, sync, max_blocks, timeout_ns, skip, stream);
+    case 5:  // one lane per thread, eight blocks per SM
+      return launch_persistent_u<kG, 1, 8>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                           views, sync, max_blocks, timeout_ns, skip, stream);
     case 2: return launch_persistent_u<kG, 2>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
                                               views, sync, max_blocks, timeout_ns, skip, stream);
     case 4: return launch_persistent_u<kG, 4>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
                                               views, sync, max_blocks, timeout_ns, skip, stream);
-    default: return set_error(CITRUS_EINVAL, "citrus_sweep_persistent: lanes per thread %d (1, 2 or 4)", unroll);
+    default:
+      return set_error(CITRUS_EINVAL, "citrus_sweep_persistent: lanes per thread form %d (1, 2, 3, 4 or 5)", unroll);
   }
 }
 

@@ -12,6 +12,7 @@ the height sums on the device) and the weighted accumulation (``citrus_weighted_
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -181,8 +182,11 @@ def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle
 
 # How the image's emission gets the multiple-collision source: "fused" forms Y_k T per point in registers
 # (citrus_attenuated_emission_moments); "product" writes Y_k T with the small-K product first and reads it
-# (citrus_attenuated_emission, the reference's interface).
-EMISSION_FORM = "product"
+# (citrus_attenuated_emission, the reference's interface). CITRUS_EMISSION_FORM picks one (both give the same image
+# to float rounding; the product form is the default, measured faster).
+EMISSION_FORM = os.environ.get("CITRUS_EMISSION_FORM", "product")
+if EMISSION_FORM not in ("product", "fused"):
+    raise ValueError(f"CITRUS_EMISSION_FORM must be 'product' or 'fused', got {EMISSION_FORM!r}")
 
 
 def _blur(src: Tensor, dst: Tensor, lines: int, length: int, strides_in: tuple, strides_out: tuple, k: int,
