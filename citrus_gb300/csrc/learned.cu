@@ -134,19 +134,21 @@ __global__ void __launch_bounds__(kConvThreads) conv_kernel(const ConvArgs a) {
 }
 
 // The same convolution as an implicit GEMM on the tcgen05 tensor cores: D[voxel, o] = sum_k A[voxel, k] B[o, k] with
-// k = (input channel, tap). A CTA takes a tile of 128 consecutive voxels (the MMA's M) x n_tile output channels (its
-// N, a multiple of 16 up to 256) and walks k in chunks of 64 through two shared-memory stages:
-//   * every thread gathers its voxel's 64 inputs of the chunk (the concatenation and the upsampling read in place,
-//     zero padding outside the volume), splits each float32 value into bfloat16 high and low parts and writes them in
-//     the K-major canonical layout (8-row x 16-byte core matrices, no swizzle);
+// k = tap C_in + input channel (tap-major, so that a run of k shares one spatial offset and its bounds test). A CTA
+// takes a tile of 128 consecutive voxels (the MMA's M) x n_tile output channels (its N, a multiple of 16 up to 256)
+// and walks k in chunks of 64 through two shared-memory stages:
+//   * two threads per voxel row gather 32 inputs each (all loads issued before the first store; the concatenation and
+//     the upsampling read in place, zero padding outside the volume), split every float32 value into bfloat16 high
+//     and low parts and write them in the K-major canonical layout (8-row x 16-byte core matrices, no swizzle);
 //   * the chunk's weights, already bfloat16, fill the B operand as they are;
 //   * one thread issues 2 x 4 MMAs (M = 128, N = n_tile, K = 16, kind::f16: A_hi B + A_lo B, exact weights, so the
 //     product keeps about sixteen bits of every input) into a float32 accumulator in tensor memory and commits them
 //     to the stage's mbarrier, while the threads build the other stage;
 //   * every wait on an mbarrier is bounded by a wall-clock limit (the CTA records the error and leaves).
-// The epilogue reads the accumulator (lane = voxel, column = output channel) and stores 32 consecutive voxels of one
-// channel per warp instruction, with the bias, the ReLU and the mask applied.
-constexpr int kCvThreads = 128;
+// The epilogue reads the accumulator (lane = voxel, column = output channel; the two warp groups take half the
+// columns each) and stores 32 consecutive voxels of one channel per warp instruction, with the bias, the ReLU and the
+// mask applied.
+constexpr int kCvThreads = 256;
 constexpr int kCvKC = 64;                     // inner dimension of one stage (four MMA K-steps)
 constexpr uint32_t kCvAStep = kTcM * 16 * 2;  // bytes of one K-step of A: 128 rows x 16 bfloat16
 
@@ -169,16 +171,19 @@ __global__ void __launch_bounds__(kCvThreads) conv_tc_kernel(const ConvArgs a, i
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid / 32;
+  const int row = tid & (kTcM - 1), half = tid >> 7;   // voxel row of the tile, half of the chunk's k range
   const int O = a.oa + a.ob, Ci = a.ca + a.cb;
   const int Ktot = Ci * K3;
   const int nchunks = (Ktot + kCvKC - 1) / kCvKC;
   const int64_t V = (int64_t)a.D * a.H * a.W;
-  const int Dc = a.D >> 1, Hc = a.H >> 1, Wc = a.W >> 1;
+  const int64_t Vc = (int64_t)(a.D >> 1) * (a.H >> 1) * (a.W >> 1);
+  const int Hc = a.H >> 1, Wc = a.W >> 1;
   const uint32_t a_bytes = 4 * kCvAStep;
   const uint32_t b_step = (uint32_t)n_tile * 32;
   const uint32_t stage_bytes = 2 * a_bytes + 4 * b_step;
   const uint32_t cols = n_tile <= 32 ? 32u : n_tile <= 64 ? 64u : n_tile <= 128 ? 128u : 256u;
   const uint32_t idesc = idesc_bf16(n_tile);
+  const int n_half = ((n_tile / 16 + 1) / 2) * 16;     // accumulator columns of the first warp group
 
   if (tid == 0) {
     abort_flag = 0;
@@ -206,11 +211,13 @@ __global__ void __launch_bounds__(kCvThreads) conv_tc_kernel(const ConvArgs a, i
     const int ct = (int)(rest % co_tiles);
     const int b = (int)(rest / co_tiles);
     const int co0 = ct * n_tile;
-    const int64_t vox = (int64_t)vt * kTcM + tid;
+    const int64_t vox = (int64_t)vt * kTcM + row;
     const bool vvalid = vox < V;
     const int x = vvalid ? (int)(vox % a.W) : 0;
     const int y = vvalid ? (int)((vox / a.W) % a.H) : 0;
     const int z = vvalid ? (int)(vox / ((int64_t)a.W * a.H)) : 0;
+    const float* src_a = a.in_a + (int64_t)b * a.ca * V;
+    const float* src_b = a.in_b + (int64_t)b * a.cb * (a.b_up ? Vc : V);
     for (int c = 0; c < nchunks; ++c) {
       const int st = c & 1;
       uint8_t* sa_hi = smem + st * stage_bytes;
@@ -222,63 +229,71 @@ __global__ void __launch_bounds__(kCvThreads) conv_tc_kernel(const ConvArgs a, i
         if (st == 0) { phase0 ^= 1u; pending0 = false; } else { phase1 ^= 1u; pending1 = false; }
         if (!ok) abort_flag = 1;
       }
-      // A: this thread's voxel row, the chunk's 64 inputs, split into bfloat16 high and low parts
-      int k = c * kCvKC;
-      int ci = k / K3, tap = k - ci * K3;
-#pragma unroll 1
-      for (int kk8 = 0; kk8 < kCvKC; kk8 += 8) {
-        float xv[8];
+      // A: this thread's 32 inputs of the chunk, k = tap Ci + ci
+      {
+        const int k0 = c * kCvKC + half * 32;
+        int t = k0 / Ci, ci = k0 - t * Ci;
+        int64_t off_a = 0, off_b = 0;
+        bool inb = false;
+        int t_cur = -1;
+        float xv[32];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < 32; ++q) {
           float v = 0.f;
-          if (vvalid && ci < Ci) {
-            const int gz = z + tap / (kK * kK) - kH, gy = y + (tap / kK) % kK - kH, gx = x + tap % kK - kH;
-            if (gz >= 0 && gz < a.D && gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
-              if (ci < a.ca)
-                v = __ldg(a.in_a + ((int64_t)b * a.ca + ci) * V + ((int64_t)gz * a.H + gy) * a.W + gx);
-              else if (a.b_up)
-                v = __ldg(a.in_b + (((int64_t)b * a.cb + (ci - a.ca)) * Dc + (gz >> 1)) * Hc * Wc +
-                          (int64_t)(gy >> 1) * Wc + (gx >> 1));
-              else
-                v = __ldg(a.in_b + ((int64_t)b * a.cb + (ci - a.ca)) * V + ((int64_t)gz * a.H + gy) * a.W + gx);
+          if (t < K3) {
+            if (t != t_cur) {  // a new tap: its spatial offset and bounds test, shared by the run of channels
+              t_cur = t;
+              const int gz = z + t / (kK * kK) - kH, gy = y + (t / kK) % kK - kH, gx = x + t % kK - kH;
+              inb = vvalid && gz >= 0 && gz < a.D && gy >= 0 && gy < a.H && gx >= 0 && gx < a.W;
+              off_a = ((int64_t)gz * a.H + gy) * a.W + gx;
+              off_b = a.b_up ? ((int64_t)(gz >> 1) * Hc + (gy >> 1)) * Wc + (gx >> 1) : off_a;
             }
+            if (inb)
+              v = ci < a.ca ? __ldg(src_a + (int64_t)ci * V + off_a)
+                            : __ldg(src_b + (int64_t)(ci - a.ca) * (a.b_up ? Vc : V) + off_b);
           }
           xv[q] = v;
-          if (++tap == K3) {
-            tap = 0;
-            ++ci;
+          if (++ci == Ci) {
+            ci = 0;
+            ++t;
           }
         }
-        uint4 hi, lo;
-        split_pair(xv[0], xv[1], hi.x, lo.x);
-        split_pair(xv[2], xv[3], hi.y, lo.y);
-        split_pair(xv[4], xv[5], hi.z, lo.z);
-        split_pair(xv[6], xv[7], hi.w, lo.w);
-        const uint32_t off = (uint32_t)(kk8 >> 4) * kCvAStep + core_offset(tid, kk8 & 15);
-        *reinterpret_cast<uint4*>(sa_hi + off) = hi;
-        *reinterpret_cast<uint4*>(sa_lo + off) = lo;
+#pragma unroll
+        for (int g8 = 0; g8 < 4; ++g8) {
+          uint4 hi, lo;
+          split_pair(xv[8 * g8 + 0], xv[8 * g8 + 1], hi.x, lo.x);
+          split_pair(xv[8 * g8 + 2], xv[8 * g8 + 3], hi.y, lo.y);
+          split_pair(xv[8 * g8 + 4], xv[8 * g8 + 5], hi.z, lo.z);
+          split_pair(xv[8 * g8 + 6], xv[8 * g8 + 7], hi.w, lo.w);
+          const int kk8 = half * 32 + g8 * 8;
+          const uint32_t off = (uint32_t)(kk8 >> 4) * kCvAStep + core_offset(row, kk8 & 15);
+          *reinterpret_cast<uint4*>(sa_hi + off) = hi;
+          *reinterpret_cast<uint4*>(sa_lo + off) = lo;
+        }
       }
       // B: n_tile output channels x the chunk's 64 weights, 8 at a time
       for (int u = tid; u < n_tile * 8; u += kCvThreads) {
-        const int row = u >> 3, g8 = u & 7;
-        const int o = co0 + row;
+        const int brow = u >> 3, g8 = u & 7;
+        const int o = co0 + brow;
+        const int k0 = c * kCvKC + g8 * 8;
+        int t = k0 / Ci, i = k0 - t * Ci;
         uint32_t w2[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           uint32_t pair = 0;
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
-            const int kq = c * kCvKC + g8 * 8 + 2 * q + h;
             uint32_t bits = 0;
-            if (o < O && kq < Ktot) {
-              const int i = kq / K3, t = kq - (kq / K3) * K3;
-              bits = a.w[a.w_base + o * a.w_o + i * a.w_i + t * a.w_t];
-            }
+            if (o < O && t < K3) bits = a.w[a.w_base + o * a.w_o + i * a.w_i + t * a.w_t];
             pair |= bits << (16 * h);
+            if (++i == Ci) {
+              i = 0;
+              ++t;
+            }
           }
           w2[q] = pair;
         }
-        const uint32_t off = (uint32_t)(g8 >> 1) * b_step + core_offset(row, (g8 & 1) * 8);
+        const uint32_t off = (uint32_t)(g8 >> 1) * b_step + core_offset(brow, (g8 & 1) * 8);
         *reinterpret_cast<uint4*>(sb + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -290,11 +305,11 @@ __global__ void __launch_bounds__(kCvThreads) conv_tc_kernel(const ConvArgs a, i
       if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const uint64_t ah = smem_desc(smem_u32(sa_hi + s * kCvAStep), 128, 256);
-          const uint64_t al = smem_desc(smem_u32(sa_lo + s * kCvAStep), 128, 256);
-          const uint64_t bd = smem_desc(smem_u32(sb + s * b_step), 128, 256);
-          mma_bf16(tmem, ah, bd, idesc, (c > 0 || s > 0) ? 1u : 0u);
+        for (int s4 = 0; s4 < 4; ++s4) {
+          const uint64_t ah = smem_desc(smem_u32(sa_hi + s4 * kCvAStep), 128, 256);
+          const uint64_t al = smem_desc(smem_u32(sa_lo + s4 * kCvAStep), 128, 256);
+          const uint64_t bd = smem_desc(smem_u32(sb + s4 * b_step), 128, 256);
+          mma_bf16(tmem, ah, bd, idesc, (c > 0 || s4 > 0) ? 1u : 0u);
           mma_bf16(tmem, al, bd, idesc, 1u);
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -320,31 +335,35 @@ __global__ void __launch_bounds__(kCvThreads) conv_tc_kernel(const ConvArgs a, i
       failed = true;
       break;
     }
-    // epilogue: accumulator lane tid = this thread's voxel, columns = output channels co0 ..
+    // epilogue: accumulator lane = voxel row, columns = output channels; warps 0-3 take columns [0, n_half), warps
+    // 4-7 the rest, each warp its own 32 lanes
+    {
+      const int j_lo = half == 0 ? 0 : n_half, j_hi = half == 0 ? n_half : n_tile;
 #pragma unroll 1
-    for (int j0 = 0; j0 < n_tile; j0 += 16) {
-      uint32_t r[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-          "%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)j0)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (vvalid) {
+      for (int j0 = j_lo; j0 < j_hi; j0 += 16) {
+        uint32_t r[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+            "%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)j0)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (vvalid) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int o = co0 + j0 + q;
-          if (o < O) {
-            float val = __uint_as_float(r[q]) + (a.bias != nullptr ? a.bias[o] : 0.f);
-            if (a.relu) val = fmaxf(val, 0.f);
-            if (o < a.oa) {
-              const int64_t idx = ((int64_t)b * a.oa + o) * V + vox;
-              if (a.mask_a != nullptr && !(a.mask_a[idx] > 0.f)) val = 0.f;
-              a.out_a[idx] = val;
-            } else {
-              a.out_b[((int64_t)b * a.ob + (o - a.oa)) * V + vox] = val;
+          for (int q = 0; q < 16; ++q) {
+            const int o = co0 + j0 + q;
+            if (o < O) {
+              float val = __uint_as_float(r[q]) + (a.bias != nullptr ? a.bias[o] : 0.f);
+              if (a.relu) val = fmaxf(val, 0.f);
+              if (o < a.oa) {
+                const int64_t idx = ((int64_t)b * a.oa + o) * V + vox;
+                if (a.mask_a != nullptr && !(a.mask_a[idx] > 0.f)) val = 0.f;
+                a.out_a[idx] = val;
+              } else {
+                a.out_b[((int64_t)b * a.ob + (o - a.oa)) * V + vox] = val;
+              }
             }
           }
         }
