@@ -55,10 +55,28 @@ __global__ void box_blur_kernel(const float* __restrict__ in, float* __restrict_
 }
 
 // The same filter with O(1) work per output pixel: a block owns one line, stages its N pixels in shared memory with
-// their float64 prefix sums (a block scan), and each output pixel is its partial first pixel, the prefix-sum
+// their prefix sums (a block scan, float32 pairs), and each output pixel is its partial first pixel, the prefix-sum
 // difference over the fully covered pixels and its partial last pixel, divided by the window length.
 constexpr int kScanThreads = 256;
 constexpr int kScanMaxN = 1024;
+
+// A float32 pair (hi, lo) that carries a sum to about 2^-40 of its magnitude: the prefix sums of the scan below are
+// kept this way instead of in float64, whose rate on this GPU is a small fraction of float32's.
+struct F2 {
+  float hi, lo;
+};
+
+// hi + lo of a + b exactly (Knuth's two-sum), then the pair renormalised
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bp = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+  const float t = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float hi = __fadd_rn(s, t);
+  return F2{hi, __fsub_rn(t, __fsub_rn(hi, s))};
+}
+
+__device__ __forceinline__ F2 f2_neg(F2 a) { return F2{-a.hi, -a.lo}; }
 
 __global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float* __restrict__ in,
                                                                      float* __restrict__ out, int64_t lines, int N,
@@ -66,8 +84,8 @@ __global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float
                                                                      int64_t os_k, int64_t os_l, int64_t os_p,
                                                                      WidthArgs wa) {
   __shared__ float x[kScanMaxN];
-  __shared__ double P[kScanMaxN + 1];   // P[j] = sum of x[0 .. j - 1]
-  __shared__ double warp_tot[kScanThreads / 32];
+  __shared__ float P_hi[kScanMaxN + 1], P_lo[kScanMaxN + 1];   // P[j] = sum of x[0 .. j - 1]
+  __shared__ F2 warp_tot[kScanThreads / 32];
   const int k = blockIdx.y;
   const int64_t line = blockIdx.x;
   const float* src = in + k * is_k + line * is_l;
@@ -76,24 +94,28 @@ __global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float
   // each thread sums a contiguous run of per = ceil(N / 256) pixels; a block-wide exclusive scan of the run sums
   const int per = (N + kScanThreads - 1) / kScanThreads;
   const int j0 = threadIdx.x * per, j1 = min(N, j0 + per);
-  double run = 0.0;
-  for (int j = j0; j < j1; ++j) run += (double)x[j];
+  F2 run{0.f, 0.f};
+  for (int j = j0; j < j1; ++j) run = f2_add(run, F2{x[j], 0.f});
   const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
-  double incl = run;
+  F2 incl = run;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const double y = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl += y;
+    const F2 y{__shfl_up_sync(0xffffffffu, incl.hi, off), __shfl_up_sync(0xffffffffu, incl.lo, off)};
+    if (lane >= off) incl = f2_add(incl, y);
   }
   if (lane == 31) warp_tot[warp] = incl;
   __syncthreads();
-  double base = 0.0;
-  for (int w = 0; w < warp; ++w) base += warp_tot[w];
-  double acc = base + incl - run;    // exclusive prefix of this thread's run
-  if (threadIdx.x == 0) P[0] = 0.0;
+  F2 base{0.f, 0.f};
+  for (int w = 0; w < warp; ++w) base = f2_add(base, warp_tot[w]);
+  F2 acc = f2_add(base, f2_add(incl, f2_neg(run)));    // exclusive prefix of this thread's run
+  if (threadIdx.x == 0) {
+    P_hi[0] = 0.f;
+    P_lo[0] = 0.f;
+  }
   for (int j = j0; j < j1; ++j) {
-    acc += (double)x[j];
-    P[j + 1] = acc;
+    acc = f2_add(acc, F2{x[j], 0.f});
+    P_hi[j + 1] = acc.hi;
+    P_lo[j + 1] = acc.lo;
   }
   __syncthreads();
   const float half = 0.5f * fmaxf(blur_width(wa, k), 1e-3f);
@@ -108,7 +130,9 @@ __global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float
       sum = fmaxf(hi - lo, 0.f) * x[a];
     } else {
       const float first = ((float)a + 1.f - lo) * x[a], last = (hi - (float)b) * x[b];
-      sum = (float)((double)first + (P[b] - P[a + 1]) + (double)last);
+      const F2 interior = f2_add(F2{P_hi[b], P_lo[b]}, F2{-P_hi[a + 1], -P_lo[a + 1]});
+      const F2 total = f2_add(f2_add(interior, F2{first, 0.f}), F2{last, 0.f});
+      sum = total.hi + total.lo;
     }
     dst[(int64_t)c * os_p] = sum / (hi - lo);
   }

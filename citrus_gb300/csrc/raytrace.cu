@@ -104,27 +104,35 @@ __device__ __forceinline__ Setup<T> ray_setup(const Box& b, const T p0[3], const
   return s;
 }
 
-// The same set-up with float64 only where it decides which voxels the line touches: the clipping parameters (the
-// reference's float64 slab test) and the entry and exit points relative to the box corner; the direction in voxel
-// units, the length and the fractional positions are float32 (their relative errors are those of the float32 walk).
-// FP64 is a small fraction of the float32 rate on this GPU, and the dense image rays need this set-up once per ray.
-__device__ __forceinline__ Setup<float> ray_setup_mixed(const Box& b, const double p0[3], const double p1[3]) {
-  Setup<float> s;
+// The constants of one oblique direction, shared by a block's rays (float64, formed once per block): the direction,
+// the segment d = 2 h omega / |omega| that every ray of the direction spans, its reciprocal components, the far
+// corner of the box and 1 / |omega|^2.
+struct DirConst {
+  double w[3];
   double d[3];
+  double inv_d[3];
+  double hi[3];
+  double inv_w2;
+  double h;
+};
+
+// The clipped set-up of a ray from p0 along the block's direction, the clip in float64 (so that a line in a face of
+// the box meets it or misses it as the float64 reference does) and the walk's set-up in float32: the clip divides by
+// nothing (the reciprocals are the block's), the exit point is p0 + d.
+__device__ __forceinline__ Setup<float> ray_setup_dir(const Box& b, const double p0[3], const DirConst& dc) {
+  Setup<float> s;
   double a_lo = 0, a_hi = 1;
   for (int a = 0; a < 3; ++a) {
-    d[a] = p1[a] - p0[a];
-    const double lo = b.lo[a], hi = add_rn(lo, mul_rn(b.delta[a], (double)b.n[a]));
-    if (d[a] != 0) {
-      const double inv = 1.0 / d[a];
-      const double t1 = (lo - p0[a]) * inv, t2 = (hi - p0[a]) * inv;
+    const double lo = b.lo[a], hi = dc.hi[a];
+    if (dc.d[a] != 0) {
+      const double t1 = (lo - p0[a]) * dc.inv_d[a], t2 = (hi - p0[a]) * dc.inv_d[a];
       a_lo = fmax(a_lo, fmin(t1, t2));
       a_hi = fmin(a_hi, fmax(t1, t2));
     } else if (!(p0[a] >= lo && p0[a] <= hi)) {
       a_hi = -1;  // parallel to this slab and outside it
     }
   }
-  const float df[3] = {(float)d[0], (float)d[1], (float)d[2]};
+  const float df[3] = {(float)dc.d[0], (float)dc.d[1], (float)dc.d[2]};
   const float len = sqrtf(df[0] * df[0] + df[1] * df[1] + df[2] * df[2]);
   s.hit = a_hi > a_lo && len > 0.f;
   if (!s.hit) {
@@ -135,13 +143,13 @@ __device__ __forceinline__ Setup<float> ray_setup_mixed(const Box& b, const doub
   for (int a = 0; a < 3; ++a) {
     const float delta = (float)b.delta[a];
     s.v[a] = df[a] / len / delta;
-    const float q = (float)(p0[a] + a_lo * d[a] - b.lo[a]) / delta;   // entry, in voxels from the corner
+    const float q = (float)(p0[a] + a_lo * dc.d[a] - b.lo[a]) / delta;   // entry, in voxels from the corner
     int i = (int)floorf(q);
     if (i < 0) i = 0;
     if (i > b.n[a] - 1) i = b.n[a] - 1;
     s.idx[a] = i;
     s.f[a] = fminf(fmaxf(q - (float)i, 0.f), 1.f);
-    int ie = (int)floorf((float)(p0[a] + a_hi * d[a] - b.lo[a]) / delta);   // exit voxel, clamped alike
+    int ie = (int)floorf((float)(p0[a] + a_hi * dc.d[a] - b.lo[a]) / delta);   // exit voxel, clamped alike
     if (ie < 0) ie = 0;
     if (ie > b.n[a] - 1) ie = b.n[a] - 1;
     s.cross[a] = ie > i ? ie - i : i - ie;
@@ -508,30 +516,37 @@ __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* _
                                                            int64_t os_r, int64_t os_col, int64_t cols) {
   const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int k = blockIdx.y;
-  // the direction's |omega|^2 and half-length, once per block (the block shares the direction)
-  __shared__ double s_dir[2];
+  // the direction's constants, once per block (the block shares the direction): float64 on this GPU runs at a small
+  // fraction of float32, so every division of the set-up is made here rather than per ray
+  __shared__ DirConst s_dc;
   if (threadIdx.x == 0) {
-    const double w0 = omegas[3 * k], w1 = omegas[3 * k + 1], w2z = omegas[3 * k + 2];
-    const double sq = add_rn(add_rn(mul_rn(w0, w0), mul_rn(w1, w1)), mul_rn(w2z, w2z));
-    s_dir[0] = sq;
-    s_dir[1] = half / sqrt(sq);
+    DirConst dc;
+    dc.w[0] = omegas[3 * k];
+    dc.w[1] = omegas[3 * k + 1];
+    dc.w[2] = omegas[3 * k + 2];
+    const double sq = add_rn(add_rn(mul_rn(dc.w[0], dc.w[0]), mul_rn(dc.w[1], dc.w[1])), mul_rn(dc.w[2], dc.w[2]));
+    dc.h = half / sqrt(sq);
+    dc.inv_w2 = 1.0 / sq;
+    for (int a = 0; a < 3; ++a) {
+      dc.d[a] = mul_rn(2.0 * dc.h, dc.w[a]);
+      dc.inv_d[a] = dc.d[a] != 0 ? 1.0 / dc.d[a] : 0.0;
+      dc.hi[a] = add_rn(b.lo[a], mul_rn(b.delta[a], (double)b.n[a]));
+    }
+    s_dc = dc;
   }
   __syncthreads();
   if (p >= P) return;
-  const double w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
+  const DirConst& dc = s_dc;
   const double px = pixels[3 * p], py = pixels[3 * p + 1], pz = pixels[3 * p + 2];
-  // the endpoints of ray_tracing.py:588-595, operation by operation
-  const double w2 = s_dir[0];
-  const double dot = add_rn(add_rn(mul_rn(cx - px, w[0]), mul_rn(cy - py, w[1])), mul_rn(cz - pz, w[2]));
-  const double cp = dot / w2;
-  const double h = s_dir[1];
-  const double tm = cp - h, tp = cp + h;
-  const double a[3] = {add_rn(px, mul_rn(tm, w[0])), add_rn(py, mul_rn(tm, w[1])), add_rn(pz, mul_rn(tm, w[2]))};
-  const double e[3] = {add_rn(px, mul_rn(tp, w[0])), add_rn(py, mul_rn(tp, w[1])), add_rn(pz, mul_rn(tp, w[2]))};
+  // the entry point of ray_tracing.py:588-595, its exit point the entry plus the direction's segment
+  const double dot = add_rn(add_rn(mul_rn(cx - px, dc.w[0]), mul_rn(cy - py, dc.w[1])), mul_rn(cz - pz, dc.w[2]));
+  const double tm = mul_rn(dot, dc.inv_w2) - dc.h;
+  const double a[3] = {add_rn(px, mul_rn(tm, dc.w[0])), add_rn(py, mul_rn(tm, dc.w[1])),
+                       add_rn(pz, mul_rn(tm, dc.w[2]))};
   const int nC = kC > 0 ? kC : C;
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
-  const Setup<float> st = ray_setup_mixed(b, a, e);
+  const Setup<float> st = ray_setup_dir(b, a, dc);
   if (st.hit) ray_walk<kC, false>(b, st, vol + (int64_t)k * field_stride, C, acc);
   const int64_t row = p / cols;
   float* o = out + (int64_t)k * os_k + row * os_r + (p - row * cols) * os_col;
