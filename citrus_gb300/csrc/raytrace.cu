@@ -249,6 +249,88 @@ __device__ __forceinline__ void ray_walk(const Box& b, const Setup<float>& s, co
   }
 }
 
+// ray_walk of one channel without compensation (the oblique projection), four steps at a time: the walk's geometry
+// never waits for a load, so the voxels and lengths of four steps are found first, their four gathers issued
+// together and the products summed in step order (the same sums as ray_walk).
+__device__ __forceinline__ float ray_walk_one_channel(const Box& b, const Setup<float>& s,
+                                                      const float* __restrict__ vol) {
+  float acc = 0.f;
+  int ix = s.idx[0], iy = s.idx[1], iz = s.idx[2];
+  float fx = s.f[0], fy = s.f[1], fz = s.f[2];
+  const float vx = s.v[0], vy = s.v[1], vz = s.v[2];
+  const float ivx = vx != 0.f ? 1.f / fabsf(vx) : INFINITY;
+  const float ivy = vy != 0.f ? 1.f / fabsf(vy) : INFINITY;
+  const float ivz = vz != 0.f ? 1.f / fabsf(vz) : INFINITY;
+  const int stx = vx > 0.f ? 1 : -1, sty = vy > 0.f ? 1 : -1, stz = vz > 0.f ? 1 : -1;
+  int cx = s.cross[0], cy = s.cross[1], cz = s.cross[2];  // crossings left along each axis
+  float t = 0.f, t_comp = 0.f;  // travelled distance, Kahan-compensated
+  const int max_steps = b.n[0] + b.n[1] + b.n[2] + 3;
+  int step = 0;
+  bool done = false;
+  while (!done) {
+    int64_t at[4];
+    float len[4];
+    int n = 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (done || step >= max_steps) {
+        done = true;
+        continue;
+      }
+      ++step;
+      const float dx = cx > 0 ? (vx > 0.f ? 1.f - fx : fx) * ivx : INFINITY;
+      const float dy = cy > 0 ? (vy > 0.f ? 1.f - fy : fy) * ivy : INFINITY;
+      const float dz = cz > 0 ? (vz > 0.f ? 1.f - fz : fz) * ivz : INFINITY;
+      int axis = 0;
+      float dt = dx;
+      if (dy < dt) { dt = dy; axis = 1; }
+      if (dz < dt) { dt = dz; axis = 2; }
+      const float remaining = (s.total - t) + t_comp;
+      const bool last = dt >= remaining;
+      if (last) dt = fmaxf(remaining, 0.f);
+      at[u] = (int64_t)(iy * b.n[0] + ix) * b.n[2] + iz;
+      len[u] = dt;
+      n = u + 1;
+      if (last) {
+        done = true;
+        continue;
+      }
+      {  // t += dt, compensated
+        const float y = dt - t_comp;
+        const float tt = t + y;
+        t_comp = (tt - t) - y;
+        t = tt;
+      }
+      fx = fminf(fmaxf(fmaf(dt, vx, fx), 0.f), 1.f);
+      fy = fminf(fmaxf(fmaf(dt, vy, fy), 0.f), 1.f);
+      fz = fminf(fmaxf(fmaf(dt, vz, fz), 0.f), 1.f);
+      if (axis == 0) {
+        ix += stx;
+        --cx;
+        fx = stx > 0 ? 0.f : 1.f;
+        if (ix < 0 || ix >= b.n[0]) done = true;
+      } else if (axis == 1) {
+        iy += sty;
+        --cy;
+        fy = sty > 0 ? 0.f : 1.f;
+        if (iy < 0 || iy >= b.n[1]) done = true;
+      } else {
+        iz += stz;
+        --cz;
+        fz = stz > 0 ? 0.f : 1.f;
+        if (iz < 0 || iz >= b.n[2]) done = true;
+      }
+    }
+    float q[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) q[u] = u < n ? __ldg(vol + at[u]) : 0.f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (u < n) acc = fmaf(len[u], q[u], acc);
+  }
+  return acc;
+}
+
 template <int kC, bool kCompensated, typename T>
 __device__ __forceinline__ void integrate(const Box& b, const T p0[3], const T p1[3], const float* vol, int C,
                                           float* acc) {
@@ -471,7 +553,35 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
   int64_t cur = v;
   float prev = 0.f;
-  for (int j = 0; j <= exit_j && j < E && prev < t_end; ++j) {
+  int j = 0;
+  if (kC == 2) {
+    // four crossings at a time: the four gathers are issued before their sums (the crossing table gives every step's
+    // voxel in advance); a step at or past the ray's end adds exactly zero, as the plain loop's exit would
+    const int jmax = min(exit_j + 1, E);
+    for (; j + 4 <= jmax && prev < t_end; j += 4) {
+      const int64_t c1 = cur + dv[j], c2 = c1 + dv[j + 1], c3 = c2 + dv[j + 2];
+      const float2 q0 = __ldg(reinterpret_cast<const float2*>(vol + cur * 2));
+      const float2 q1 = __ldg(reinterpret_cast<const float2*>(vol + c1 * 2));
+      const float2 q2 = __ldg(reinterpret_cast<const float2*>(vol + c2 * 2));
+      const float2 q3 = __ldg(reinterpret_cast<const float2*>(vol + c3 * 2));
+      const float t0 = t_cross[j], t1 = t_cross[j + 1], t2 = t_cross[j + 2], t3 = t_cross[j + 3];
+      const float s0 = prev < t_end ? fminf(t0, t_end) - prev : 0.f;
+      const float s1 = t0 < t_end ? fminf(t1, t_end) - t0 : 0.f;
+      const float s2 = t1 < t_end ? fminf(t2, t_end) - t1 : 0.f;
+      const float s3 = t2 < t_end ? fminf(t3, t_end) - t2 : 0.f;
+      acc[0] = fmaf(s0, q0.x, acc[0]);
+      acc[kC > 1 ? 1 : 0] = fmaf(s0, q0.y, acc[kC > 1 ? 1 : 0]);
+      acc[0] = fmaf(s1, q1.x, acc[0]);
+      acc[kC > 1 ? 1 : 0] = fmaf(s1, q1.y, acc[kC > 1 ? 1 : 0]);
+      acc[0] = fmaf(s2, q2.x, acc[0]);
+      acc[kC > 1 ? 1 : 0] = fmaf(s2, q2.y, acc[kC > 1 ? 1 : 0]);
+      acc[0] = fmaf(s3, q3.x, acc[0]);
+      acc[kC > 1 ? 1 : 0] = fmaf(s3, q3.y, acc[kC > 1 ? 1 : 0]);
+      prev = t3;
+      cur = c3 + dv[j + 3];
+    }
+  }
+  for (; j <= exit_j && j < E && prev < t_end; ++j) {
     const float tj = t_cross[j];
     const float seg = fminf(tj, t_end) - prev;
     const float* vox = vol + cur * nC;
@@ -547,7 +657,10 @@ __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* _
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
   const Setup<float> st = ray_setup_dir(b, a, dc);
-  if (st.hit) ray_walk<kC, false>(b, st, vol + (int64_t)k * field_stride, C, acc);
+  if (st.hit) {
+    if (kC == 1) acc[0] = ray_walk_one_channel(b, st, vol + (int64_t)k * field_stride);
+    else ray_walk<kC, false>(b, st, vol + (int64_t)k * field_stride, C, acc);
+  }
   const int64_t row = p / cols;
   float* o = out + (int64_t)k * os_k + row * os_r + (p - row * cols) * os_col;
   for (int c = 0; c < nC; ++c) o[(int64_t)c * os_c] = acc[c];
