@@ -9,8 +9,9 @@ gets the caller's default, untimed.
 
 Tuned here:
 
-* ``small_k_gemm``: the float32 small-K product's kernel — the streaming forms against the shared-memory tiled
-  kernel at each of its tile heights (``citrus_small_k_gemm_config``), timed into a scratch output;
+* ``small_k_gemm``: the small-K product's kernel — the float32 streaming forms against the shared-memory tiled
+  kernel at each of its tile heights (``citrus_small_k_gemm_config``) and, in the bf16x3 precision, the tcgen05
+  bf16 hi/lo product, timed into a scratch output;
 * ``sweep``: views per persistent sweep launch of the batched step and lanes per sweep thread
   (``citrus_sweep_persistent_config``), timed on a zero store of that many views (the sweep's work does not depend
   on the values), the per-view time compared.
@@ -123,24 +124,34 @@ def tuner() -> Autotuner:
 GEMM_CANDIDATES = ([1, 0], [2, 1], [2, 2], [2, 4], [2, 8], [2, 16])   # (variant, tile row groups)
 
 
-def small_k_gemm_config(A, B, C, M: int, K: int, J: int, batch: int, sb: int, sc: int, accumulate: bool) -> list:
-    """(variant, tile rows) of the float32 small-K product for this shape, tuned into a scratch output."""
-    key = Autotuner.key("small_k_gemm", A.device, M=M, K=K, J=J, batch=batch, acc=int(bool(accumulate)),
+TENSOR_CORES = [3, 0]   # the tcgen05 bf16 hi/lo product, a candidate of the bf16x3 precision
+
+
+def small_k_gemm_config(A, B, C, M: int, K: int, J: int, batch: int, sb: int, sc: int, accumulate: bool,
+                        tensor_cores=None) -> list:
+    """(variant, tile rows) of the small-K product for this shape, tuned into a scratch output: the float32 forms,
+    and the tensor-core product ([3, 0]) when ``tensor_cores(out, ld_out, stride_out)`` runs it."""
+    key = Autotuner.key("small_k_gemm" + ("_bf16x3" if tensor_cores else ""), A.device, M=M, K=K, J=J, batch=batch,
+                        acc=int(bool(accumulate)),
                         aligned=int(J % 4 == 0 and B.stride(1) % 4 == 0 and C.stride(1) % 4 == 0))
     entry = tuner().table.get(key)
     if entry is not None:
         return entry["choice"]
     if torch.cuda.is_current_stream_capturing():
-        return [0, 0]
+        return list(TENSOR_CORES) if tensor_cores else [0, 0]
     scratch = torch.empty((batch, M, J), device=A.device, dtype=torch.float32)
     stream = _lib.stream_handle(A.device)
 
     def run(c):
+        if c == TENSOR_CORES:
+            tensor_cores(scratch, J, M * J if batch > 1 else 0)
+            return
         _lib.call("citrus_small_k_gemm_config", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1),
                   scratch.data_ptr(), J, M, K, J, batch, sb, M * J if batch > 1 else 0, int(bool(accumulate)),
                   int(c[0]), int(c[1]), stream)
 
-    choice = tuner().choose(key, GEMM_CANDIDATES, run, [0, 0])
+    candidates = list(GEMM_CANDIDATES) + ([list(TENSOR_CORES)] if tensor_cores and M <= 128 * 8 else [])
+    choice = tuner().choose(key, candidates, run, list(TENSOR_CORES) if tensor_cores else [0, 0])
     del scratch
     return choice
 

@@ -137,13 +137,14 @@ PRECISIONS = ("fp32", "bf16x3")
 
 
 def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, precision: str = "fp32",
-                 error_word: Optional[Tensor] = None) -> Tensor:
+                 error_word: Optional[Tensor] = None, tensor_cores_only: bool = False) -> Tensor:
     """``C (=|+=) A @ B`` for A [M, K] and B, C [.., K or M, J] row-major 2-D (or batched 3-D) views.
 
     B and C may be strided views whose last axis is contiguous. ``precision`` "fp32" multiplies in float32 on the CUDA
-    cores; "bf16x3" splits both operands into bfloat16 high and low parts and accumulates A_hi B_hi + A_hi B_lo +
-    A_lo B_hi in float32 on the tcgen05 tensor cores (M <= 128, K <= 128; ``error_word``, an int32 device tensor,
-    becomes non-zero if a wait for the tensor cores ran out).
+    cores; "bf16x3" allows the tcgen05 tensor-core product, which splits both operands into bfloat16 high and low
+    parts and accumulates A_hi B_hi + A_hi B_lo + A_lo B_hi in float32 (``error_word``, an int32 device tensor,
+    becomes non-zero if a wait for the tensor cores ran out), where the autotuner finds it faster than the float32
+    forms for the shape; ``tensor_cores_only`` takes it whatever the timing (for checks of that kernel).
     """
     if precision not in PRECISIONS:
         raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
@@ -164,24 +165,36 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, prec
         raise ValueError("B and C need a contiguous last axis")
     sb, sc = (B.stride(0), C.stride(0)) if batch > 1 else (0, 0)
     stream = _lib.stream_handle(A.device)
-    if precision == "fp32":
-        from .autotune import small_k_gemm_config
-
-        variant, tile = small_k_gemm_config(A, B, C, M, K, J, batch, sb, sc, accumulate)
-        _lib.call("citrus_small_k_gemm_config", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
-                  C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), int(variant), int(tile), stream)
-        return C
-    # the tensor-core product takes at most 128 rows and 128 inner terms per call; inner dimensions above 64 go in
-    # steps of 64 (partial sums added), which keeps the split operands of a CTA small enough for three per SM
     err = None if error_word is None else error_word.data_ptr()
-    step = K if K <= 64 else 64
-    for r0 in range(0, M, 128):
-        rows = min(128, M - r0)
-        for k0 in range(0, K, step):
-            inner = min(step, K - k0)
-            _lib.call("citrus_small_k_gemm_bf16x3", A[r0:, k0:].data_ptr(), A.stride(0),
-                      B[:, k0:].data_ptr(), B.stride(1), C[:, r0:].data_ptr(), C.stride(1), rows, inner, J, batch,
-                      sb, sc, int(bool(accumulate) or k0 > 0), err, stream)
+
+    def tensor_cores(out: Tensor, ld_out: int, s_out: int) -> None:
+        # at most 128 rows and 128 inner terms per call; inner dimensions above 64 go in steps of 64 (partial sums
+        # added), which keeps the split operands of a CTA small enough for three per SM
+        step = K if K <= 64 else 64
+        for r0 in range(0, M, 128):
+            rows = min(128, M - r0)
+            for k0 in range(0, K, step):
+                inner = min(step, K - k0)
+                _lib.call("citrus_small_k_gemm_bf16x3", A[r0:, k0:].data_ptr(), A.stride(0),
+                          B[:, k0:].data_ptr(), B.stride(1), out.data_ptr() + 4 * r0 * ld_out, ld_out, rows, inner,
+                          J, batch, sb, s_out, int(bool(accumulate) or k0 > 0), err, stream)
+
+    if tensor_cores_only:
+        if precision != "bf16x3":
+            raise ValueError("tensor_cores_only needs precision='bf16x3'")
+        tensor_cores(C, C.stride(1), sc)
+        return C
+    from .autotune import small_k_gemm_config
+
+    # the kernel: the autotuner's choice for this shape among the float32 forms, and in "bf16x3" also the
+    # tensor-core product (a float32 form is at least as accurate, so it may serve the bf16x3 precision too)
+    variant, tile = small_k_gemm_config(A, B, C, M, K, J, batch, sb, sc, accumulate,
+                                        tensor_cores=tensor_cores if precision == "bf16x3" else None)
+    if variant == 3:
+        tensor_cores(C, C.stride(1), sc)
+        return C
+    _lib.call("citrus_small_k_gemm_config", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
+              C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), int(variant), int(tile), stream)
     return C
 
 

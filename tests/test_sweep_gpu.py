@@ -130,7 +130,8 @@ def test_bf16x3_tensor_core_gemm_error_against_float64(cuda_device, M, K, J, bat
     dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
     C = dev(C0)
     err = torch.zeros(1, dtype=torch.int32, device=cuda_device)
-    kernels.small_k_gemm(dev(A), dev(B), C, accumulate=accumulate, precision="bf16x3", error_word=err)
+    kernels.small_k_gemm(dev(A), dev(B), C, accumulate=accumulate, precision="bf16x3", error_word=err,
+                         tensor_cores_only=True)
     torch.cuda.synchronize()
     assert int(err[0]) == 0
     scale = np.abs(A).max() * np.abs(B).max() * K
