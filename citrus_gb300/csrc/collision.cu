@@ -17,6 +17,7 @@
 // warp reads and writes 32 consecutive points of one group. The transfer table is laid out [M, N_eta, G_out, G_in]
 // (downscatter only, zero above the diagonal), so the 32 B row of one outgoing group at one node is one vector load.
 #include <math.h>
+#include <type_traits>
 #include <stdlib.h>
 
 #include "common.cuh"
@@ -464,7 +465,8 @@ __device__ void stage_window(const Table& tb, bool valid, float ux, float uy, fl
 }
 
 // S_FC of group g at one point for one direction, rows from the window (win_lo >= 0) or from global memory
-template <int kGP, int kMM>
+// kWindow: 1 the rows are in the block's shared-memory window, 2 in global memory, 0 decided by win_lo >= 0
+template <int kGP, int kMM, int kWindow = 0>
 __device__ __forceinline__ float fc_group(const Table& tb, const float* s_tab, int win_lo, int i0, float w, int g,
                                           const float* rho, const float* phi) {
   const int G = tb.G, RS = window_row_stride(G);
@@ -474,7 +476,7 @@ __device__ __forceinline__ float fc_group(const Table& tb, const float* s_tab, i
     const float r = rho[m];
     if (m >= tb.M || r == 0.f) continue;
     float a0, a1;
-    if (win_lo >= 0) {
+    if (kWindow == 1 || (kWindow == 0 && win_lo >= 0)) {
       const float* row0 = s_tab + ((i0 - win_lo) * tb.M + m) * RS + g * G;
       a0 = row_dot<kGP, true>(row0, phi, G);
       a1 = row_dot<kGP, true>(row0 + tb.M * RS, phi, G);
@@ -572,69 +574,82 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
                emission_window_bytes(kDirs));
   const int win_lo = s_window[0];
 
-  for (int dd = 0; dd < nd; ++dd) {
-    const int d = d0 + dd;
-    float e = 0.f;
-    if (valid && gvalid) {
-      const float ox = s_om[dd][0], oy = s_om[dd][1], oz = s_om[dd][2];
-      const float cosine = ux * ox + uy * oy + uz * oz;
-      int i0;
-      float w;
-      table_position(tb, cosine, i0, w);
-      const float offset = pg.f > 1 ? oy * offy + ox * offx + oz * offz : 0.f;  // one point per cell: its centre
-      const float src = fc_group<kGP, kMM>(tb, s_tab, win_lo, i0, w, g, rho, phi);
-      const int64_t kc = ((int64_t)d * NC + cell) * G + g;
-      float smc = 0.f;
-      if (kFused) {
+  // running pointers to this lane's element of direction d0 + dd (advanced once per direction)
+  const float* mp = kFused ? nullptr : multiple + ((int64_t)d0 * NC + cell) * G + g;
+  const float* tp = tau_mu != nullptr ? tau + ((int64_t)d0 * NC + cell) * TM : tau + ((int64_t)d0 * NC + cell) * G + g;
+  const int64_t mp_step = NC * G, tp_step = tau_mu != nullptr ? NC * TM : NC * G;
+  float* op = signal_weight != nullptr ? out + (int64_t)d0 * in.V + v : out + ((int64_t)d0 * in.V + v) * G + g;
+  const int64_t op_step = signal_weight != nullptr ? in.V : in.V * G;
+  // the table window (or, where a block's nodes do not fit it, the table in global memory) is fixed for the block:
+  // the direction loop is compiled for each case, with no test of it per direction
+  auto directions = [&](auto windowed) {
+    constexpr bool kWin = decltype(windowed)::value;
+    for (int dd = 0; dd < nd; ++dd) {
+      float e = 0.f;
+      if (valid && gvalid) {
+        const float ox = s_om[dd][0], oy = s_om[dd][1], oz = s_om[dd][2];
+        const float cosine = ux * ox + uy * oy + uz * oz;
+        int i0;
+        float w;
+        table_position(tb, cosine, i0, w);
+        const float offset = pg.f > 1 ? oy * offy + ox * offx + oz * offz : 0.f;  // one point per cell: its centre
+        const float src = fc_group<kGP, kMM, kWin ? 1 : 2>(tb, s_tab, win_lo, i0, w, g, rho, phi);
+        float smc = 0.f;
+        if (kFused) {
 #pragma unroll
-        for (int n = 0; n < (kFused ? kRegMoments : 1); n += 4) {
-          const float4 y = *reinterpret_cast<const float4*>(&s_y[kFused ? dd : 0][n]);
-          smc = fmaf(y.x, tmom[n], smc);
-          if (n + 1 < kRegMoments) smc = fmaf(y.y, tmom[n + 1], smc);
-          if (n + 2 < kRegMoments) smc = fmaf(y.z, tmom[n + 2], smc);
-          if (n + 3 < kRegMoments) smc = fmaf(y.w, tmom[n + 3], smc);
+          for (int n = 0; n < (kFused ? kRegMoments : 1); n += 4) {
+            const float4 y = *reinterpret_cast<const float4*>(&s_y[kFused ? dd : 0][n]);
+            smc = fmaf(y.x, tmom[n], smc);
+            if (n + 1 < kRegMoments) smc = fmaf(y.y, tmom[n + 1], smc);
+            if (n + 2 < kRegMoments) smc = fmaf(y.z, tmom[n + 2], smc);
+            if (n + 3 < kRegMoments) smc = fmaf(y.w, tmom[n + 3], smc);
+          }
+          for (int n = kRegMoments; n < NS; ++n)
+            smc = fmaf(s_y[kFused ? dd : 0][n], __ldg(moments + ((int64_t)n * NC + cell) * G + g), smc);
+        } else {
+          smc = __ldg(mp);
         }
-        for (int n = kRegMoments; n < NS; ++n)
-          smc = fmaf(s_y[kFused ? dd : 0][n], __ldg(moments + ((int64_t)n * NC + cell) * G + g), smc);
-      } else {
-        smc = __ldg(multiple + kc);
+        float t;
+        if (tau_mu != nullptr) {  // sum_m mu[m, g] P_m, in material order
+          t = 0.f;
+#pragma unroll
+          for (int m = 0; m < kMM; ++m)
+            if (m < TM) t = fmaf(tmu[m], __ldg(tp + m), t);
+        } else {
+          t = __ldg(tp);
+        }
+        const float depth = pg.f > 1 ? fmaxf(t - muc * offset, 0.f) : fmaxf(t, 0.f);
+        e = (src + smc) * expf(-depth);
       }
-      float t;
-      if (tau_mu != nullptr) {  // sum_m mu[m, g] P_m, in material order
-        const float* pm = tau + ((int64_t)d * NC + cell) * TM;
-        t = 0.f;
+      // group sums over the kGP lanes of the point (in group order), then the warp's points
+      float tot = e, sgl = signal_weight != nullptr ? s_sw[dd][g] * e : 0.f;
 #pragma unroll
-        for (int m = 0; m < kMM; ++m)
-          if (m < TM) t = fmaf(tmu[m], __ldg(pm + m), t);
-      } else {
-        t = __ldg(tau + kc);
+      for (int off = 1; off < kGP; off <<= 1) {
+        tot += __shfl_xor_sync(0xffffffffu, tot, off);
+        sgl += __shfl_xor_sync(0xffffffffu, sgl, off);
       }
-      const float depth = pg.f > 1 ? fmaxf(t - muc * offset, 0.f) : fmaxf(t, 0.f);
-      e = (src + smc) * expf(-depth);
-    }
-    // group sums over the kGP lanes of the point (in group order), then the warp's points
-    float tot = e, sgl = signal_weight != nullptr ? s_sw[dd][g] * e : 0.f;
+      if (signal_weight != nullptr) {
+        if (g == 0 && valid) *op = sgl;
+      } else if (valid && gvalid) {
+        *op = e;
+      }
+      float a = (g == 0) ? tot : 0.f, b = (g == 0) ? tot * h : 0.f;
 #pragma unroll
-    for (int off = 1; off < kGP; off <<= 1) {
-      tot += __shfl_xor_sync(0xffffffffu, tot, off);
-      sgl += __shfl_xor_sync(0xffffffffu, sgl, off);
+      for (int off = kGP; off < 32; off <<= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+      }
+      if (lane == 0) {
+        s_sum[dd][warp][0] = a;
+        s_sum[dd][warp][1] = b;
+      }
+      if (!kFused) mp += mp_step;
+      tp += tp_step;
+      op += op_step;
     }
-    if (signal_weight != nullptr) {
-      if (g == 0 && valid) out[(int64_t)d * in.V + v] = sgl;
-    } else if (valid && gvalid) {
-      out[((int64_t)d * in.V + v) * G + g] = e;
-    }
-    float a = (g == 0) ? tot : 0.f, b = (g == 0) ? tot * h : 0.f;
-#pragma unroll
-    for (int off = kGP; off < 32; off <<= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, off);
-      b += __shfl_xor_sync(0xffffffffu, b, off);
-    }
-    if (lane == 0) {
-      s_sum[dd][warp][0] = a;
-      s_sum[dd][warp][1] = b;
-    }
-  }
+  };
+  if (win_lo >= 0) directions(std::true_type{});
+  else directions(std::false_type{});
   __syncthreads();
   if (tid < 2 * nd) {
     const int dd = tid / 2, which = tid % 2;
