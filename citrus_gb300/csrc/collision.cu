@@ -367,15 +367,14 @@ __global__ void fc_sums_kernel(FCInputs in, Table tb, PointGrid pg, const float*
 // e = (S_FC + S_MC,cell) exp(-max(0, tau_cell - mu_cell omega . (r - r_cell))), written voxel-major [k, V, G] (or the
 // weighted group sum [k, V] with signal weights), and per block the sums of e and e h (h = panel height of the point).
 //
-// A block is 32 points (threadIdx.x) by the G groups (threadIdx.y) by kEmitDirs directions: a warp reads 32
-// consecutive cells of one group (coalesced [K, G, NC] loads), the point's inputs are loaded once for all of the
-// block's directions, and the transfer rows of the eta nodes that the block's points and directions touch are staged
+// A block is 32 points by the G groups (a warp holds 32 / G points with their groups in adjacent lanes) by 16, 32 or
+// 64 directions (emission_dirs): the [K, NC, G] loads of a warp are coalesced, the point's inputs are loaded once for
+// all of the block's directions, and the transfer rows of the eta nodes that the block's points and directions touch are staged
 // in shared memory (the window). S_MC is either read ([K, G, NC], the reference's interface) or formed from the
 // scattering-source moments of the point's cell held in registers, T[n, g, cell] for n < N_sh, and the harmonics of
 // the block's directions in shared memory. The per-block sums are a fixed-order warp butterfly and a fixed-order sum
 // over the groups: deterministic.
 constexpr int kEmitPoints = 32;
-constexpr int kEmitDirs = 16;
 constexpr int kMaxMoments = 64;
 constexpr int kRegMoments = 36;  // scattering-source moments held in registers (P5); more are read per direction
 
@@ -804,14 +803,13 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
     FCInputs in, PointGrid pg, const float* __restrict__ omegas, int K, const float* __restrict__ cache,
     const int32_t* __restrict__ cache_index, const float* __restrict__ scale, const float* __restrict__ beta,
     float slope_scale, float* __restrict__ out, int64_t out_k_stride) {
-  __shared__ float4 s_tile[kEmitPoints * kGP];
+  // thread (cell, group) with the group fastest: a warp's float4 outputs [cell, group, 4] are contiguous
   const int G = (int)(blockDim.y);
-  const int g = threadIdx.y, lane = threadIdx.x;
-  const int nthreads = kEmitPoints * G, tid = g * kEmitPoints + lane;
+  const int tid = threadIdx.y * kEmitPoints + threadIdx.x;
+  const int lane = tid / G, g = tid - lane * G;
   const int64_t NC = (int64_t)pg.Rc * pg.Cc * pg.Sc;
   const int64_t c0 = (int64_t)blockIdx.x * kEmitPoints;
   const int64_t c = c0 + lane;
-  const int ncells = (int)min((int64_t)kEmitPoints, NC - c0);
   const bool valid = c < NC;
   const int F = pg.f;
   int ic = 0, jc = 0, kc = 0;
@@ -834,15 +832,14 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
     be1 = __ldg(beta + (int64_t)g * in.V + v1);
   }
   for (int d = blockIdx.y * kFcBatch; d < dlast; ++d) {
+    if (!valid) break;
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (valid && F == 1) {
-      const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+    const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+    const float* src = cache + (int64_t)__ldg(cache_index + d) * G * in.V + (int64_t)g * in.V;
+    if (F == 1) {
       const float cosine = u1x * ox + u1y * oy + u1z * oz;
-      const float* src = cache + (int64_t)__ldg(cache_index + d) * G * in.V + (int64_t)g * in.V;
       r.x = __ldg(src + v1) * sc1 * (1.f + be1 * cosine) * inv;
-    } else if (valid) {
-      const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
-      const float* src = cache + (int64_t)__ldg(cache_index + d) * G * in.V + (int64_t)g * in.V;
+    } else {
       float m0 = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
       for (int a = 0; a < F; ++a) {      // rows (y)
         for (int b = 0; b < F; ++b) {    // cols (x)
@@ -867,11 +864,7 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
       r.z = my * (inv * slope_scale);
       r.w = mz * (inv * slope_scale);
     }
-    s_tile[lane * G + g] = r;
-    __syncthreads();
-    float4* o = reinterpret_cast<float4*>(out + d * out_k_stride + c0 * G * 4);
-    for (int q = tid; q < ncells * G; q += nthreads) o[q] = s_tile[q];
-    __syncthreads();
+    reinterpret_cast<float4*>(out + d * out_k_stride)[c * G + g] = r;
   }
 }
 
