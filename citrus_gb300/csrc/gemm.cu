@@ -318,6 +318,7 @@ int launch_stream(const float* A, int64_t lda, const float* B, int64_t ldb, floa
                   int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, cudaStream_t s) {
   if (K <= 16) return launch_cols<16, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (K <= 32) return launch_cols<32, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
+  if (K <= 36) return launch_cols<36, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (K <= 48) return launch_cols<48, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (K <= 64) return launch_cols<64, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
   if (M <= 16) return launch_rows<16, kPair, kAcc>(A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c, s);
