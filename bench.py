@@ -288,7 +288,7 @@ def run_reference(args):
         line = {"metric": STEP_METRIC, "value": value, "unit": "ms/view", "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
                 "dtype": "f64", "data": "synthetic (seeded phantom and library)",
-                "config": {"workload": step_workload_name(args.cells, 60, args.batch)}, "cpu_baseline": base,
+                "config": {"workload": step_workload_name(args.cells, 60, args.batch, args.graph)}, "cpu_baseline": base,
                 "e2e": {"value": value, "unit": "ms/view", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
