@@ -12,9 +12,10 @@ Tuned here:
 * ``small_k_gemm``: the small-K product's kernel — the float32 streaming forms against the shared-memory tiled
   kernel at each of its tile heights (``citrus_small_k_gemm_config``) and, in the bf16x3 precision, the tcgen05
   bf16 hi/lo product, timed into a scratch output;
-* ``sweep``: views per persistent sweep launch of the batched step and lanes per sweep thread
-  (``citrus_sweep_persistent_config``), timed on a zero store of that many views (the sweep's work does not depend
-  on the values), the per-view time compared.
+* ``sweep``: views per persistent sweep launch of the batched step and the form of the sweep threads
+  (``citrus_sweep_persistent_config``), timed on a store of ones of that many views (the sweep's memory traffic
+  does not depend on the values; non-zero moments keep the divisions on their usual path), the per-view time
+  compared.
 """
 
 from __future__ import annotations
@@ -157,14 +158,15 @@ def small_k_gemm_config(A, B, C, M: int, K: int, J: int, batch: int, sb: int, sc
 
 
 VIEW_CANDIDATES = (1, 2, 4, 8)
-# lanes-per-thread forms of the persistent sweep: one lane with the registers capped for 5 (form 1), 6 (form 3) or
-# 8 (form 5) blocks of 256 threads per SM, or 2 lanes loaded before they are solved (form 2)
-UNROLL_CANDIDATES = (1, 3, 5, 2)
+# thread forms of the persistent sweep (each thread solves its lane in every view): one view at a time with the
+# registers capped for 5 (form 1), 6 (form 3) or 4 (form 5) blocks of 256 threads per SM, or the loads of 2 (form 2)
+# or 4 (form 4) views issued before their solves
+UNROLL_CANDIDATES = (1, 3, 5, 2, 4)
 
 
 def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> tuple:
     """(views per persistent sweep launch, lanes per thread) for ``views`` views on this grid: the per-view time of
-    the sweep on a zero store of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device
+    the sweep on a store of ones of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device
     memory) in each lanes-per-thread form; the first (fewest views) within 3 % of the fastest."""
     from . import kernels
 
@@ -184,7 +186,7 @@ def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> 
             if b not in stores:
                 stores.clear()
                 torch.cuda.empty_cache()
-                stores[b] = torch.zeros(b, 8, D8, N, Q, device=device)
+                stores[b] = torch.ones(b, 8, D8, N, Q, device=device)  # non-zero moments, as in a real step
             kernels.sweep_planes(ctx.flat_index, stores[b], mu_cells, ctx.c, method="persistent", lanes_per_thread=u)
 
         tuner().choose(key, candidates, run, list(default), slack=0.03, per_unit=lambda c: float(c[0]))

@@ -2,10 +2,11 @@
 // diagonal wavefront plane, in place in the chunk's cell-major store [views, 8, Dc, N, 4G].
 //
 // The cell equations are those of citrus/scatter_solver/linear_discontinuous_cell.py:14-87 (right-hand sides from the
-// source and the three upstream neighbours, then the closed-form 4 x 4 solve), evaluated term by term in float32 with
-// IEEE division. Two drivers share the lane body: one launch per plane (the reference's plan,
-// sweep_kernels.py:265-290) and one persistent cooperative launch that walks all planes with a bounded grid barrier
-// between them, so a whole chunk is a single launch.
+// source and the three upstream neighbours, then the closed-form 4 x 4 solve), evaluated term by term in float32: the
+// coefficients of a lane with IEEE division, the per-view quotients as products with correctly rounded reciprocals.
+// Two drivers share the lane body: one launch per plane (the reference's plan, sweep_kernels.py:265-290) and one
+// persistent cooperative launch that walks all planes with a bounded grid barrier between them, so a whole chunk is a
+// single launch.
 #include "common.cuh"
 #include <mutex>
 
@@ -15,137 +16,155 @@ namespace {
 constexpr int kThreads = 256;
 
 template <bool kCoherent>
-__device__ __forceinline__ float4 load4(const float* p) {
-  if (kCoherent) return __ldcg(reinterpret_cast<const float4*>(p));  // L2 only: written by other SMs this launch
-  return *reinterpret_cast<const float4*>(p);
+__device__ __forceinline__ float4 load4(const float4* p) {
+  if (kCoherent) return __ldcg(p);  // L2 only: written by other SMs this launch
+  return *p;
 }
 
-// The inputs of one lane: entry e of the plane, direction d of the chunk, group g, view v. Upstream neighbours lie on
-// the previous plane (already swept); an upstream index N is a vacuum face and reads zeros.
-struct LaneIn {
-  float4 s, X, Y, Z;  // source moments, and (psi0, psi_x, psi_y, psi_z) of the x, y, z upstream neighbours
-  float cx, cy, cz, m;
-  int o;
-  float* dst;
+// The view-independent part of one lane (entry e of the plane, direction d of the chunk, group g): the octant signs,
+// the direction's c_a, every coefficient of the 4 x 4 solve that depends on c and the cell's attenuation only, and
+// the float4 positions within one view's store of the cell and of its three upstream neighbours (upstream neighbours
+// lie on the previous plane, already swept; kVacuum marks a vacuum face, which reads zeros). The views of a launch
+// share it: a thread computes it once and solves the lane in every view.
+constexpr uint32_t kVacuum = 0xffffffffu;
+
+struct LaneCoef {
+  float sx, sy, sz, cx, cy, cz;
+  float k3x, k3y, k3z;  // 3 s_a c_a
+  float rdx, rdy, rdz;  // 1 / d_a, d_a = 3 c_a + sum_{b != a} c_b + m
+  float qsx, qsy, qsz;  // s_a c_a / d_a
+  float rden;           // 1 / (sum_a c_a + m + 3 sum_a c_a q_a)
+  uint32_t at, ax, ay, az;
 };
 
-template <int kG, bool kCoherent>
-__device__ __forceinline__ void gather_lane(int64_t lane, LaneIn& in, float* __restrict__ store,
-                                            const float* __restrict__ mu, const float* __restrict__ c,
-                                            const int* __restrict__ octant, const int* __restrict__ cell,
-                                            const int* __restrict__ upstream, int64_t start, int64_t E, int64_t N,
-                                            int G_runtime, int64_t Dc, int64_t view_stride) {
-  const int G = kG > 0 ? kG : G_runtime;
-  const int g = (int)(lane % G);
-  int64_t t = lane / G;
-  const int64_t d = t % Dc;
-  t /= Dc;
-  const int64_t e = start + t % E;
-  const int64_t v = t / E;
+// lane = (e - start) Dc G + d G + g and every float4 position of a view are below 2^31 (checked on the host)
+template <int kG>
+__device__ __forceinline__ void lane_coef(uint32_t lane, LaneCoef& k, const float* __restrict__ mu,
+                                          const float* __restrict__ c, const int* __restrict__ octant,
+                                          const int* __restrict__ cell, const int* __restrict__ upstream,
+                                          uint32_t start, uint32_t N, int G_runtime, uint32_t Dc) {
+  const uint32_t G = kG > 0 ? kG : G_runtime;
+  const uint32_t g = lane % G, t = lane / G;
+  const uint32_t d = t % Dc, e = start + t / Dc;
   const int o = __ldg(octant + e);
-  const int64_t n = __ldg(cell + e);
-  const int64_t ux = __ldg(upstream + 3 * e), uy = __ldg(upstream + 3 * e + 1), uz = __ldg(upstream + 3 * e + 2);
-  const int64_t od = (int64_t)o * Dc + d;
-  in.o = o;
-  in.cx = __ldg(c + 3 * od);
-  in.cy = __ldg(c + 3 * od + 1);
-  in.cz = __ldg(c + 3 * od + 2);
-  in.m = __ldg(mu + n * G + g);
-  const int64_t Q = 4 * (int64_t)G;
-  float* base = store + v * view_stride + od * N * Q + 4 * g;
-  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  in.dst = base + n * Q;
-  in.s = load4<kCoherent>(in.dst);
-  in.X = ux < N ? load4<kCoherent>(base + ux * Q) : zero;
-  in.Y = uy < N ? load4<kCoherent>(base + uy * Q) : zero;
-  in.Z = uz < N ? load4<kCoherent>(base + uz * Q) : zero;
-}
-
-// The closed-form cell solve of one lane and its store over the source. Every operation is rounded on its own (no
-// multiply-add contraction), so every kernel that inlines it computes the same bits.
-__device__ __forceinline__ void finish_lane(const LaneIn& in) {
-  const float sx = (in.o & 4) ? -1.f : 1.f, sy = (in.o & 2) ? -1.f : 1.f, sz = (in.o & 1) ? -1.f : 1.f;
-  const float cx = in.cx, cy = in.cy, cz = in.cz, m = in.m;
-  const float4 s = in.s, X = in.X, Y = in.Y, Z = in.Z;
-  // face-averaged inflow psibar_a = psi_0[N_a] + s_a psi_a[N_a]
-  const float pbx = __fadd_rn(X.x, __fmul_rn(sx, X.y));
-  const float pby = __fadd_rn(Y.x, __fmul_rn(sy, Y.z));
-  const float pbz = __fadd_rn(Z.x, __fmul_rn(sz, Z.w));
-  const float r0 = __fadd_rn(s.x, __fadd_rn(__fadd_rn(__fmul_rn(cx, pbx), __fmul_rn(cy, pby)), __fmul_rn(cz, pbz)));
-  // R_a = S_a - 3 s_a c_a psibar_a + sum_{b != a} c_b psi_a[N_b]
-  const float tx = __fmul_rn(__fmul_rn(__fmul_rn(3.f, sx), cx), pbx);
-  const float ty = __fmul_rn(__fmul_rn(__fmul_rn(3.f, sy), cy), pby);
-  const float tz = __fmul_rn(__fmul_rn(__fmul_rn(3.f, sz), cz), pbz);
-  const float rx = __fadd_rn(__fsub_rn(s.y, tx), __fadd_rn(__fmul_rn(cy, Y.y), __fmul_rn(cz, Z.y)));
-  const float ry = __fadd_rn(__fsub_rn(s.z, ty), __fadd_rn(__fmul_rn(cx, X.z), __fmul_rn(cz, Z.z)));
-  const float rz = __fadd_rn(__fsub_rn(s.w, tz), __fadd_rn(__fmul_rn(cx, X.w), __fmul_rn(cy, Y.w)));
+  const uint32_t n = __ldg(cell + e);
+  const uint32_t ux = __ldg(upstream + 3 * e), uy = __ldg(upstream + 3 * e + 1), uz = __ldg(upstream + 3 * e + 2);
+  const uint32_t od = (uint32_t)o * Dc + d;
+  const float cx = __ldg(c + 3 * od), cy = __ldg(c + 3 * od + 1), cz = __ldg(c + 3 * od + 2);
+  const float m = __ldg(mu + (size_t)n * G + g);
+  const uint32_t base = od * N;
+  k.at = (base + n) * G + g;
+  k.ax = ux < N ? (base + ux) * G + g : kVacuum;
+  k.ay = uy < N ? (base + uy) * G + g : kVacuum;
+  k.az = uz < N ? (base + uz) * G + g : kVacuum;
+  // every operation is rounded on its own (no multiply-add contraction), so every kernel computes the same bits
+  const float sx = (o & 4) ? -1.f : 1.f, sy = (o & 2) ? -1.f : 1.f, sz = (o & 1) ? -1.f : 1.f;
+  k.sx = sx, k.sy = sy, k.sz = sz, k.cx = cx, k.cy = cy, k.cz = cz;
+  k.k3x = __fmul_rn(__fmul_rn(3.f, sx), cx);
+  k.k3y = __fmul_rn(__fmul_rn(3.f, sy), cy);
+  k.k3z = __fmul_rn(__fmul_rn(3.f, sz), cz);
   const float csum = __fadd_rn(__fadd_rn(cx, cy), cz);
   const float dx = __fadd_rn(__fadd_rn(__fmul_rn(3.f, cx), __fsub_rn(csum, cx)), m);
   const float dy = __fadd_rn(__fadd_rn(__fmul_rn(3.f, cy), __fsub_rn(csum, cy)), m);
   const float dz = __fadd_rn(__fadd_rn(__fmul_rn(3.f, cz), __fsub_rn(csum, cz)), m);
   const float qx = __fdiv_rn(cx, dx), qy = __fdiv_rn(cy, dy), qz = __fdiv_rn(cz, dz);
   const float qsum = __fadd_rn(__fadd_rn(__fmul_rn(cx, qx), __fmul_rn(cy, qy)), __fmul_rn(cz, qz));
-  const float denom = __fadd_rn(__fadd_rn(csum, m), __fmul_rn(3.f, qsum));
-  const float corr = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(sx, qx), rx), __fmul_rn(__fmul_rn(sy, qy), ry)),
-                               __fmul_rn(__fmul_rn(sz, qz), rz));
-  const float p0 = __fdiv_rn(__fsub_rn(r0, corr), denom);
+  k.rden = __frcp_rn(__fadd_rn(__fadd_rn(csum, m), __fmul_rn(3.f, qsum)));
+  k.rdx = __frcp_rn(dx);
+  k.rdy = __frcp_rn(dy);
+  k.rdz = __frcp_rn(dz);
+  k.qsx = __fmul_rn(sx, qx);
+  k.qsy = __fmul_rn(sy, qy);
+  k.qsz = __fmul_rn(sz, qz);
+}
+
+// The store moments a lane reads in one view: the source (s) and (psi0, psi_x, psi_y, psi_z) of the x, y, z upstream
+// neighbours
+struct LaneIn {
+  float4 s, X, Y, Z;
+};
+
+template <bool kCoherent>
+__device__ __forceinline__ void gather_view(const LaneCoef& k, const float4* view, LaneIn& in) {
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  in.s = load4<kCoherent>(view + k.at);
+  in.X = k.ax != kVacuum ? load4<kCoherent>(view + k.ax) : zero;
+  in.Y = k.ay != kVacuum ? load4<kCoherent>(view + k.ay) : zero;
+  in.Z = k.az != kVacuum ? load4<kCoherent>(view + k.az) : zero;
+}
+
+// The closed-form cell solve of the equations of linear_discontinuous_cell.py:14-87 in one view, stored over the
+// source.
+__device__ __forceinline__ void solve_view(const LaneCoef& k, const LaneIn& in, float4* view) {
+  const float4 s = in.s, X = in.X, Y = in.Y, Z = in.Z;
+  // face-averaged inflow psibar_a = psi_0[N_a] + s_a psi_a[N_a]
+  const float pbx = __fadd_rn(X.x, __fmul_rn(k.sx, X.y));
+  const float pby = __fadd_rn(Y.x, __fmul_rn(k.sy, Y.z));
+  const float pbz = __fadd_rn(Z.x, __fmul_rn(k.sz, Z.w));
+  const float r0 =
+      __fadd_rn(s.x, __fadd_rn(__fadd_rn(__fmul_rn(k.cx, pbx), __fmul_rn(k.cy, pby)), __fmul_rn(k.cz, pbz)));
+  // R_a = S_a - 3 s_a c_a psibar_a + sum_{b != a} c_b psi_a[N_b]
+  const float rx = __fadd_rn(__fsub_rn(s.y, __fmul_rn(k.k3x, pbx)), __fadd_rn(__fmul_rn(k.cy, Y.y), __fmul_rn(k.cz, Z.y)));
+  const float ry = __fadd_rn(__fsub_rn(s.z, __fmul_rn(k.k3y, pby)), __fadd_rn(__fmul_rn(k.cx, X.z), __fmul_rn(k.cz, Z.z)));
+  const float rz = __fadd_rn(__fsub_rn(s.w, __fmul_rn(k.k3z, pbz)), __fadd_rn(__fmul_rn(k.cx, X.w), __fmul_rn(k.cy, Y.w)));
+  const float corr =
+      __fadd_rn(__fadd_rn(__fmul_rn(k.qsx, rx), __fmul_rn(k.qsy, ry)), __fmul_rn(k.qsz, rz));
+  // the per-view quotients as products with the lane's correctly rounded reciprocals (within 1.5 ulp of the quotient)
+  const float p0 = __fmul_rn(__fsub_rn(r0, corr), k.rden);
   float4 out;
   out.x = p0;
-  out.y = __fdiv_rn(__fadd_rn(rx, __fmul_rn(__fmul_rn(__fmul_rn(3.f, sx), cx), p0)), dx);
-  out.z = __fdiv_rn(__fadd_rn(ry, __fmul_rn(__fmul_rn(__fmul_rn(3.f, sy), cy), p0)), dy);
-  out.w = __fdiv_rn(__fadd_rn(rz, __fmul_rn(__fmul_rn(__fmul_rn(3.f, sz), cz), p0)), dz);
-  *reinterpret_cast<float4*>(in.dst) = out;
+  out.y = __fmul_rn(__fadd_rn(rx, __fmul_rn(k.k3x, p0)), k.rdx);
+  out.z = __fmul_rn(__fadd_rn(ry, __fmul_rn(k.k3y, p0)), k.rdy);
+  out.w = __fmul_rn(__fadd_rn(rz, __fmul_rn(k.k3z, p0)), k.rdz);
+  view[k.at] = out;
 }
 
-template <int kG, bool kCoherent>
-__device__ __forceinline__ void solve_lane(int64_t lane, float* __restrict__ store, const float* __restrict__ mu,
-                                           const float* __restrict__ c, const int* __restrict__ octant,
-                                           const int* __restrict__ cell, const int* __restrict__ upstream,
-                                           int64_t start, int64_t E, int64_t N, int G_runtime, int64_t Dc,
-                                           int64_t view_stride) {
-  LaneIn in;
-  gather_lane<kG, kCoherent>(lane, in, store, mu, c, octant, cell, upstream, start, E, N, G_runtime, Dc,
-                             view_stride);
-  finish_lane(in);
-}
-
+// One plane, one lane (view v, entry, direction, group) per thread: the reference's launch plan.
 template <int kG>
-__global__ void __launch_bounds__(kThreads) plane_kernel(float* __restrict__ store, const float* __restrict__ mu,
+__global__ void __launch_bounds__(kThreads) plane_kernel(float4* __restrict__ store, const float* __restrict__ mu,
                                                          const float* __restrict__ c, const int* __restrict__ octant,
                                                          const int* __restrict__ cell, const int* __restrict__ upstream,
-                                                         int64_t start, int64_t E, int64_t N, int G, int64_t Dc,
-                                                         int64_t views, int64_t view_stride) {
+                                                         uint32_t start, uint32_t per_view, uint32_t N, int G,
+                                                         uint32_t Dc, int64_t views, int64_t view_stride) {
   const int64_t lane = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-  const int64_t total = views * E * Dc * (kG > 0 ? kG : G);
-  if (lane >= total) return;
-  solve_lane<kG, false>(lane, store, mu, c, octant, cell, upstream, start, E, N, G, Dc, view_stride);
+  if (lane >= views * per_view) return;
+  const int64_t v = lane / per_view;
+  LaneCoef k;
+  lane_coef<kG>((uint32_t)(lane - v * per_view), k, mu, c, octant, cell, upstream, start, N, G, Dc);
+  LaneIn in;
+  float4* view = store + v * view_stride;
+  gather_view<false>(k, view, in);
+  solve_view(k, in, view);
 }
 
-// All planes in one cooperative launch. A thread takes kU lanes of a plane at a time (stride apart, so every warp
-// still reads whole cells): all their loads are issued before the first solve and store, which a plain loop cannot
-// do (the stores might alias the next lane's loads as far as the compiler knows; within a plane they never do).
-template <int kG, int kU, int kMinBlocks>
+// All planes in one cooperative launch, with a bounded grid barrier between planes. A thread takes one lane (entry,
+// direction, group) of a plane at a time and solves it in every view, kVB views at a time: the loads of kVB views are
+// issued before their solves (which a plain loop cannot do: the stores might alias the next view's loads as far as
+// the compiler knows; within a plane they never do).
+template <int kG, int kVB, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_kernel(
-    float* __restrict__ store, const float* __restrict__ mu, const float* __restrict__ c,
+    float4* __restrict__ store, const float* __restrict__ mu, const float* __restrict__ c,
     const int* __restrict__ octant, const int* __restrict__ cell, const int* __restrict__ upstream,
-    const int* __restrict__ offsets, int num_planes, int64_t N, int G, int64_t Dc, int64_t views,
-    int64_t view_stride, unsigned* sync, uint64_t timeout_ns, int skip) {
-  const int64_t stride = (int64_t)gridDim.x * kThreads;
-  const int64_t per_entry = Dc * (kG > 0 ? kG : G) * views;
+    const int* __restrict__ offsets, int num_planes, uint32_t N, int G, uint32_t Dc, int views, int64_t view_stride,
+    unsigned* sync, uint64_t timeout_ns, int skip) {
+  const uint32_t stride = gridDim.x * kThreads;
+  const uint32_t per_entry = Dc * (kG > 0 ? kG : G);
   for (int p = 0; p < num_planes; ++p) {
-    const int64_t start = __ldg(offsets + p);
-    const int64_t E = __ldg(offsets + p + 1) - start;
-    const int64_t total = E * per_entry;
-    for (int64_t lane0 = (int64_t)blockIdx.x * kThreads + threadIdx.x; lane0 < total; lane0 += stride * kU) {
-      LaneIn in[kU];
+    const uint32_t start = __ldg(offsets + p);
+    const uint32_t total = (__ldg(offsets + p + 1) - start) * per_entry;
+    for (uint32_t lane = blockIdx.x * kThreads + threadIdx.x; lane < total; lane += stride) {
+      LaneCoef k;
+      lane_coef<kG>(lane, k, mu, c, octant, cell, upstream, start, N, G, Dc);
+      float4* view = store;
+      for (int v0 = 0; v0 < views; v0 += kVB, view += kVB * view_stride) {
+        LaneIn in[kVB];
 #pragma unroll
-      for (int u = 0; u < kU; ++u)
-        if (lane0 + u * stride < total)
-          gather_lane<kG, true>(lane0 + u * stride, in[u], store, mu, c, octant, cell, upstream, start, E, N, G, Dc,
-                                view_stride);
+        for (int j = 0; j < kVB; ++j)
+          if (v0 + j < views) gather_view<true>(k, view + j * view_stride, in[j]);
 #pragma unroll
-      for (int u = 0; u < kU; ++u)
-        if (lane0 + u * stride < total) finish_lane(in[u]);
+        for (int j = 0; j < kVB; ++j)
+          if (v0 + j < views) solve_view(k, in[j], view + j * view_stride);
+      }
     }
     if (p + 1 < num_planes && !grid_barrier(sync, gridDim.x, timeout_ns, skip)) return;
   }
@@ -155,36 +174,40 @@ template <int kG>
 int launch_planes(float* store, const float* mu, const float* c, const int* octant, const int* cell,
                   const int* upstream, const int64_t* offsets, int64_t num_planes, int64_t N, int G, int64_t Dc,
                   int64_t views, cudaStream_t stream) {
-  const int64_t view_stride = 8 * Dc * N * 4 * (int64_t)G;
+  const int64_t view_stride = 8 * Dc * N * (int64_t)G;  // float4 per view
   for (int64_t p = 0; p < num_planes; ++p) {
     const int64_t start = offsets[p], E = offsets[p + 1] - offsets[p];
-    const int64_t total = views * E * Dc * G;
-    if (total <= 0) continue;
-    plane_kernel<kG><<<(unsigned)cdiv(total, kThreads), kThreads, 0, stream>>>(
-        store, mu, c, octant, cell, upstream, start, E, N, G, Dc, views, view_stride);
+    const int64_t per_view = E * Dc * G;
+    if (per_view <= 0) continue;
+    plane_kernel<kG><<<(unsigned)cdiv(views * per_view, kThreads), kThreads, 0, stream>>>(
+        reinterpret_cast<float4*>(store), mu, c, octant, cell, upstream, (uint32_t)start, (uint32_t)per_view,
+        (uint32_t)N, G, (uint32_t)Dc, views, view_stride);
     note_launches();
   }
   return launch_status("citrus_sweep_planes");
 }
 
-template <int kG, int kU, int kMinBlocks = 1>
+template <int kG, int kVB, int kMinBlocks = 1>
 int launch_persistent_u(float* store, const float* mu, const float* c, const int* octant, const int* cell,
                         const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
                         int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
                         cudaStream_t stream) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG, kU, kMinBlocks>,
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel<kG, kVB, kMinBlocks>,
                                                                 kThreads, 0);
   if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: occupancy query failed");
   int64_t blocks = (int64_t)per_sm * num_sms();
   if (max_blocks > 0 && max_blocks < blocks) blocks = max_blocks;
   if (skip >= blocks) skip = (int)blocks - 1;
-  int64_t view_stride = 8 * Dc * N * 4 * (int64_t)G;
+  float4* store4 = reinterpret_cast<float4*>(store);
+  uint32_t n32 = (uint32_t)N, dc32 = (uint32_t)Dc;
+  int views32 = (int)views;
+  int64_t view_stride = 8 * Dc * N * (int64_t)G;  // float4 per view
   cudaError_t z = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned), stream);
   if (z != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_sweep_persistent: %s", cudaGetErrorString(z));
-  void* args[] = {&store, &mu, &c, &octant, &cell, &upstream, &offsets, &num_planes, &N, &G, &Dc, &views,
+  void* args[] = {&store4, &mu, &c, &octant, &cell, &upstream, &offsets, &num_planes, &n32, &G, &dc32, &views32,
                   &view_stride, &sync, &timeout_ns, &skip};
-  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG, kU, kMinBlocks>, dim3((unsigned)blocks),
+  e = cudaLaunchCooperativeKernel((const void*)persistent_kernel<kG, kVB, kMinBlocks>, dim3((unsigned)blocks),
                                   dim3(kThreads), args, 0, stream);
   if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_persistent: %s", cudaGetErrorString(e));
   note_launches();
@@ -193,25 +216,28 @@ int launch_persistent_u(float* store, const float* mu, const float* c, const int
 
 constexpr int kDefaultUnroll = 1;
 
+// the forms of the persistent launch's threads, chosen per grid by the autotuner
 template <int kG>
 int launch_persistent(float* store, const float* mu, const float* c, const int* octant, const int* cell,
                       const int* upstream, const int* offsets, int num_planes, int64_t N, int G, int64_t Dc,
                       int64_t views, unsigned* sync, int64_t max_blocks, uint64_t timeout_ns, int skip,
                       cudaStream_t stream, int unroll = kDefaultUnroll) {
   switch (unroll) {
-    case 1:  // one lane per thread, five blocks of 256 threads per SM
+    case 1:  // one view at a time, five blocks of 256 threads per SM
       return launch_persistent_u<kG, 1, 5>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
                                            views, sync, max_blocks, timeout_ns, skip, stream);
-    case 3:  // one lane per thread, registers capped for six blocks of 256 threads per SM
+    case 3:  // one view at a time, registers capped for six blocks of 256 threads per SM
       return launch_persistent_u<kG, 1, 6>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
                                            views, sync, max_blocks, timeout_ns, skip, stream);
-    case 5:  // one lane per thread, eight blocks per SM
-      return launch_persistent_u<kG, 1, 8>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+    case 5:  // one view at a time, four blocks per SM
+      return launch_persistent_u<kG, 1, 4>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
                                            views, sync, max_blocks, timeout_ns, skip, stream);
-    case 2: return launch_persistent_u<kG, 2>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
-                                              views, sync, max_blocks, timeout_ns, skip, stream);
-    case 4: return launch_persistent_u<kG, 4>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
-                                              views, sync, max_blocks, timeout_ns, skip, stream);
+    case 2:  // the loads of two views before their solves, three blocks per SM
+      return launch_persistent_u<kG, 2, 3>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                           views, sync, max_blocks, timeout_ns, skip, stream);
+    case 4:  // the loads of four views before their solves, two blocks per SM
+      return launch_persistent_u<kG, 4, 2>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
+                                           views, sync, max_blocks, timeout_ns, skip, stream);
     default:
       return set_error(CITRUS_EINVAL, "citrus_sweep_persistent: lanes per thread form %d (1, 2, 3, 4 or 5)", unroll);
   }
@@ -224,6 +250,10 @@ int check_sweep_args(const float* store, const float* mu, const float* c, const 
                  "sweep: sizes must be positive (planes %lld, cells %lld, groups %lld, dc %lld, views %lld)",
                  (long long)num_planes, (long long)N, (long long)G, (long long)Dc, (long long)views);
   CITRUS_REQUIRE(N < (1ll << 31) / 8, "sweep: %lld cells exceed the int32 entry tables", (long long)N);
+  CITRUS_REQUIRE(views < (1ll << 31), "sweep: too many views (%lld)", (long long)views);
+  CITRUS_REQUIRE(8 * N * Dc * G < (1ll << 31),
+                 "sweep: one view's store of %lld float4 exceeds the 32-bit lane positions; sweep fewer directions "
+                 "per chunk", (long long)(8 * N * Dc * G));
   CITRUS_REQUIRE(G <= 4096, "sweep: too many groups (%lld)", (long long)G);
   CITRUS_REQUIRE(((uintptr_t)store % 16) == 0, "sweep: store must be 16-byte aligned");
   return CITRUS_OK;

@@ -88,8 +88,9 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
         max_blocks: cap on the persistent grid (0: as many blocks as fit).
         timeout_ns: bound of every barrier wait of the persistent launch.
         skip_block: test hook forcing a barrier timeout (-1 in normal use).
-        lanes_per_thread: the form of the persistent launch's threads: 1, 2 or 4 lanes loaded before they are solved,
-            3 or 5 for one lane with registers capped for 6 or 8 blocks per SM (0: 1).
+        lanes_per_thread: the form of the persistent launch's threads, each of which solves its lane (entry,
+            direction, group) in every view: 2 or 4 views loaded before they are solved, or one view at a time with
+            registers capped for 5 (1), 6 (3) or 4 (5) blocks per SM (0: 1).
 
     Returns:
         The sync words of the persistent launch (``sync[2] != 0`` means a barrier wait ran out), or None.
