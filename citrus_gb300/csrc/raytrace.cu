@@ -157,6 +157,164 @@ __device__ __forceinline__ Setup<float> ray_setup_dir(const Box& b, const double
   return s;
 }
 
+// ---- float-pair set-up of the oblique rays --------------------------------------------------------------------
+// float64 runs at a small fraction of the float32 rate on this GPU, so the oblique set-up is carried in float pairs
+// (hi + lo, Knuth's two-sum and an fmaf-exact product error: ~2^-44 relative), which place a line's entry point and
+// its clip to ~1e-11 cm, far inside the tolerances below. Every discrete decision of the float64 set-up (hit or miss,
+// the binding faces, the entry and exit voxels) is taken from the pair values only when they lie clear of the
+// decision's boundary by a margin (kFaceTol in cm, kParamTol along the line, kVoxelTol in voxels) that dwarfs both
+// set-ups' rounding; a line nearer than that (a line in a face of the box, through an edge, or onto a voxel plane)
+// is set up in float64 as before, so its voxels are the float64 set-up's.
+constexpr float kFaceTol = 1e-7f;
+constexpr float kParamTol = 1e-6f;
+constexpr float kVoxelTol = 1e-5f;
+
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_norm(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ff_norm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, FF{-b.hi, -b.lo}); }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = fmaf(a.hi, b.hi, -p);
+  return ff_norm(p, __fadd_rn(e, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi))));
+}
+__device__ __forceinline__ FF ff_mul(FF a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  const float e = fmaf(a.hi, b, -p);
+  return ff_norm(p, __fadd_rn(e, __fmul_rn(a.lo, b)));
+}
+__device__ __forceinline__ float ff_float(FF a) { return __fadd_rn(a.hi, a.lo); }
+
+// A float64 value as a float pair by integer operations on its bits: the top 24 bits of the significand (exact) and
+// the low 29 rounded to float (2^-49 relative); magnitudes outside [2^-74, 2^151) are converted directly (zero).
+__device__ __forceinline__ FF ff_from(double x) {
+  const long long bits = __double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if (e < 949 || e > 1173) return {__double2float_rn(x), 0.f};
+  const unsigned long long m = ((unsigned long long)bits & 0xfffffffffffffull) | (1ull << 52);
+  const float hi = __fmul_rn(__uint2float_rn((unsigned)(m >> 29)), __int_as_float((e - 919) << 23));
+  const float lo = __fmul_rn(__uint2float_rn((unsigned)(m & 0x1fffffffull)), __int_as_float((e - 948) << 23));
+  return bits < 0 ? FF{-hi, -lo} : FF{hi, lo};
+}
+
+// The per-direction constants of the float-pair set-up (formed once per block from the float64 ones).
+struct DirPair {
+  FF c[3], inv_w2, h, d[3], inv_d[3], lo[3], hi[3];
+  float w[3], inv_df[3], delta[3], v[3], len;
+};
+
+__device__ __forceinline__ void make_dir_pair(const Box& b, const DirConst& dc, const double c[3], DirPair& dp) {
+  dp.inv_w2 = ff_from(dc.inv_w2);
+  dp.h = ff_from(dc.h);
+  float df[3];
+  for (int a = 0; a < 3; ++a) {
+    dp.c[a] = ff_from(c[a]);
+    dp.d[a] = ff_from(dc.d[a]);
+    dp.inv_d[a] = ff_from(dc.inv_d[a]);
+    dp.lo[a] = ff_from(b.lo[a]);
+    dp.hi[a] = ff_from(dc.hi[a]);
+    dp.w[a] = (float)dc.w[a];
+    dp.inv_df[a] = (float)dc.inv_d[a];
+    dp.delta[a] = (float)b.delta[a];
+    df[a] = (float)dc.d[a];
+  }
+  dp.len = sqrtf(df[0] * df[0] + df[1] * df[1] + df[2] * df[2]);
+  for (int a = 0; a < 3; ++a) dp.v[a] = df[a] / dp.len / dp.delta[a];
+}
+
+// The entry voxel along one axis from the pair position x (cm from the box's low face), as the float64 set-up forms
+// it; false when x lies within kVoxelTol of an interior voxel plane.
+__device__ __forceinline__ bool pair_voxel(FF x, float delta, int n, int& i, float& q) {
+  q = ff_float(x) / delta;
+  const float r = rintf(q);
+  if (r >= 1.f && r <= (float)(n - 1) && fabsf(q - r) < kVoxelTol) return false;
+  i = (int)floorf(q);
+  if (i < 0) i = 0;
+  if (i > n - 1) i = n - 1;
+  return true;
+}
+
+// The clipped set-up of the ray through the pixel centre (px, py, pz) along the block's direction in float pairs:
+// the same entry point (ray_tracing.py:588-595), clip and walk set-up as ray_setup_dir. Returns false, with s
+// undefined, when a decision lies within its tolerance; the caller then sets the ray up in float64.
+__device__ __forceinline__ bool ray_setup_pair(const Box& b, const DirPair& dp, double px, double py, double pz,
+                                               Setup<float>& s) {
+  const FF p[3] = {ff_from(px), ff_from(py), ff_from(pz)};
+  FF dot = ff_mul(ff_sub(dp.c[0], p[0]), dp.w[0]);
+  dot = ff_add(dot, ff_mul(ff_sub(dp.c[1], p[1]), dp.w[1]));
+  dot = ff_add(dot, ff_mul(ff_sub(dp.c[2], p[2]), dp.w[2]));
+  const FF tm = ff_sub(ff_mul(dot, dp.inv_w2), dp.h);
+  FF a[3];
+  for (int k = 0; k < 3; ++k) a[k] = ff_add(p[k], ff_mul(tm, dp.w[k]));
+  // the clip: the largest entry and smallest exit parameter over the slabs (and the segment's own 0 and 1), with the
+  // runner-up of each, so that a binding face that another one nearly ties with is left to float64
+  float t_lo = 0.f, t_lo2 = -INFINITY, t_hi = 1.f, t_hi2 = INFINITY;
+  FF f_lo = {0.f, 0.f}, f_hi = {0.f, 0.f};  // the binding faces' distances (cm), -1 axis: the segment's end
+  int ax_lo = -1, ax_hi = -1;
+  bool inside = true;
+  for (int k = 0; k < 3; ++k) {
+    const FF dl = ff_sub(dp.lo[k], a[k]), dh = ff_sub(dp.hi[k], a[k]);
+    const float dlf = ff_float(dl), dhf = ff_float(dh);
+    if (fabsf(dlf) < kFaceTol || fabsf(dhf) < kFaceTol) return false;
+    if (dp.w[k] != 0.f) {
+      const float t1 = dlf * dp.inv_df[k], t2 = dhf * dp.inv_df[k];
+      const bool first = t1 <= t2;
+      const float tn = first ? t1 : t2, tx = first ? t2 : t1;
+      if (tn > t_lo) {
+        t_lo2 = t_lo;
+        t_lo = tn;
+        ax_lo = k;
+        f_lo = first ? dl : dh;
+      } else {
+        t_lo2 = fmaxf(t_lo2, tn);
+      }
+      if (tx < t_hi) {
+        t_hi2 = t_hi;
+        t_hi = tx;
+        ax_hi = k;
+        f_hi = first ? dh : dl;
+      } else {
+        t_hi2 = fminf(t_hi2, tx);
+      }
+    } else if (!(dlf <= 0.f && dhf >= 0.f)) {
+      inside = false;  // parallel to this slab and outside it
+    }
+  }
+  if (t_lo - t_lo2 < kParamTol || t_hi2 - t_hi < kParamTol) return false;
+  if (fabsf(t_hi - t_lo) < kParamTol) return false;
+  s.hit = inside && t_hi > t_lo && dp.len > 0.f;
+  if (!s.hit) {
+    s.total = 0.f;
+    return true;
+  }
+  const FF a_lo = ax_lo >= 0 ? ff_mul(f_lo, dp.inv_d[ax_lo]) : FF{0.f, 0.f};
+  const FF a_hi = ax_hi >= 0 ? ff_mul(f_hi, dp.inv_d[ax_hi]) : FF{1.f, 0.f};
+  s.total = ff_float(ff_sub(a_hi, a_lo)) * dp.len;
+  for (int k = 0; k < 3; ++k) {
+    const FF rel = ff_sub(a[k], dp.lo[k]);
+    int i, ie;
+    float q, qe;
+    if (!pair_voxel(ff_add(rel, ff_mul(a_lo, dp.d[k])), dp.delta[k], b.n[k], i, q)) return false;
+    if (!pair_voxel(ff_add(rel, ff_mul(a_hi, dp.d[k])), dp.delta[k], b.n[k], ie, qe)) return false;
+    s.v[k] = dp.v[k];
+    s.idx[k] = i;
+    s.f[k] = fminf(fmaxf(q - (float)i, 0.f), 1.f);
+    s.cross[k] = ie > i ? ie - i : i - ie;
+  }
+  return true;
+}
+
 // Walk one clipped ray and add the integral of the C channels to acc (in cm times the field unit).
 template <int kC, bool kCompensated>
 __device__ __forceinline__ void ray_walk(const Box& b, const Setup<float>& s, const float* __restrict__ vol, int C,
@@ -629,6 +787,7 @@ __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* _
   // the direction's constants, once per block (the block shares the direction): float64 on this GPU runs at a small
   // fraction of float32, so every division of the set-up is made here rather than per ray
   __shared__ DirConst s_dc;
+  __shared__ DirPair s_dp;
   if (threadIdx.x == 0) {
     DirConst dc;
     dc.w[0] = omegas[3 * k];
@@ -643,20 +802,25 @@ __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* _
       dc.hi[a] = add_rn(b.lo[a], mul_rn(b.delta[a], (double)b.n[a]));
     }
     s_dc = dc;
+    const double c[3] = {cx, cy, cz};
+    make_dir_pair(b, dc, c, s_dp);
   }
   __syncthreads();
   if (p >= P) return;
   const DirConst& dc = s_dc;
   const double px = pixels[3 * p], py = pixels[3 * p + 1], pz = pixels[3 * p + 2];
-  // the entry point of ray_tracing.py:588-595, its exit point the entry plus the direction's segment
-  const double dot = add_rn(add_rn(mul_rn(cx - px, dc.w[0]), mul_rn(cy - py, dc.w[1])), mul_rn(cz - pz, dc.w[2]));
-  const double tm = mul_rn(dot, dc.inv_w2) - dc.h;
-  const double a[3] = {add_rn(px, mul_rn(tm, dc.w[0])), add_rn(py, mul_rn(tm, dc.w[1])),
-                       add_rn(pz, mul_rn(tm, dc.w[2]))};
   const int nC = kC > 0 ? kC : C;
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
-  const Setup<float> st = ray_setup_dir(b, a, dc);
+  Setup<float> st;
+  if (!ray_setup_pair(b, s_dp, px, py, pz, st)) {
+    // the entry point of ray_tracing.py:588-595 in float64, its exit point the entry plus the direction's segment
+    const double dot = add_rn(add_rn(mul_rn(cx - px, dc.w[0]), mul_rn(cy - py, dc.w[1])), mul_rn(cz - pz, dc.w[2]));
+    const double tm = mul_rn(dot, dc.inv_w2) - dc.h;
+    const double a[3] = {add_rn(px, mul_rn(tm, dc.w[0])), add_rn(py, mul_rn(tm, dc.w[1])),
+                         add_rn(pz, mul_rn(tm, dc.w[2]))};
+    st = ray_setup_dir(b, a, dc);
+  }
   if (st.hit) {
     if (kC == 1) acc[0] = ray_walk_one_channel(b, st, vol + (int64_t)k * field_stride);
     else ray_walk<kC, false>(b, st, vol + (int64_t)k * field_stride, C, acc);
