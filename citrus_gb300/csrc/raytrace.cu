@@ -7,8 +7,9 @@
 // every segment length is computed from quantities of voxel size (relative error ~ float epsilon per segment), and the
 // travelled distance is summed with a compensated (Kahan) sum, so the end of the ray is placed to float epsilon of its
 // total length, and it crosses along each axis only as many planes as lie between the entry and exit voxels. Rays that
-// must meet 1e-6 relative path lengths (upstream to points, primary) and the oblique rays through the pixel centres,
-// some of which run along a face of the box, do their set-up in float64; the downstream rays do it in float32.
+// must meet 1e-6 relative path lengths (upstream to points, primary) do their set-up in float64; the oblique rays
+// through the pixel centres, some of which run along a face of the box, do it in float pairs with float64 for the
+// lines near a face; the downstream rays do it in float32.
 //
 // Volumes are read voxel-major, [V, C] with the C channels (groups or materials) of a voxel contiguous, so one voxel
 // visit is one or two 16-byte loads for every channel at once.
@@ -26,6 +27,7 @@ struct Box {
   double lo[3];     // lower corner (x, y, z) in cm
   double delta[3];  // voxel sizes (x, y, z) in cm
   int n[3];         // voxel counts (x = columns, y = rows, z = slices)
+  float lof[3], deltaf[3];  // the same rounded to float (float64 runs at a small fraction of float32 on this GPU)
 };
 
 Box make_box(const double* box, const int64_t* dims) {
@@ -34,8 +36,15 @@ Box make_box(const double* box, const int64_t* dims) {
     b.lo[a] = box[a];
     b.delta[a] = box[3 + a];
     b.n[a] = (int)dims[a];
+    b.lof[a] = (float)b.lo[a];
+    b.deltaf[a] = (float)b.delta[a];
   }
   return b;
+}
+
+// the centre of voxel i along axis a, in float
+__device__ __forceinline__ float voxel_centre(const Box& b, int a, int i) {
+  return b.lof[a] + b.deltaf[a] * ((float)i + 0.5f);
 }
 
 template <typename T>
@@ -558,23 +567,24 @@ __global__ void __launch_bounds__(kThreads) from_source_kernel(Box b, const floa
 }
 
 // ---- downstream: from every voxel centre along each direction to the panel ----------------------------------
+// The detector surface the downstream rays stop at, in float (rounded on the host, once).
 struct Panel {
   int curved;
-  double center[3], normal[3];  // flat panel: a point of the plane and its normal (toward the source)
-  double source[3], radius;     // curved panel: the cylinder about the vertical axis through the source
+  float center[3], normal[3];  // flat panel: a point of the plane and its normal (toward the source)
+  float source[3], radius2;    // curved panel: the cylinder about the vertical axis through the source
 };
 
 __device__ __forceinline__ float panel_distance(const Panel& p, const float r[3], const float w[3]) {
   if (!p.curved) {
-    const float den = w[0] * (float)p.normal[0] + w[1] * (float)p.normal[1] + w[2] * (float)p.normal[2];
-    const float num = ((float)p.center[0] - r[0]) * (float)p.normal[0] + ((float)p.center[1] - r[1]) * (float)p.normal[1] +
-                      ((float)p.center[2] - r[2]) * (float)p.normal[2];
+    const float den = w[0] * p.normal[0] + w[1] * p.normal[1] + w[2] * p.normal[2];
+    const float num = (p.center[0] - r[0]) * p.normal[0] + (p.center[1] - r[1]) * p.normal[1] +
+                      (p.center[2] - r[2]) * p.normal[2];
     return num / den;
   }
-  const float dx = r[0] - (float)p.source[0], dy = r[1] - (float)p.source[1];
+  const float dx = r[0] - p.source[0], dy = r[1] - p.source[1];
   const float a = w[0] * w[0] + w[1] * w[1];
   const float bb = dx * w[0] + dy * w[1];
-  const float c = dx * dx + dy * dy - (float)(p.radius * p.radius);
+  const float c = dx * dx + dy * dy - p.radius2;
   const float disc = bb * bb - a * c;
   const float root = sqrtf(fmaxf(disc, 0.f));
   const bool pos = bb >= 0.f;
@@ -604,8 +614,7 @@ __global__ void __launch_bounds__(kThreads) downstream_kernel(Box b, const float
   const int64_t rem = v - (int64_t)iy * nzx;
   const int ix = (int)(rem / b.n[2]);
   const int iz = (int)(rem - (int64_t)ix * b.n[2]);
-  const float r[3] = {(float)(b.lo[0] + b.delta[0] * (ix + 0.5)), (float)(b.lo[1] + b.delta[1] * (iy + 0.5)),
-                      (float)(b.lo[2] + b.delta[2] * (iz + 0.5))};
+  const float r[3] = {voxel_centre(b, 0, ix), voxel_centre(b, 1, iy), voxel_centre(b, 2, iz)};
   const float w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
   float t = panel_distance(panel, r, w);
   t = fminf(fmaxf(t, 0.f), diagonal);
@@ -692,8 +701,7 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
   const int64_t rem = v - (int64_t)iy * nzx;
   const int ix = (int)(rem / b.n[2]);
   const int iz = (int)(rem - (int64_t)ix * b.n[2]);
-  const float r[3] = {(float)(b.lo[0] + b.delta[0] * (ix + 0.5)), (float)(b.lo[1] + b.delta[1] * (iy + 0.5)),
-                      (float)(b.lo[2] + b.delta[2] * (iz + 0.5))};
+  const float r[3] = {voxel_centre(b, 0, ix), voxel_centre(b, 1, iy), voxel_centre(b, 2, iz)};
   const float w[3] = {omegas[3 * k], omegas[3 * k + 1], omegas[3 * k + 2]};
   float t_end = fminf(fmaxf(panel_distance(panel, r, w), 0.f), diagonal);
   // the crossing that leaves the box: along axis a after the voxels left between i_a and the face ahead
@@ -772,9 +780,10 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
 }
 
 // ---- oblique: through every pixel centre along each direction, clipped to the box on both sides --------------
-// The set-up is float64 from float64 pixel centres, as the reference forms these lines: a line that grazes a face of
-// the box is inside or outside exactly as in float64, where a float32 rounding of the pixel centre could move it onto
-// the face and integrate a whole slice.
+// The set-up starts from the float64 pixel centres, as the reference forms these lines, in float pairs
+// (ray_setup_pair), and in float64 for a line within its tolerances of a face, an edge or a voxel plane: a line that
+// grazes a face of the box is inside or outside exactly as in float64, where a float32 rounding of the pixel centre
+// could move it onto the face and integrate a whole slice.
 template <int kC>
 __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* __restrict__ vol, int C,
                                                            int64_t field_stride, const float* __restrict__ omegas,
@@ -908,11 +917,11 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
   Panel p;
   p.curved = panel[0] != 0.0;
   for (int a = 0; a < 3; ++a) {
-    p.center[a] = panel[1 + a];
-    p.normal[a] = panel[4 + a];
-    p.source[a] = panel[7 + a];
+    p.center[a] = (float)panel[1 + a];
+    p.normal[a] = (float)panel[4 + a];
+    p.source[a] = (float)panel[7 + a];
   }
-  p.radius = panel[10];
+  p.radius2 = (float)(panel[10] * panel[10]);
   const Box b = make_box(box, dims);
   const int64_t V = dims[0] * dims[1] * dims[2];
   const int C = (int)channels;
