@@ -679,15 +679,21 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
                                                                       const int32_t* __restrict__ table,
                                                                       float* __restrict__ out, int64_t os_k,
                                                                       int64_t os_c, int64_t os_v) {
-  extern __shared__ int32_t s_tab[];  // [3E] of this direction
+  extern __shared__ int32_t s_tab[];  // [4E] of this direction: t, dv, first, and the segment lengths
   const int k = blockIdx.y;
   const int E = b.n[0] + b.n[1] + b.n[2];
   const int32_t* src = table + (int64_t)k * 3 * E;
   for (int i = threadIdx.x; i < 3 * E; i += kThreads) s_tab[i] = src[i];
+  // the length of the segment that ends at crossing j: t[j] - t[j - 1] (t[-1] = 0), as the walk forms it
+  for (int i = threadIdx.x; i < E; i += kThreads) {
+    const float tj = __int_as_float(src[i]), tp = i > 0 ? __int_as_float(src[i - 1]) : 0.f;
+    s_tab[3 * E + i] = __float_as_int(tj - tp);
+  }
   __syncthreads();
   const float* t_cross = reinterpret_cast<const float*>(s_tab);
   const int32_t* dv = s_tab + E;
   const int32_t* first = s_tab + 2 * E;
+  const float* ds = reinterpret_cast<const float*>(s_tab + 3 * E);
   const int64_t v = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   if (v >= V) return;
   const int nC = kC > 0 ? kC : C;
@@ -715,26 +721,34 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
     exit_j = min(exit_j, first[off[a] + left]);
   }
   if (exit_j < E) t_end = fminf(t_end, t_cross[exit_j]);
+  // the segments ending at crossings 0 .. J - 1 are whole (t_j <= t_end); the one ending at crossing J, when the ray
+  // ends before its exit crossing, is cut at t_end (the first j with t_j > t_end, by bisection of the sorted table)
+  int J = min(exit_j + 1, E);
+  bool cut = false;
+  if (J > 0 && t_cross[J - 1] > t_end) {
+    int lo = 0, hi = J - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (t_cross[mid] > t_end) hi = mid;
+      else lo = mid + 1;
+    }
+    J = lo;
+    cut = true;
+  }
   float acc[kC > 0 ? kC : kMaxChannels];
   for (int c = 0; c < nC; ++c) acc[c] = 0.f;
-  int64_t cur = v;
-  float prev = 0.f;
+  int cur = (int)v;
   int j = 0;
   if (kC == 2) {
-    // four crossings at a time: the four gathers are issued before their sums (the crossing table gives every step's
-    // voxel in advance); a step at or past the ray's end adds exactly zero, as the plain loop's exit would
-    const int jmax = min(exit_j + 1, E);
-    for (; j + 4 <= jmax && prev < t_end; j += 4) {
-      const int64_t c1 = cur + dv[j], c2 = c1 + dv[j + 1], c3 = c2 + dv[j + 2];
-      const float2 q0 = __ldg(reinterpret_cast<const float2*>(vol + cur * 2));
-      const float2 q1 = __ldg(reinterpret_cast<const float2*>(vol + c1 * 2));
-      const float2 q2 = __ldg(reinterpret_cast<const float2*>(vol + c2 * 2));
-      const float2 q3 = __ldg(reinterpret_cast<const float2*>(vol + c3 * 2));
-      const float t0 = t_cross[j], t1 = t_cross[j + 1], t2 = t_cross[j + 2], t3 = t_cross[j + 3];
-      const float s0 = prev < t_end ? fminf(t0, t_end) - prev : 0.f;
-      const float s1 = t0 < t_end ? fminf(t1, t_end) - t0 : 0.f;
-      const float s2 = t1 < t_end ? fminf(t2, t_end) - t1 : 0.f;
-      const float s3 = t2 < t_end ? fminf(t3, t_end) - t2 : 0.f;
+    // four segments at a time: the four gathers are issued before their sums (the crossing table gives every step's
+    // voxel in advance)
+    for (; j + 4 <= J; j += 4) {
+      const int c1 = cur + dv[j], c2 = c1 + dv[j + 1], c3 = c2 + dv[j + 2];
+      const float2 q0 = __ldg(reinterpret_cast<const float2*>(vol) + cur);
+      const float2 q1 = __ldg(reinterpret_cast<const float2*>(vol) + c1);
+      const float2 q2 = __ldg(reinterpret_cast<const float2*>(vol) + c2);
+      const float2 q3 = __ldg(reinterpret_cast<const float2*>(vol) + c3);
+      const float s0 = ds[j], s1 = ds[j + 1], s2 = ds[j + 2], s3 = ds[j + 3];
       acc[0] = fmaf(s0, q0.x, acc[0]);
       acc[kC > 1 ? 1 : 0] = fmaf(s0, q0.y, acc[kC > 1 ? 1 : 0]);
       acc[0] = fmaf(s1, q1.x, acc[0]);
@@ -743,14 +757,20 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
       acc[kC > 1 ? 1 : 0] = fmaf(s2, q2.y, acc[kC > 1 ? 1 : 0]);
       acc[0] = fmaf(s3, q3.x, acc[0]);
       acc[kC > 1 ? 1 : 0] = fmaf(s3, q3.y, acc[kC > 1 ? 1 : 0]);
-      prev = t3;
       cur = c3 + dv[j + 3];
     }
   }
-  for (; j <= exit_j && j < E && prev < t_end; ++j) {
-    const float tj = t_cross[j];
-    const float seg = fminf(tj, t_end) - prev;
-    const float* vox = vol + cur * nC;
+  // the remaining whole segments, then the cut one (step j == J)
+  for (; j <= J; ++j) {
+    float seg;
+    if (j < J) {
+      seg = ds[j];
+    } else {
+      const float prev = j > 0 ? t_cross[j - 1] : 0.f;
+      if (!cut || !(prev < t_end)) break;
+      seg = t_end - prev;
+    }
+    const float* vox = vol + (int64_t)cur * nC;
     if (kC == 8 || kC == 4) {
 #pragma unroll
       for (int c = 0; c < (kC > 0 ? kC : 1); c += 4) {
@@ -767,8 +787,7 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
     } else {
       for (int c = 0; c < nC; ++c) acc[c] = fmaf(seg, __ldg(vox + c), acc[c]);
     }
-    prev = tj;
-    cur += dv[j];
+    if (j < J) cur += dv[j];
   }
   if ((kC == 8 || kC == 4) && os_c == 1 && os_v == nC) {  // voxel-major out: the channels of a ray in float4s
 #pragma unroll
@@ -936,13 +955,14 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
   CITRUS_REQUIRE(crossings_words >= 3 * E * num_directions,
                  "citrus_downstream_cumulative: crossing table holds %lld words, needs %lld",
                  (long long)crossings_words, (long long)(3 * E * num_directions));
-  CITRUS_REQUIRE(3 * E * 4 <= 48 * 1024, "citrus_downstream_cumulative: grid too large for the crossing table");
+  CITRUS_REQUIRE(4 * E * 4 <= 48 * 1024, "citrus_downstream_cumulative: grid too large for the crossing table");
+  CITRUS_REQUIRE(V * (int64_t)channels < (1ll << 31), "citrus_downstream_cumulative: volume too large");
   if (C % 2 == 0) CITRUS_REQUIRE(((uintptr_t)volume % 16) == 0, "citrus_downstream_cumulative: unaligned volume");
   if (C % 4 == 0 && os_c == 1 && os_v == C)
     CITRUS_REQUIRE(((uintptr_t)out % 16) == 0 && os_k % 4 == 0, "citrus_downstream_cumulative: unaligned out");
   crossing_table_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, s>>>(b, omegas, (int)num_directions, crossings);
   note_launches();
-  const size_t smem = (size_t)3 * E * sizeof(int32_t);
+  const size_t smem = (size_t)4 * E * sizeof(int32_t);
 #define CITRUS_LATTICE(KC)                                                                                        \
   downstream_lattice_kernel<KC><<<grid, kThreads, smem, s>>>(b, volume, C, omegas, toward, p, (float)diagonal, V, \
                                                             crossings, out, os_k, os_c, os_v)

@@ -103,13 +103,15 @@ def test_oblique_line_grazing_a_box_face(cuda_device):
 
 @pytest.mark.parametrize("channels", [1, 2, 3, 8])
 @pytest.mark.parametrize("curved", [False, True])
-def test_downstream_lattice_walk_matches_per_ray_walk_and_oracle(cuda_device, channels, curved):
+@pytest.mark.parametrize("sdd", [45.0, 32.0])
+def test_downstream_lattice_walk_matches_per_ray_walk_and_oracle(cuda_device, channels, curved, sdd):
     """The shared per-direction crossing table against the independent per-ray walk and the float64 oracle, with
-    directions along the axes, in the planes of two axes and oblique, on a grid with unequal voxel sizes."""
+    directions along the axes, in the planes of two axes and oblique, on a grid with unequal voxel sizes; with the
+    panel beyond the grid (sdd 45) and through it (sdd 32: rays end at the panel, inside the box)."""
     grid = Grid((9, 7, 6), 1.1, 0.8 / 1.1, 1.3 / 1.1)
     rng = np.random.default_rng(channels)
     vol_np = rng.random((channels, *grid.shape))
-    geo = ConeGeometry(30.0, 45.0, 10, 12, 1.5, 1.5, use_curved_detector=curved)
+    geo = ConeGeometry(30.0, sdd, 10, 12, 1.5, 1.5, use_curved_detector=curved)
     angle = 0.4
     n_hat = np.asarray(geo.panel_axes(angle)[2])
     om = rng.standard_normal((40, 3))
