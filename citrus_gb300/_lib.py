@@ -30,6 +30,7 @@ SIGNATURES = {
     "citrus_sweep_persistent_static": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, P],
     "citrus_small_k_gemm": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P],
     "citrus_small_k_gemm_config": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, I32, I32, P],
+    "citrus_source_expansion_first": [P, I64, P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I64, P],
     "citrus_small_k_gemm_bf16x3": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P, P],
     "citrus_state_encode": [P, I64, I64, I64, I64, I64, I64, P, P, P],
     "citrus_state_decode": [P, P, I64, I64, I64, P, I64, I64, I64, I64, P],
@@ -45,6 +46,7 @@ SIGNATURES = {
     "citrus_first_collision_moments": [P, I64, P, I64, P, P, I64, P, P, I64, F64, F64, P, I64, P, P, P, P, P, I64,
                                        P],
     "citrus_first_collision_correction": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, P, I64, P, P, P, P, P, P],
+    "citrus_first_collision_means": [I64, P, P, P, P, I64, P, P, P, P, P, I64, P],
     "citrus_attenuated_emission": [P, I64, P, I64, P, P, I64, P, P, P, I64, F64, F64, P, I64, P, P, I64, P, P, P, P,
                                    P, P, I64, P, P],
     "citrus_attenuated_emission_moments": [P, I64, P, I64, P, P, I64, P, P, P, I64, F64, F64, P, I64, P, P, I64, P, P,

@@ -75,22 +75,37 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
         views = list(range(b0, min(V, b0 + batch)))
         B = len(views)
         store = torch.empty(B, 8, D8, N, Q, device=device)
-        phi_uc = []
-        for j, v in enumerate(views):
+        phi_uc, firsts = [], []
+        for v in views:
             uc = solver.uncollided_fluence(fields, float(angles[v]))
-            first = solver.first_collision_moment_source(fields, float(angles[v]), uc, ctx)
-            first(index, out=store[j].view((8 * D8,) + shape + (G, 4)))
+            firsts.append(solver.first_collision_moment_source(fields, float(angles[v]), uc, ctx))
             phi_uc.append(uc)
         previous = [states[v].collided_moments for v in views]
         # the previous scalar flux, kept for the change norm before an in-place store overwrites it
         previous_scalar = [None if p is None else p[:, 0, 0].clone() for p in previous]
-        if any(p is not None for p in previous):
+        warm = any(p is not None for p in previous)
+        # with one point per cell the first-collision moments are (mean, 0, 0, 0): their means go into the float32
+        # source expansion's output pass instead of being written into the store and read back by it (in either
+        # moment precision: the single pass moves less than half the bytes of the two, whichever form the product takes)
+        fused = warm and N_sh <= 64 and all(f.means is not None for f in firsts)
+        if fused:
+            means = torch.empty(B, 8 * D8, N * G, device=device)
+            for j, first in enumerate(firsts):
+                first.means(index, out=means[j])
+        else:
+            for j, first in enumerate(firsts):
+                first(index, out=store[j].view((8 * D8,) + shape + (G, 4)))
+        if warm:
             T_all = torch.zeros(B, N_sh, J, device=device)
             for j, p in enumerate(previous):
                 if p is not None:
                     kernels.scattering_moments(fields.mu_s_l_coarse, p, "cell_major",
                                                out=T_all[j].view((N_sh,) + shape + (G, 4)))
-            kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
+            if fused:
+                kernels.source_expansion_first(Y, T_all, store.view(B, 8 * D8, J), means)
+                del means
+            else:
+                kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
             del T_all
         syncs.append(kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c, method="persistent",
                                           lanes_per_thread=lanes))

@@ -798,7 +798,9 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_correction_kernel(
 // A block is 32 cells by the G groups by kFcBatch directions of the chunk: S_FC read from cache [K, G, V] at the
 // chunk direction's cache_index, corrected (scale (1 + beta cos)) and restricted to the cell's LD moments; the
 // block's [cells, G, 4] tile goes out through shared memory as contiguous float4 rows.
-template <int kGP>
+// kMean: one point per cell, whose LD slopes vanish; only the mean is written, out [K, NC, G] (direction stride
+// out_k_stride floats) instead of the quadruples [K, NC, G, 4]
+template <int kGP, bool kMean = false>
 __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
     FCInputs in, PointGrid pg, const float* __restrict__ omegas, int K, const float* __restrict__ cache,
     const int32_t* __restrict__ cache_index, const float* __restrict__ scale, const float* __restrict__ beta,
@@ -864,7 +866,8 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
       r.z = my * (inv * slope_scale);
       r.w = mz * (inv * slope_scale);
     }
-    reinterpret_cast<float4*>(out + d * out_k_stride)[c * G + g] = r;
+    if (kMean) out[d * out_k_stride + c * G + g] = r.x;
+    else reinterpret_cast<float4*>(out + d * out_k_stride)[c * G + g] = r;
   }
 }
 
@@ -1039,14 +1042,14 @@ int launch_fc_correction(dim3 grid, int G, cudaStream_t s, const FCInputs& in, c
                                             cache);
 }
 
-template <int kGP>
+template <int kGP, bool kMean = false>
 void launch_fc_moments_cached(int64_t NC, int G, int K, cudaStream_t s, const FCInputs& in, const PointGrid& pg,
                               const float* omegas, const float* cache, const int32_t* cache_index,
                               const float* scale, const float* beta, float slope_scale, float* out,
                               int64_t out_k_stride) {
   dim3 grid((unsigned)cdiv(NC, kEmitPoints), (unsigned)cdiv(K, kFcBatch));
-  fc_moments_cached_kernel<kGP><<<grid, dim3(kEmitPoints, G), 0, s>>>(in, pg, omegas, K, cache, cache_index, scale,
-                                                                      beta, slope_scale, out, out_k_stride);
+  fc_moments_cached_kernel<kGP, kMean><<<grid, dim3(kEmitPoints, G), 0, s>>>(
+      in, pg, omegas, K, cache, cache_index, scale, beta, slope_scale, out, out_k_stride);
   note_launches();
 }
 
@@ -1101,6 +1104,30 @@ extern "C" int citrus_first_collision_moments(const float* rho, int64_t num_mate
   CITRUS_G_DISPATCH(G, fc_moments_kernel, grid, block, 0, s, in, tb, pg, omegas, K, scale, beta, slope_scale, out,
                     out_direction_stride)
   return launch_status("citrus_first_collision_moments");
+}
+
+extern "C" int citrus_first_collision_means(int64_t num_groups, const float* axes, const int64_t* point_dims,
+                                            const double* focal_spot, const float* omegas, int64_t num_directions,
+                                            const float* scale, const float* beta, const float* cache,
+                                            const int32_t* cache_index, float* out, int64_t out_direction_stride,
+                                            void* stream) {
+  CITRUS_REQUIRE(axes && point_dims && focal_spot && omegas && scale && beta && cache && cache_index && out,
+                 "citrus_first_collision_means: null pointer");
+  CITRUS_REQUIRE(num_groups >= 1 && num_groups <= 32 && num_directions <= 65535,
+                 "citrus_first_collision_means: bad sizes");
+  const int64_t V = point_dims[0] * point_dims[1] * point_dims[2];
+  CITRUS_REQUIRE(out_direction_stride >= V * num_groups, "citrus_first_collision_means: direction stride too small");
+  if (V == 0 || num_directions == 0) return CITRUS_OK;
+  const FCInputs in = make_inputs(nullptr, nullptr, axes, V, focal_spot, point_dims);  // points only
+  const PointGrid pg = make_grid(point_dims, 1);
+  const int G = (int)num_groups, K = (int)num_directions;
+  cudaStream_t s = as_stream(stream);
+#define CITRUS_FCM(GP) \
+  (launch_fc_moments_cached<GP, true>(V, G, K, s, in, pg, omegas, cache, cache_index, scale, beta, 0.f, out, \
+                                      out_direction_stride), 0)
+  (void)CITRUS_GP_DISPATCH(G, CITRUS_FCM);
+#undef CITRUS_FCM
+  return launch_status("citrus_first_collision_means");
 }
 
 extern "C" int citrus_first_collision_correction(const float* rho, int64_t num_materials, const float* phi,

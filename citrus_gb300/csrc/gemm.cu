@@ -103,11 +103,17 @@ __global__ void __launch_bounds__(kThreads) small_k_gemm_kernel(const float* __r
 constexpr int kStreamThreads = 128;
 constexpr int kStreamRows = 128;  // rows of A per block of the column-stationary form
 
-template <int kKP, bool kPair, bool kAccumulate>
+// kMode: 0 C = A B, 1 C += A B, 2 C = A B plus, in the first of every four columns, the matching element of F (the
+// means [M, J / 4] of a store of LD moment quadruples, the others zero), i.e. C = A B + the quadruples (F, 0, 0, 0)
+// without reading C (pairs of columns only)
+template <int kKP, bool kPair, int kMode>
 __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* __restrict__ A, int64_t lda,
                                                                   const float* __restrict__ B, int64_t ldb,
                                                                   float* __restrict__ C, int64_t ldc, int M, int K,
-                                                                  int64_t J, int64_t stride_b, int64_t stride_c) {
+                                                                  int64_t J, int64_t stride_b, int64_t stride_c,
+                                                                  const float* __restrict__ F, int64_t ldf,
+                                                                  int64_t stride_f) {
+  constexpr bool kAccumulate = kMode == 1;
   extern __shared__ float4 s_a4[];
   float (*As)[kKP] = reinterpret_cast<float (*)[kKP]>(s_a4);  // [kStreamRows + 3][kKP], zero past the tile
   constexpr int kCols = kPair ? 2 : 1;
@@ -119,6 +125,7 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* 
   }
   B += blockIdx.z * stride_b;
   C += blockIdx.z * stride_c;
+  if (kMode == 2) F += blockIdx.z * stride_f;
   const int64_t col = ((int64_t)blockIdx.x * kStreamThreads + threadIdx.x) * kCols;
   const bool valid = col < J;
   float b0[kKP], b1[kKP];
@@ -174,6 +181,13 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* 
         a0[q] += o[q].x;
         a1[q] += o[q].y;
       }
+    }
+    if (kMode == 2 && (col & 3) == 0) {  // the four means before the first store
+      float f[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) f[q] = r0 + q < rows ? F[(int64_t)(row0 + r0 + q) * ldf + (col >> 2)] : 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a0[q] += f[q];
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -279,19 +293,20 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_rows_kernel(const float* 
   }
 }
 
-template <int kKP, bool kPair, bool kAcc>
+template <int kKP, bool kPair, int kMode>
 int launch_cols(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int M, int K,
-                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, cudaStream_t s) {
+                int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c, cudaStream_t s,
+                const float* F = nullptr, int64_t ldf = 0, int64_t stride_f = 0) {
   const int64_t cols_per_block = (int64_t)kStreamThreads * (kPair ? 2 : 1);
   const size_t smem = (size_t)(kStreamRows + 3) * kKP * sizeof(float);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_cols_kernel<kKP, kPair, kAcc>,
+    cudaError_t e = cudaFuncSetAttribute(gemm_cols_kernel<kKP, kPair, kMode>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm: %s", cudaGetErrorString(e));
   }
   dim3 grid((unsigned)cdiv(J, cols_per_block), (unsigned)cdiv(M, kStreamRows), (unsigned)batch);
-  gemm_cols_kernel<kKP, kPair, kAcc><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
-                                                                       stride_c);
+  gemm_cols_kernel<kKP, kPair, kMode><<<grid, kStreamThreads, smem, s>>>(A, lda, B, ldb, C, ldc, M, K, J, stride_b,
+                                                                        stride_c, F, ldf, stride_f);
   note_launches();
   return launch_status("citrus_small_k_gemm");
 }
@@ -424,6 +439,32 @@ extern "C" int citrus_small_k_gemm_config(const float* A, int64_t lda, const flo
     return set_error(CITRUS_EINVAL, "citrus_small_k_gemm: K %lld too large for a shared-memory tile of %d row groups",
                      (long long)K, tile);
   return launch_tiled(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, accumulate, tile, s);
+}
+
+extern "C" int citrus_source_expansion_first(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                                             int64_t ldc, const float* F, int64_t ldf, int64_t M, int64_t K,
+                                             int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
+                                             int64_t stride_f, void* stream) {
+  CITRUS_REQUIRE(A && B && C && F, "citrus_source_expansion_first: null pointer argument");
+  CITRUS_REQUIRE(M >= 1 && K >= 1 && K <= 64 && J >= 0 && batch >= 1 && batch <= 65535 && M <= (1 << 20),
+                 "citrus_source_expansion_first: bad sizes M %lld K %lld (at most 64) J %lld batch %lld",
+                 (long long)M, (long long)K, (long long)J, (long long)batch);
+  CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J && ldf >= J / 4,
+                 "citrus_source_expansion_first: leading dimensions too small");
+  CITRUS_REQUIRE(J % 4 == 0 && ldb % 2 == 0 && ldc % 2 == 0 && stride_b % 2 == 0 && stride_c % 2 == 0 &&
+                     ((uintptr_t)B % 8) == 0 && ((uintptr_t)C % 8) == 0,
+                 "citrus_source_expansion_first: columns must come in quadruples of 8-byte aligned pairs");
+  if (J == 0) return CITRUS_OK;
+  const int m = (int)M, k = (int)K;
+  cudaStream_t s = as_stream(stream);
+#define CITRUS_EXPAND(KP) \
+  launch_cols<KP, true, 2>(A, lda, B, ldb, C, ldc, m, k, J, batch, stride_b, stride_c, s, F, ldf, stride_f)
+  if (K <= 16) return CITRUS_EXPAND(16);
+  if (K <= 32) return CITRUS_EXPAND(32);
+  if (K <= 36) return CITRUS_EXPAND(36);
+  if (K <= 48) return CITRUS_EXPAND(48);
+  return CITRUS_EXPAND(64);
+#undef CITRUS_EXPAND
 }
 
 extern "C" int citrus_small_k_gemm(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,

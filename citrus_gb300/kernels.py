@@ -134,6 +134,34 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
 # small-K products
 # =====================================================================================================================
 
+def source_expansion_first(A: Tensor, B: Tensor, C: Tensor, F: Tensor) -> Tensor:
+    """``C[b] = A @ B[b]`` plus the LD quadruples ``(F[b], 0, 0, 0)``: the source of an accumulator sweep (the
+    expansion ``Y @ T`` of ``transport_sweep.py:524`` added to first-collision moments of one point per cell, given by
+    their means) in one float32 pass that writes C without reading it; the same values as writing the quadruples into
+    C and accumulating ``small_k_gemm(A, B, C)`` over them.
+
+    Args:
+        A: [M, K] float32 contiguous, K <= 64.
+        B: [batch, K, J] float32 contiguous, J a multiple of 4.
+        C: [batch, M, J] float32 contiguous output.
+        F: [batch, M, J // 4] float32 contiguous means.
+    """
+    for name, t in (("A", A), ("B", B), ("C", C), ("F", F)):
+        _check_cuda_f32(name, t)
+    if A.dim() != 2 or B.dim() != 3 or C.dim() != 3 or F.dim() != 3:
+        raise ValueError("A must be [M, K], B [batch, K, J], C [batch, M, J], F [batch, M, J / 4]")
+    M, K = A.shape
+    batch, _, J = B.shape
+    if tuple(B.shape) != (batch, K, J) or tuple(C.shape) != (batch, M, J) or tuple(F.shape) != (batch, M, J // 4):
+        raise ValueError(f"shapes A {tuple(A.shape)}, B {tuple(B.shape)}, C {tuple(C.shape)}, F {tuple(F.shape)} "
+                         "do not chain")
+    if J % 4 or K > 64:
+        raise ValueError("J must be a multiple of 4 and K at most 64")
+    _lib.call("citrus_source_expansion_first", A.data_ptr(), K, B.data_ptr(), J, C.data_ptr(), J, F.data_ptr(),
+              J // 4, M, K, J, batch, K * J, M * J, M * (J // 4), _lib.stream_handle(C.device))
+    return C
+
+
 PRECISIONS = ("fp32", "bf16x3")
 
 

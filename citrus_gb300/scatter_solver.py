@@ -31,8 +31,9 @@ from .scatter_image import (combined_scatter_image, make_direction_context, pane
 from .source_iteration import (SourceIterationResult, multiple_collision_source_moments, scatter_moments,
                                scatter_source_function, source_iteration)
 from .transport_sweep import SweepContext, make_sweep_context, sweep
-from .uncollided import (FirstCollisionSamplingCorrection, first_collision_moments_at_directions,
-                         first_collision_sampling_correction, present_materials, uncollided_fluence)
+from .uncollided import (FirstCollisionSamplingCorrection, first_collision_means_at_directions,
+                         first_collision_moments_at_directions, first_collision_sampling_correction,
+                         present_materials, uncollided_fluence)
 
 SWEEP_CHUNK_BUDGET_BYTES = 8 * 2 ** 30
 IMAGE_CHUNK_BUDGET_BYTES = 4 * 2 ** 30
@@ -286,7 +287,17 @@ class ScatterSolver:
                                                          correction, fields.q, out=out, cell_major=True,
                                                          direction_index=index)
 
+        def means(direction_index: Tensor, out: Optional[Tensor] = None) -> Tensor:
+            """[K, NC, G] means of the same moments (one point per cell, cached source values only)."""
+            index = direction_index.to(self.device)
+            return first_collision_means_at_directions(library, fields.rho_quadrature, phi_uncollided,
+                                                       fields.grid_quadrature, geometry, angle,
+                                                       omega.index_select(0, index), correction, index, out=out)
+
         source_function.cell_major = True  # type: ignore[attr-defined]
+        # the moments are (mean, 0, 0, 0) quadruples when a cell holds one point and the correction kept its source
+        # values: then the means alone describe them
+        source_function.means = means if (fields.q == 1 and correction.cache is not None) else None  # type: ignore
         return source_function
 
     def scatter_moment_source(self, fields: MaterialFields, phi: Tensor,

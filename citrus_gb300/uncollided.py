@@ -219,6 +219,32 @@ def first_collision_source_at_directions(library: MultigroupLibrary, rho: Tensor
     return out
 
 
+def first_collision_means_at_directions(library: MultigroupLibrary, rho: Tensor, phi_uncollided: Tensor, grid: Grid,
+                                        geometry: ConeGeometry, angle: float, omegas: Tensor,
+                                        correction: FirstCollisionSamplingCorrection, direction_index: Tensor,
+                                        out: Optional[Tensor] = None) -> Tensor:
+    """[K, NC, G] means of the LD moments of the corrected source with one point per cell (whose slopes vanish), read
+    from the correction's cached source values: the first components of ``first_collision_moments_at_directions``
+    (reference ``uncollided.py:464-511``), for the fused source expansion of an accumulator sweep."""
+    if correction.cache is None:
+        raise ValueError("the correction did not keep its source values")
+    a = _FCArgs(library, rho, phi_uncollided, grid, geometry, angle)
+    om = omegas.to(device=a.device, dtype=torch.float32).reshape(-1, 3).contiguous()
+    K = om.shape[0]
+    index = direction_index.to(device=a.device, dtype=torch.int32).reshape(-1).contiguous()
+    if index.numel() != K:
+        raise ValueError("direction_index must give one cache row per direction")
+    expected = (K, a.V, a.G)
+    if out is None:
+        out = torch.empty(expected, device=a.device)
+    elif out.numel() != K * a.V * a.G or not out.is_contiguous() or out.dtype != torch.float32:
+        raise ValueError(f"out must be a contiguous float32 tensor of {K * a.V * a.G} elements")
+    _lib.call("citrus_first_collision_means", a.G, a.axes.data_ptr(), a.dims, a.focal, om.data_ptr(), K,
+              correction.scale.contiguous().data_ptr(), correction.beta.contiguous().data_ptr(),
+              correction.cache.data_ptr(), index.data_ptr(), out.data_ptr(), a.V * a.G, a.stream)
+    return out.view(expected)
+
+
 def first_collision_moments_at_directions(library: MultigroupLibrary, rho: Tensor, phi_uncollided: Tensor, grid: Grid,
                                           geometry: ConeGeometry, angle: float, omegas: Tensor,
                                           correction: FirstCollisionSamplingCorrection, factor: int,

@@ -107,6 +107,16 @@ int citrus_small_k_gemm_config(const float* A, int64_t lda, const float* B, int6
                                int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
                                int32_t accumulate, int32_t variant, int32_t tile_rows, void* stream);
 
+/* The source of an accumulator sweep in one pass: C[b] = A B[b] + the quadruples (F[b], 0, 0, 0), i.e. the source
+ * expansion Y @ T (transport_sweep.py:524, source_iteration.py:94) added to the first-collision LD moments of one
+ * point per cell given by their means F[b] [M, J / 4] (ldf floats per row, stride_f floats between batches), without
+ * reading C. The float32 column-stationary form of citrus_small_k_gemm: the same products in the same order, so C
+ * equals that of citrus_first_collision_moments followed by an accumulating citrus_small_k_gemm. K <= 64, J a multiple
+ * of 4, B and C in 8-byte aligned column pairs. */
+int citrus_source_expansion_first(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                                  const float* F, int64_t ldf, int64_t M, int64_t K, int64_t J, int64_t batch,
+                                  int64_t stride_b, int64_t stride_c, int64_t stride_f, void* stream);
+
 /* The same product on the tcgen05 tensor cores, M <= 128 and K <= 128: each float32 operand is split into a bfloat16
  * high part and a bfloat16 low part (x - hi), the product accumulated in float32 as A_hi B_hi + A_hi B_lo + A_lo B_hi
  * (relative error ~1e-5 of the largest term). error_word (NULL: none), when given, is set to 1 if a wait for the
@@ -216,6 +226,16 @@ int citrus_first_collision_moments(const float* rho, int64_t num_materials, cons
                                    double eta_hi, const float* omegas, int64_t num_directions, const float* scale,
                                    const float* beta, const float* cache, const int32_t* cache_index, float* out,
                                    int64_t out_direction_stride, void* stream);
+
+/* The means of the first-collision LD moments at one point per cell (points_per_cell 1, where the slopes vanish),
+ * from the S_FC that citrus_first_collision_correction cached (cache row cache_index[k] for chunk direction k): out
+ * [K, NC, G] with out_direction_stride floats between directions, the first components of the quadruples that
+ * citrus_first_collision_moments writes; read by citrus_source_expansion_first. Part of
+ * first_collision_moments_at_directions (uncollided.py:464-511, uncollided_kernels.py:552-634). */
+int citrus_first_collision_means(int64_t num_groups, const float* axes, const int64_t* point_dims,
+                                 const double* focal_spot, const float* omegas, int64_t num_directions,
+                                 const float* scale, const float* beta, const float* cache, const int32_t* cache_index,
+                                 float* out, int64_t out_direction_stride, void* stream);
 
 /* Sampling correction: quadrature sums I0, I1, I2 over the K sweep directions (weights [K]) and exact moments E0, E1
  * from moments [M, 2, G_out, G_in] (Legendre l = 0, 1), optionally stored in sums [5, G, V], and the float64 factors

@@ -35,6 +35,30 @@ def test_batched_steps_equal_per_view_steps(cuda_device, name):
 
 
 @pytest.mark.parametrize("name", ["flat", "curved"])
+def test_one_point_per_cell_batched_steps_equal_per_view_steps(cuda_device, name):
+    """One point per transport cell: the warm batched steps form the sweep source in one pass from the first-collision
+    means (citrus_first_collision_means, citrus_source_expansion_first); the per-view steps write the moment
+    quadruples and accumulate the expansion over them. Same states and signals."""
+    g, solver = _solver(name, cuda_device, quadrature_point_spacing_cm=2.0)
+    grid = Grid((8, 8, 6), 1.0)
+    fields = solver.material_fields(torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device), grid)
+    assert fields.q == 1
+    angles = [0.3, 1.7, 4.0]
+    single = [CitrusState() for _ in angles]
+    batched = [CitrusState() for _ in angles]
+    for _ in range(3):
+        ref = []
+        for v, a in enumerate(angles):
+            s, _, single[v] = citrus_view_step(solver, single[v], fields, a, primary=False)
+            ref.append(s)
+        signals, _, batched = batched_view_steps(solver, batched, fields, angles, batch=2)
+        for v in range(len(angles)):
+            assert rel_err(signals[v], ref[v]) < 1e-6
+            assert rel_err(batched[v].collided_moments, single[v].collided_moments) < 1e-6
+            assert abs(batched[v].history[-1] - single[v].history[-1]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["flat", "curved"])
 def test_graphed_outer_iterations_equal_batched_steps(cuda_device, name):
     """The outer iteration recorded into a CUDA graph (accumulators updated in place) gives the eager batched steps'
     results on every replay, including after the densities change."""

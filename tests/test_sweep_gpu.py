@@ -7,7 +7,7 @@ import pytest
 import torch
 
 from conftest import golden, rel_err
-from citrus_gb300 import kernels
+from citrus_gb300 import _lib, kernels
 from citrus_gb300.geometry import Grid
 from citrus_gb300.quadrature import product_quadrature
 from citrus_gb300.source_iteration import scatter_moments, scatter_source_function, source_iteration
@@ -114,6 +114,29 @@ def test_small_k_gemm_matches_numpy(cuda_device, M, K, J, batch, accumulate):
     C = dev(C0)
     kernels.small_k_gemm(dev(A), dev(B), C, accumulate=accumulate)
     assert rel_err(C, expected) < 1e-5
+
+
+@pytest.mark.parametrize("M, K, J, batch", [(120, 36, 4096, 2), (133, 36, 2060, 1), (5, 7, 64, 3), (1, 1, 4, 1),
+                                            (64, 64, 1032, 2), (17, 20, 516, 1)])
+def test_source_expansion_with_first_collision_means_equals_two_passes(cuda_device, M, K, J, batch):
+    """C = A B + (F, 0, 0, 0) in one pass equals the quadruples written into C and an accumulating product over them
+    (the same products in the same order), bit for bit."""
+    rng = np.random.default_rng(M + K + J)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    A, B, F = dev(rng.standard_normal((M, K))), dev(rng.standard_normal((batch, K, J))), dev(
+        rng.standard_normal((batch, M, J // 4)))
+    two = torch.zeros(batch, M, J // 4, 4, device=cuda_device)
+    two[..., 0] = F
+    two = two.reshape(batch, M, J)
+    # the accumulating product in its streaming (column-stationary) form, the one the single pass extends
+    _lib.call("citrus_small_k_gemm_config", A.data_ptr(), K, B.data_ptr(), J, two.data_ptr(), J, M, K, J, batch,
+              K * J, M * J, 1, 1, 0, _lib.stream_handle(two.device))
+    one = torch.full((batch, M, J), float("nan"), device=cuda_device)
+    kernels.source_expansion_first(A, B, one, F)
+    assert torch.equal(one, two)
+    expected = np.einsum("mk,bkj->bmj", A.cpu().numpy().astype(np.float64), B.cpu().numpy().astype(np.float64))
+    expected.reshape(batch, M, J // 4, 4)[..., 0] += F.cpu().numpy()
+    assert rel_err(one, expected) < 1e-5
 
 
 @pytest.mark.parametrize("M, K, J, batch, accumulate", [(120, 36, 4096, 1, False), (36, 120, 1028, 1, True),
