@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
           t = __ldg(tp);
         }
         const float depth = pg.f > 1 ? fmaxf(t - muc * offset, 0.f) : fmaxf(t, 0.f);
-        e = (src + smc) * expf(-depth);
+        e = (src + smc) * __expf(-depth);  // the fast exponential: within a few ulp for these depths
       }
       // group sums over the kGP lanes of the point (in group order), then the warp's points
       float tot = e, sgl = signal_weight != nullptr ? s_sw[dd][g] * e : 0.f;
@@ -798,9 +798,7 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_correction_kernel(
 // A block is 32 cells by the G groups by kFcBatch directions of the chunk: S_FC read from cache [K, G, V] at the
 // chunk direction's cache_index, corrected (scale (1 + beta cos)) and restricted to the cell's LD moments; the
 // block's [cells, G, 4] tile goes out through shared memory as contiguous float4 rows.
-// kMean: one point per cell, whose LD slopes vanish; only the mean is written, out [K, NC, G] (direction stride
-// out_k_stride floats) instead of the quadruples [K, NC, G, 4]
-template <int kGP, bool kMean = false>
+template <int kGP>
 __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
     FCInputs in, PointGrid pg, const float* __restrict__ omegas, int K, const float* __restrict__ cache,
     const int32_t* __restrict__ cache_index, const float* __restrict__ scale, const float* __restrict__ beta,
@@ -866,8 +864,51 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_moments_cached_kernel(
       r.z = my * (inv * slope_scale);
       r.w = mz * (inv * slope_scale);
     }
-    if (kMean) out[d * out_k_stride + c * G + g] = r.x;
-    else reinterpret_cast<float4*>(out + d * out_k_stride)[c * G + g] = r;
+    reinterpret_cast<float4*>(out + d * out_k_stride)[c * G + g] = r;
+  }
+}
+
+// The means alone, for one point per cell (whose LD slopes vanish): out [K, NC, G] with out_k_stride floats between
+// directions. A block is 32 cells by the G groups and 16 directions: it reads the cached source rows [g][cells] whole
+// (a warp per group) and writes each direction's [cells, G] run whole, through shared memory.
+template <int kGP>
+__global__ void __launch_bounds__(kEmitPoints * kGP) fc_means_kernel(
+    FCInputs in, PointGrid pg, const float* __restrict__ omegas, int K, const float* __restrict__ cache,
+    const int32_t* __restrict__ cache_index, const float* __restrict__ scale, const float* __restrict__ beta,
+    float* __restrict__ out, int64_t out_k_stride) {
+  constexpr int kPass = kGP >= 16 ? 128 / kGP : kFcBatch;  // directions per shared-memory pass (16 KB)
+  __shared__ float s_out[kPass][kEmitPoints * kGP];
+  const int G = (int)blockDim.y;
+  const int x = threadIdx.x, g = threadIdx.y, tid = g * kEmitPoints + x;
+  const int64_t c0 = (int64_t)blockIdx.x * kEmitPoints;
+  const int64_t c = c0 + x;  // one point per cell: the cell is the point
+  const int n = (int)min((int64_t)kEmitPoints, in.V - c0);  // cells of this block
+  float ux = 0.f, uy = 0.f, uz = 0.f, sc = 0.f, be = 0.f;
+  if (x < n) {
+    int i, j, k;
+    point_rcs(c, pg, i, j, k);
+    primary_direction(__ldg(in.ax_x + j), __ldg(in.ax_y + i), __ldg(in.ax_z + k), in.r0x, in.r0y, in.r0z, ux, uy, uz);
+    sc = __ldg(scale + (int64_t)g * in.V + c);
+    be = __ldg(beta + (int64_t)g * in.V + c);
+  }
+  const int d0 = blockIdx.y * kFcBatch, dlast = min(K, d0 + kFcBatch);
+  for (int p0 = d0; p0 < dlast; p0 += kPass) {
+    const int np = min(kPass, dlast - p0);
+#pragma unroll 4
+    for (int q = 0; q < np; ++q) {
+      const int d = p0 + q;
+      float r = 0.f;
+      if (x < n) {
+        const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+        const float cosine = ux * ox + uy * oy + uz * oz;
+        r = __ldg(cache + ((int64_t)__ldg(cache_index + d) * G + g) * in.V + c) * sc * (1.f + be * cosine);
+      }
+      s_out[q][x * G + g] = r;
+    }
+    __syncthreads();
+    for (int q = 0; q < np; ++q)
+      if (tid < n * G) out[(int64_t)(p0 + q) * out_k_stride + c0 * G + tid] = s_out[q][tid];
+    __syncthreads();
   }
 }
 
@@ -1042,14 +1083,24 @@ int launch_fc_correction(dim3 grid, int G, cudaStream_t s, const FCInputs& in, c
                                             cache);
 }
 
-template <int kGP, bool kMean = false>
+template <int kGP>
 void launch_fc_moments_cached(int64_t NC, int G, int K, cudaStream_t s, const FCInputs& in, const PointGrid& pg,
                               const float* omegas, const float* cache, const int32_t* cache_index,
                               const float* scale, const float* beta, float slope_scale, float* out,
                               int64_t out_k_stride) {
   dim3 grid((unsigned)cdiv(NC, kEmitPoints), (unsigned)cdiv(K, kFcBatch));
-  fc_moments_cached_kernel<kGP, kMean><<<grid, dim3(kEmitPoints, G), 0, s>>>(
-      in, pg, omegas, K, cache, cache_index, scale, beta, slope_scale, out, out_k_stride);
+  fc_moments_cached_kernel<kGP><<<grid, dim3(kEmitPoints, G), 0, s>>>(in, pg, omegas, K, cache, cache_index, scale,
+                                                                      beta, slope_scale, out, out_k_stride);
+  note_launches();
+}
+
+template <int kGP>
+void launch_fc_means(int G, int K, cudaStream_t s, const FCInputs& in, const PointGrid& pg, const float* omegas,
+                     const float* cache, const int32_t* cache_index, const float* scale, const float* beta, float* out,
+                     int64_t out_k_stride) {
+  dim3 grid((unsigned)cdiv(in.V, kEmitPoints), (unsigned)cdiv(K, kFcBatch));
+  fc_means_kernel<kGP><<<grid, dim3(kEmitPoints, G), 0, s>>>(in, pg, omegas, K, cache, cache_index, scale, beta, out,
+                                                             out_k_stride);
   note_launches();
 }
 
@@ -1123,8 +1174,7 @@ extern "C" int citrus_first_collision_means(int64_t num_groups, const float* axe
   const int G = (int)num_groups, K = (int)num_directions;
   cudaStream_t s = as_stream(stream);
 #define CITRUS_FCM(GP) \
-  (launch_fc_moments_cached<GP, true>(V, G, K, s, in, pg, omegas, cache, cache_index, scale, beta, 0.f, out, \
-                                      out_direction_stride), 0)
+  (launch_fc_means<GP>(G, K, s, in, pg, omegas, cache, cache_index, scale, beta, out, out_direction_stride), 0)
   (void)CITRUS_GP_DISPATCH(G, CITRUS_FCM);
 #undef CITRUS_FCM
   return launch_status("citrus_first_collision_means");
