@@ -679,21 +679,26 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
                                                                       const int32_t* __restrict__ table,
                                                                       float* __restrict__ out, int64_t os_k,
                                                                       int64_t os_c, int64_t os_v) {
-  extern __shared__ int32_t s_tab[];  // [4E] of this direction: t, dv, first, and the segment lengths
+  // [4E] words of this direction: the steps (segment length, flat index step) as int2 [E] (E rounded up to even, so
+  // that two steps are one 16-byte load), then t [E] and first [E]
+  extern __shared__ int4 s_tab4[];
   const int k = blockIdx.y;
   const int E = b.n[0] + b.n[1] + b.n[2];
+  const int E2 = (E + 1) & ~1;
+  int2* s_step = reinterpret_cast<int2*>(s_tab4);
+  int32_t* s_words = reinterpret_cast<int32_t*>(s_tab4) + 2 * E2;
   const int32_t* src = table + (int64_t)k * 3 * E;
-  for (int i = threadIdx.x; i < 3 * E; i += kThreads) s_tab[i] = src[i];
-  // the length of the segment that ends at crossing j: t[j] - t[j - 1] (t[-1] = 0), as the walk forms it
   for (int i = threadIdx.x; i < E; i += kThreads) {
+    // the length of the segment that ends at crossing i: t[i] - t[i - 1] (t[-1] = 0), as the walk forms it
     const float tj = __int_as_float(src[i]), tp = i > 0 ? __int_as_float(src[i - 1]) : 0.f;
-    s_tab[3 * E + i] = __float_as_int(tj - tp);
+    s_step[i] = make_int2(__float_as_int(tj - tp), src[E + i]);
+    s_words[i] = src[i];
+    s_words[E + i] = src[2 * E + i];
   }
+  if (threadIdx.x == 0 && E2 > E) s_step[E] = make_int2(0, 0);
   __syncthreads();
-  const float* t_cross = reinterpret_cast<const float*>(s_tab);
-  const int32_t* dv = s_tab + E;
-  const int32_t* first = s_tab + 2 * E;
-  const float* ds = reinterpret_cast<const float*>(s_tab + 3 * E);
+  const float* t_cross = reinterpret_cast<const float*>(s_words);
+  const int32_t* first = s_words + E;
   const int64_t v = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   if (v >= V) return;
   const int nC = kC > 0 ? kC : C;
@@ -743,12 +748,14 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
     // four segments at a time: the four gathers are issued before their sums (the crossing table gives every step's
     // voxel in advance)
     for (; j + 4 <= J; j += 4) {
-      const int c1 = cur + dv[j], c2 = c1 + dv[j + 1], c3 = c2 + dv[j + 2];
+      const int4 e01 = s_tab4[j >> 1], e23 = s_tab4[(j >> 1) + 1];  // steps j .. j + 3 (j even)
+      const int c1 = cur + e01.y, c2 = c1 + e01.w, c3 = c2 + e23.y;
       const float2 q0 = __ldg(reinterpret_cast<const float2*>(vol) + cur);
       const float2 q1 = __ldg(reinterpret_cast<const float2*>(vol) + c1);
       const float2 q2 = __ldg(reinterpret_cast<const float2*>(vol) + c2);
       const float2 q3 = __ldg(reinterpret_cast<const float2*>(vol) + c3);
-      const float s0 = ds[j], s1 = ds[j + 1], s2 = ds[j + 2], s3 = ds[j + 3];
+      const float s0 = __int_as_float(e01.x), s1 = __int_as_float(e01.z), s2 = __int_as_float(e23.x),
+                  s3 = __int_as_float(e23.z);
       acc[0] = fmaf(s0, q0.x, acc[0]);
       acc[kC > 1 ? 1 : 0] = fmaf(s0, q0.y, acc[kC > 1 ? 1 : 0]);
       acc[0] = fmaf(s1, q1.x, acc[0]);
@@ -757,14 +764,14 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
       acc[kC > 1 ? 1 : 0] = fmaf(s2, q2.y, acc[kC > 1 ? 1 : 0]);
       acc[0] = fmaf(s3, q3.x, acc[0]);
       acc[kC > 1 ? 1 : 0] = fmaf(s3, q3.y, acc[kC > 1 ? 1 : 0]);
-      cur = c3 + dv[j + 3];
+      cur = c3 + e23.w;
     }
   }
   // the remaining whole segments, then the cut one (step j == J)
   for (; j <= J; ++j) {
     float seg;
     if (j < J) {
-      seg = ds[j];
+      seg = __int_as_float(s_step[j].x);
     } else {
       const float prev = j > 0 ? t_cross[j - 1] : 0.f;
       if (!cut || !(prev < t_end)) break;
@@ -787,7 +794,7 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
     } else {
       for (int c = 0; c < nC; ++c) acc[c] = fmaf(seg, __ldg(vox + c), acc[c]);
     }
-    if (j < J) cur += dv[j];
+    if (j < J) cur += s_step[j].y;
   }
   if ((kC == 8 || kC == 4) && os_c == 1 && os_v == nC) {  // voxel-major out: the channels of a ray in float4s
 #pragma unroll
@@ -962,7 +969,7 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
     CITRUS_REQUIRE(((uintptr_t)out % 16) == 0 && os_k % 4 == 0, "citrus_downstream_cumulative: unaligned out");
   crossing_table_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, s>>>(b, omegas, (int)num_directions, crossings);
   note_launches();
-  const size_t smem = (size_t)4 * E * sizeof(int32_t);
+  const size_t smem = (size_t)(2 * ((E + 1) & ~1) + 2 * E) * sizeof(int32_t);
 #define CITRUS_LATTICE(KC)                                                                                        \
   downstream_lattice_kernel<KC><<<grid, kThreads, smem, s>>>(b, volume, C, omegas, toward, p, (float)diagonal, V, \
                                                             crossings, out, os_k, os_c, os_v)
