@@ -87,8 +87,13 @@ def accumulator_update_operator(solver: ScatterSolver, rho, grid, angle: float, 
         _check_accumulator(solver, fields, collided_moments)
         previous = collided_moments.to(solver.device)
         scatter = solver.scatter_moment_source(fields, previous, ctx)
+        # one point per cell: the first-collision moments are (mean, 0, 0, 0), and their means go into the
+        # expansion's single pass over the store instead of a write of the quadruples and an accumulating pass
+        fused = getattr(first, "means", None) is not None and getattr(scatter, "with_means", None) is not None
 
         def summed_source(direction_index: Tensor, out: Optional[Tensor] = None) -> Tensor:
+            if fused and out is not None:
+                return scatter.with_means(direction_index, first.means(direction_index), out)
             src = first(direction_index, out)                              # cell-major, into the sweep's store
             return scatter(direction_index, out=src, accumulate=True)      # one accumulating small-K product
 

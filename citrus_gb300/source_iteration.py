@@ -61,7 +61,16 @@ def scatter_source_function(ctx: SweepContext, T: Tensor, precision: str = "fp32
                              precision=precision)
         return out
 
+    def with_means(direction_index: Tensor, means: Tensor, out: Tensor) -> Tensor:
+        """``out`` = the same expansion plus the LD quadruples ``(means, 0, 0, 0)`` (means ``[Dsel, R, C, S, G]``)
+        in one float32 pass that writes ``out`` without reading it."""
+        Y_sel = ctx.Y.index_select(0, direction_index.to(ctx.Y.device)).contiguous()
+        D = Y_sel.shape[0]
+        kernels.source_expansion_first(Y_sel, matrix.unsqueeze(0), out.view(1, D, -1), means.reshape(1, D, -1))
+        return out
+
     source.cell_major = True  # type: ignore[attr-defined]
+    source.with_means = with_means if num_moments <= 64 else None  # type: ignore[attr-defined]
     return source
 
 

@@ -58,6 +58,25 @@ def test_one_point_per_cell_batched_steps_equal_per_view_steps(cuda_device, name
             assert abs(batched[v].history[-1] - single[v].history[-1]) < 1e-6
 
 
+def test_first_collision_means_are_the_moments_first_components(cuda_device):
+    """With one point per cell the first-collision LD moments are (mean, 0, 0, 0); citrus_first_collision_means gives
+    the means alone, read from the same cached source values."""
+    g, solver = _solver("curved", cuda_device, quadrature_point_spacing_cm=2.0)
+    fields = solver.material_fields(torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device),
+                                    Grid((8, 8, 6), 1.0))
+    assert fields.q == 1
+    ctx = solver.sweep_context(fields.grid_coarse)
+    uc = solver.uncollided_fluence(fields, 0.9)
+    first = solver.first_collision_moment_source(fields, 0.9, uc, ctx)
+    assert first.means is not None
+    index = torch.arange(ctx.omega.shape[0], device=cuda_device)
+    quads = first(index)
+    means = first.means(index)
+    assert tuple(means.shape) == tuple(quads.shape[:1]) + (ctx.num_cells, solver.num_groups)
+    assert float(quads[..., 1:].abs().max()) == 0.0
+    assert rel_err(means, quads[..., 0].reshape(means.shape)) < 1e-6
+
+
 @pytest.mark.parametrize("name", ["flat", "curved"])
 def test_graphed_outer_iterations_equal_batched_steps(cuda_device, name):
     """The outer iteration recorded into a CUDA graph (accumulators updated in place) gives the eager batched steps'
