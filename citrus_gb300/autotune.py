@@ -165,7 +165,7 @@ UNROLL_CANDIDATES = (1, 3, 5, 2, 4)
 
 
 def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> tuple:
-    """(views per persistent sweep launch, lanes per thread) for ``views`` views on this grid: the per-view time of
+    """(views per persistent sweep launch, sweep thread form) for ``views`` views on this grid: the per-view time of
     the sweep on a store of ones of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device
     memory) in each lanes-per-thread form; the first (fewest views) within 3 % of the fastest."""
     from . import kernels
@@ -187,7 +187,7 @@ def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> 
                 stores.clear()
                 torch.cuda.empty_cache()
                 stores[b] = torch.ones(b, 8, D8, N, Q, device=device)  # non-zero moments, as in a real step
-            kernels.sweep_planes(ctx.flat_index, stores[b], mu_cells, ctx.c, method="persistent", lanes_per_thread=u)
+            kernels.sweep_planes(ctx.flat_index, stores[b], mu_cells, ctx.c, method="persistent", thread_form=u)
 
         tuner().choose(key, candidates, run, list(default), slack=0.03, per_unit=lambda c: float(c[0]))
         stores.clear()

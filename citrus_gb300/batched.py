@@ -34,15 +34,15 @@ def _check_states(states: Sequence[CitrusState], angles: Sequence[float]) -> Non
 
 
 def sweep_launch_config(solver: ScatterSolver, fields: MaterialFields, views: int, batch: int) -> tuple:
-    """(views per sweep launch, lanes per thread of the sweep): the autotuner's choice for this grid, with ``batch``
+    """(views per sweep launch, form of the sweep threads): the autotuner's choice for this grid, with ``batch``
     views when it is positive."""
     from .autotune import sweep_config
 
     ctx = solver.sweep_context(fields.grid_coarse)
     G = solver.num_groups
     mu_cells = fields.mu_t_coarse.reshape(G, ctx.num_cells).t().contiguous()
-    tuned_views, lanes = sweep_config(ctx, mu_cells, G, views)
-    return (min(int(batch), max(1, views)) if batch > 0 else tuned_views), lanes
+    tuned_views, form = sweep_config(ctx, mu_cells, G, views)
+    return (min(int(batch), max(1, views)) if batch > 0 else tuned_views), form
 
 
 def resolve_batch(solver: ScatterSolver, fields: MaterialFields, views: int, batch: int) -> int:
@@ -70,7 +70,7 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
     Yw_t = ctx.Y_weighted.index_select(0, index).t().contiguous()  # [N_sh, 8 D8]
     mu_cells = fields.mu_t_coarse.reshape(G, N).t().contiguous()
     syncs, norms, accumulators = [], [], []
-    batch, lanes = sweep_launch_config(solver, fields, V, batch)
+    batch, form = sweep_launch_config(solver, fields, V, batch)
     for b0 in range(0, V, batch):
         views = list(range(b0, min(V, b0 + batch)))
         B = len(views)
@@ -108,7 +108,7 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
                 kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
             del T_all
         syncs.append(kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c, method="persistent",
-                                          lanes_per_thread=lanes))
+                                          thread_form=form))
         moments = torch.empty(B, N_sh, J, device=device) if store_out is None else store_out[b0:b0 + B]
         kernels.small_k_gemm(Yw_t, store.view(B, 8 * D8, J), moments, precision=precision)
         del store

@@ -239,7 +239,7 @@ int launch_persistent(float* store, const float* mu, const float* c, const int* 
       return launch_persistent_u<kG, 4, 2>(store, mu, c, octant, cell, upstream, offsets, num_planes, N, G, Dc,
                                            views, sync, max_blocks, timeout_ns, skip, stream);
     default:
-      return set_error(CITRUS_EINVAL, "citrus_sweep_persistent: lanes per thread form %d (1, 2, 3, 4 or 5)", unroll);
+      return set_error(CITRUS_EINVAL, "citrus_sweep_persistent: thread form %d (1, 2, 3, 4 or 5)", unroll);
   }
 }
 
@@ -294,7 +294,7 @@ extern "C" int citrus_sweep_persistent_config(float* store, const float* mu_cell
                                               const int32_t* octant, const int32_t* cell, const int32_t* upstream,
                                               const int32_t* plane_offsets_dev, int64_t num_planes, int64_t num_cells,
                                               int64_t num_groups, int64_t dc, int64_t views, uint32_t* sync,
-                                              int64_t max_blocks, int32_t lanes_per_thread, int64_t timeout_ns,
+                                              int64_t max_blocks, int32_t thread_form, int64_t timeout_ns,
                                               int64_t skip_block, void* stream) {
   int status = check_sweep_args(store, mu_cells, c, octant, cell, upstream, num_planes, num_cells, num_groups, dc,
                                 views);
@@ -304,7 +304,7 @@ extern "C" int citrus_sweep_persistent_config(float* store, const float* mu_cell
   CITRUS_REQUIRE(timeout_ns > 0, "citrus_sweep_persistent: timeout_ns must be positive");
   const int G = (int)num_groups, P = (int)num_planes, skip = skip_block < 0 ? -1 : (int)skip_block;
   const uint64_t t = (uint64_t)timeout_ns;
-  const int u = lanes_per_thread <= 0 ? kDefaultUnroll : lanes_per_thread;
+  const int u = thread_form <= 0 ? kDefaultUnroll : thread_form;
   unsigned* sy = reinterpret_cast<unsigned*>(sync);
   cudaStream_t s = as_stream(stream);
   switch (G) {

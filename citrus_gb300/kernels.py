@@ -74,7 +74,7 @@ class FlatPlaneIndex:
 def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tensor, *, method: str = "persistent",
                  sync: Optional[Tensor] = None, max_blocks: int = 0,
                  timeout_ns: int = DEFAULT_BARRIER_TIMEOUT_NS, skip_block: int = -1,
-                 lanes_per_thread: int = 0) -> Optional[Tensor]:
+                 thread_form: int = 0) -> Optional[Tensor]:
     """Sweep one direction chunk in place (reference ``sweep_kernels.py:265-290``).
 
     Args:
@@ -88,7 +88,7 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
         max_blocks: cap on the persistent grid (0: as many blocks as fit).
         timeout_ns: bound of every barrier wait of the persistent launch.
         skip_block: test hook forcing a barrier timeout (-1 in normal use).
-        lanes_per_thread: the form of the persistent launch's threads, each of which solves its lane (entry,
+        thread_form: the form of the persistent launch's threads, each of which solves its lane (entry,
             direction, group) in every view: 2 or 4 views loaded before they are solved, or one view at a time with
             registers capped for 5 (1), 6 (3) or 4 (5) blocks per SM (0: 1).
 
@@ -125,7 +125,7 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
         sync = torch.empty(4, dtype=torch.int32, device=store.device)
     _lib.call("citrus_sweep_persistent_config", store.data_ptr(), mu_cells.data_ptr(), c.data_ptr(),
               index.octant.data_ptr(), index.cell.data_ptr(), index.upstream.data_ptr(), index.offsets_device.data_ptr(),
-              index.num_planes, N, G, Dc, views, sync.data_ptr(), int(max_blocks), int(lanes_per_thread),
+              index.num_planes, N, G, Dc, views, sync.data_ptr(), int(max_blocks), int(thread_form),
               int(timeout_ns), int(skip_block), stream)
     return sync
 

@@ -66,12 +66,12 @@ int citrus_sweep_persistent(float* store, const float* mu_cells, const float* c,
 
 /* citrus_sweep_persistent with the form of its threads chosen by the caller (the autotuner). Every thread solves its
  * lane (entry, direction, group) in all views of the store, with the view-independent part of the cell solve
- * computed once: lanes_per_thread 2 or 4 views whose loads a thread issues before their solves, or one view at a
+ * computed once: thread_form 2 or 4 views whose loads a thread issues before their solves, or one view at a
  * time with the registers capped for 5 (1), 6 (3) or 4 (5) blocks of 256 threads per SM (0: 1). */
 int citrus_sweep_persistent_config(float* store, const float* mu_cells, const float* c, const int32_t* octant,
                                    const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_dev,
                                    int64_t num_planes, int64_t num_cells, int64_t num_groups, int64_t dc,
-                                   int64_t views, uint32_t* sync, int64_t max_blocks, int32_t lanes_per_thread,
+                                   int64_t views, uint32_t* sync, int64_t max_blocks, int32_t thread_form,
                                    int64_t timeout_ns, int64_t skip_block, void* stream);
 
 /* The persistent sweep without any allocation: no counterpart in the reference, which always runs the sweep through

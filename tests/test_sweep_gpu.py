@@ -75,10 +75,10 @@ def test_batched_views_sweep_matches_single_views(cuda_device):
     single = stores.clone()
     for v in range(V):
         kernels.sweep_planes(ctx.flat_index, single[v], mu, c, method="planes")
-    for lanes in (1, 2, 3, 4, 5):   # every lanes-per-thread form the autotuner chooses between
+    for form in (1, 2, 3, 4, 5):   # every thread form the autotuner chooses between
         batched = stores.clone()
-        sync = kernels.sweep_planes(ctx.flat_index, batched, mu, c, method="persistent", lanes_per_thread=lanes)
-        assert torch.equal(single, batched), lanes
+        sync = kernels.sweep_planes(ctx.flat_index, batched, mu, c, method="persistent", thread_form=form)
+        assert torch.equal(single, batched), form
         assert int(sync[2]) == 0
 
 
