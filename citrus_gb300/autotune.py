@@ -172,7 +172,9 @@ def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> 
 
     N, D8, Q = ctx.num_cells, ctx.directions_per_octant, 4 * num_groups
     device = ctx.device
-    key = Autotuner.key("sweep", device, N=N, D8=D8, G=num_groups, shape="x".join(map(str, ctx.shape)))
+    # "form" names the thread forms' meaning: entries timed with the one-lane-per-(view, entry) threads are not reused
+    key = Autotuner.key("sweep", device, N=N, D8=D8, G=num_groups, shape="x".join(map(str, ctx.shape)),
+                        form="views-per-thread")
     entry = tuner().table.get(key)
     if entry is None and not torch.cuda.is_current_stream_capturing():
         free, _ = torch.cuda.mem_get_info(device)
