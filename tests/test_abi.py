@@ -61,3 +61,16 @@ def test_bad_arguments_are_rejected_before_any_launch(library):
     assert b"null" in lib.citrus_last_error_string()
     status = lib.citrus_sweep_planes(None, None, None, None, None, None, None, 1, 1, 1, 1, 1, None)
     assert status == 1
+
+
+def test_fused_source_entry_points_check_their_arguments(library):
+    """The first-collision means and the one-pass source expansion reject null pointers, and the expansion columns
+    that do not come in quadruples, with CITRUS_EINVAL before any launch."""
+    lib = _lib.library()
+    status = lib.citrus_source_expansion_first(None, 1, None, 4, None, 4, None, 1, 1, 1, 4, 1, 0, 0, 0, None)
+    assert status == 1 and b"null" in lib.citrus_last_error_string()
+    fake = 256  # never dereferenced: the sizes are refused first
+    status = lib.citrus_source_expansion_first(fake, 1, fake, 6, fake, 6, fake, 2, 1, 1, 6, 1, 0, 0, 0, None)
+    assert status == 1 and b"quadruples" in lib.citrus_last_error_string()
+    status = lib.citrus_first_collision_means(8, None, None, None, None, 1, None, None, None, None, None, 8, None)
+    assert status == 1 and b"null" in lib.citrus_last_error_string()
