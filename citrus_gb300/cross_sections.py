@@ -75,23 +75,52 @@ class MultigroupLibrary:
             self._device_cache[key] = t
         return t
 
+    _FIELDS = ("group_edges", "group_energy", "spectrum_fraction", "mu_t", "mu_pe", "mu_s_l", "eta_grid", "mu_s_eta",
+               "fine_energy", "fine_mu_t", "fine_weight", "fine_group")
+
     def save(self, path: str) -> None:
-        np.savez(path, **{k: getattr(self, k) for k in ("group_edges", "group_energy", "spectrum_fraction", "mu_t",
-                                                         "mu_pe", "mu_s_l", "eta_grid", "mu_s_eta", "fine_energy",
-                                                         "fine_mu_t", "fine_weight", "fine_group", "nominal_density")},
-                 materials=np.array(self.materials))
+        """Write the library in the reference's on-disk format (``cross_sections.py:624-630``): ``torch.save`` of a
+        dict of every field of its dataclass, float64 tensors (``fine_group`` int64), ``materials`` a tuple of names
+        and ``eta_map`` None (a uniform table), so the reference's ``MultigroupLibrary.load`` reads the file."""
+        fields = {k: torch.as_tensor(np.asarray(getattr(self, k)),
+                                     dtype=torch.int64 if k == "fine_group" else torch.float64) for k in self._FIELDS}
+        fields["materials"] = tuple(str(m) for m in self.materials)
+        fields["nominal_density"] = torch.as_tensor(np.asarray(self.nominal_density), dtype=torch.float64)
+        fields["eta_map"] = None
+        torch.save(fields, path)
 
     @staticmethod
     def load(path: str) -> "MultigroupLibrary":
-        with np.load(path) as d:
-            fields = {k: d[k] for k in d.files if k != "materials"}
-            return MultigroupLibrary(materials=tuple(str(m) for m in d["materials"]), **fields)
+        """Read a library written by ``save`` or by the reference's ``MultigroupLibrary.save`` (``:632-650``); a
+        file without ``eta_map`` is a uniform table. Raises KeyError for a missing field (as the reference does) and
+        ValueError for an adaptive table (``eta_map`` set), whose node placement this package does not evaluate."""
+        fields = torch.load(path, map_location="cpu", weights_only=True)
+        missing = [k for k in (*MultigroupLibrary._FIELDS, "materials", "nominal_density") if k not in fields]
+        if missing:
+            raise KeyError(f"library file {path!r} lacks fields {missing}")
+        if fields.get("eta_map") is not None:
+            raise ValueError(f"library file {path!r} holds an adaptive eta table (eta_map); only uniform tables "
+                             "are evaluated here")
+        arrays = {k: fields[k].detach().cpu().numpy() for k in MultigroupLibrary._FIELDS}
+        return MultigroupLibrary(materials=tuple(fields["materials"]),
+                                 nominal_density=fields["nominal_density"].detach().cpu().numpy(), **arrays)
+
+
+# the reference's seven default materials and their nominal densities (``cross_sections.py:211-214``), and the
+# (scale, bone fraction) of each row of its seven-material synthetic library (``cross_sections.py:1112-1117``)
+REFERENCE_MATERIALS = ("air", "lung_icrp", "adipose_icrp", "water", "muscle_icru44", "soft_tissue_icru44",
+                       "bone_cortical_icrp")
+REFERENCE_NOMINAL_DENSITIES = (0.0012, 0.26, 0.95, 1.0, 1.05, 1.06, 1.85)
+_SYNTHETIC_BLENDS = {"air": (0.90, 0.0), "lung_icrp": (0.95, 0.02), "adipose_icrp": (0.97, 0.0), "water": (1.0, 0.0),
+                     "muscle_icru44": (1.0, 0.02), "soft_tissue_icru44": (1.0, 0.04), "bone_cortical_icrp": (1.0, 1.0)}
 
 
 def synthetic_library(num_groups: int = 4, legendre_order: int = 5, num_eta: int = 401,
-                      num_fine_per_group: int = 4, fine_spread: float = 0.0) -> MultigroupLibrary:
-    """The reference's two-material test library: kernel ``a (1 + b eta) / 4 pi``, linear in eta, so table and moments
-    agree exactly (reference ``cross_sections.py:1043-1109``)."""
+                      num_fine_per_group: int = 4, fine_spread: float = 0.0,
+                      num_materials: int = 2) -> MultigroupLibrary:
+    """The reference's test library: kernel ``a (1 + b eta) / 4 pi``, linear in eta, so table and moments agree
+    exactly (reference ``cross_sections.py:1043-1131``). Two materials are (water, bone); seven are the reference's
+    default materials, each row a scaled blend of the two; any other M > 2 blends named "m0", "m1", ..."""
     G, L = num_groups, legendre_order
     edges = np.linspace(125.0, 10.0, G + 1)
     energy = 0.5 * (edges[:-1] + edges[1:])
@@ -117,8 +146,27 @@ def synthetic_library(num_groups: int = 4, legendre_order: int = 5, num_eta: int
     fine_group = np.repeat(np.arange(G), n)
     fine_weight = fraction[fine_group] / n
     fine_mu_t = mu_t[:, fine_group] * (1.0 + float(fine_spread) * np.tile(x, G))[None, :]
-    return MultigroupLibrary(edges, energy, fraction, mu_t, mu_pe, mu_s_l, eta, mu_s_eta, fine_energy, fine_mu_t,
-                             fine_weight, fine_group)
+    M = int(num_materials)
+    if M == 2:
+        return MultigroupLibrary(edges, energy, fraction, mu_t, mu_pe, mu_s_l, eta, mu_s_eta, fine_energy, fine_mu_t,
+                                 fine_weight, fine_group)
+    if M < 2:
+        raise ValueError("num_materials must be >= 2")
+    if M == len(REFERENCE_MATERIALS):
+        rows = [_SYNTHETIC_BLENDS[n] for n in REFERENCE_MATERIALS]
+        names, nominal = REFERENCE_MATERIALS, np.array(REFERENCE_NOMINAL_DENSITIES)
+    else:
+        rows = [(1.0, 0.0), (1.0, 1.0)] + [(1.0 + 0.1 * m, (m - 1) / (M - 1)) for m in range(2, M)]
+        names, nominal = tuple(f"m{m}" for m in range(M)), np.arange(1.0, M + 1.0)
+
+    def blend(a):
+        # a pure row (scale 1, fraction 0 or 1) is that material's row itself, bit for bit
+        return np.stack([a[int(t)].copy() if s == 1.0 and t in (0.0, 1.0) else s * ((1.0 - t) * a[0] + t * a[1])
+                         for s, t in rows])
+
+    return MultigroupLibrary(edges, energy, fraction, blend(mu_t), blend(mu_pe), blend(mu_s_l), eta, blend(mu_s_eta),
+                             fine_energy, blend(fine_mu_t), fine_weight, fine_group, materials=names,
+                             nominal_density=nominal)
 
 
 # ---- spectral library ---------------------------------------------------------------------------------------------

@@ -3,7 +3,9 @@
 //
 // Encoding: for every (group, moment) the largest |cell mean| over the cells is mapped to 2^14, scale = max / 2^14
 // (1 where the maximum is 0), and each cell mean is stored as float16(mean / scale) with IEEE division and
-// round-to-nearest-even conversion, as the reference's float32 tensor arithmetic does. Decoding multiplies back in
+// round-to-nearest-even conversion, as the reference's float32 tensor arithmetic does. The maximum carries a NaN as
+// the reference's abs().amax() does; "maximum > 0" is then false and that (group, moment) takes the scale 1, its
+// other cells stored unscaled, exactly as the reference stores them. Decoding multiplies back in
 // float32 and writes zero slopes. One block per (group, moment) reduces the maximum in a fixed order, so the codec is
 // bit-exact and deterministic.
 #include <cuda_fp16.h>
@@ -16,6 +18,9 @@ namespace {
 constexpr int kStateThreads = 256;
 constexpr float kFloat16Target = 16384.0f;  // 2^14: |q| <= 16384 < 65504
 
+// max that returns a NaN operand (fmaxf drops it)
+__device__ __forceinline__ float max_keep_nan(float a, float b) { return isnan(a) ? a : (isnan(b) ? b : fmaxf(a, b)); }
+
 // element (g, n, cell) of the cell-mean component at g * s_g + n * s_n + cell * s_x
 __global__ void __launch_bounds__(kStateThreads) state_encode_kernel(const float* __restrict__ acc, int N,
                                                                      int64_t cells, int64_t s_g, int64_t s_n,
@@ -26,11 +31,11 @@ __global__ void __launch_bounds__(kStateThreads) state_encode_kernel(const float
   const float* src = acc + g * s_g + n * s_n;
   __shared__ float red[kStateThreads];
   float m = 0.f;
-  for (int64_t x = threadIdx.x; x < cells; x += kStateThreads) m = fmaxf(m, fabsf(__ldg(src + x * s_x)));
+  for (int64_t x = threadIdx.x; x < cells; x += kStateThreads) m = max_keep_nan(m, fabsf(__ldg(src + x * s_x)));
   red[threadIdx.x] = m;
   __syncthreads();
   for (int w = kStateThreads / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+    if (threadIdx.x < w) red[threadIdx.x] = max_keep_nan(red[threadIdx.x], red[threadIdx.x + w]);
     __syncthreads();
   }
   const float maximum = red[0];

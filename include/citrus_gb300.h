@@ -79,9 +79,11 @@ int citrus_sweep_persistent_config(float* store, const float* mu_cells, const fl
  * per device, at most 8191 planes, i.e. R + C + S - 2 <= 8191; more planes return CITRUS_EINVAL). The call clears
  * the barrier words and copies plane_offsets_host [num_planes + 1] (int32, host memory; a pinned buffer must stay
  * unchanged until the stream reaches the copy) into the array on the stream, then launches. The first call on each
- * device looks the array's address up (that device must be current); make it before any stream capture. Calls on
- * one device share the array, so calls that overlap in time (two streams, two host threads) race and must not be
- * made. timeout_word, when not NULL, receives the barrier error word on the stream (non-zero: a wait ran out and
+ * device looks the array's address up (that device must be current); make it before any stream capture. The address
+ * is kept for the life of the process: after cudaDeviceReset (or any teardown of the device's primary context) the
+ * entry point must not be called again in that process. A pageable plane_offsets_host has been read by the time the
+ * call returns. Calls on one device share the array, so calls that overlap in time (two streams, two host threads)
+ * race and must not be made. timeout_word, when not NULL, receives the barrier error word on the stream (non-zero: a wait ran out and
  * the store is invalid); a pageable host word makes the call wait for the sweep. */
 int citrus_sweep_persistent_static(float* store, const float* mu_cells, const float* c, const int32_t* octant,
                                    const int32_t* cell, const int32_t* upstream, const int32_t* plane_offsets_host,

@@ -36,6 +36,39 @@ def rel_err(a, b) -> float:
     return float(np.abs(a - b).max() / (scale if scale > 0 else 1.0))
 
 
+def elementwise_rel_err(a, b, floor: float = 1e-3) -> float:
+    """max over elements of |a - b| / |b|, over the elements with |b| above ``floor`` times max |b|."""
+    a = np.asarray(a.detach().cpu().double() if hasattr(a, "detach") else a, dtype=np.float64)
+    b = np.asarray(b.detach().cpu().double() if hasattr(b, "detach") else b, dtype=np.float64)
+    mask = np.abs(b) > floor * np.abs(b).max()
+    return float((np.abs(a - b)[mask] / np.abs(b)[mask]).max())
+
+
+def block_means(image, n: int = 8) -> np.ndarray:
+    """Means of an image over n x n blocks, rows and channels split as numpy.array_split does (the layout of the
+    reference's regression cases, its ``tests/test_quadrature_grid.py:54-59``)."""
+    image = np.asarray(image.detach().cpu().double() if hasattr(image, "detach") else image, dtype=np.float64)
+    r = np.array_split(np.arange(image.shape[0]), n)
+    c = np.array_split(np.arange(image.shape[1]), n)
+    return np.array([[image[np.ix_(ri, ci)].mean() for ci in c] for ri in r])
+
+
+def check_regression_case(scatter, primary, iterations, final_change, g, name: str, tolerance: float) -> None:
+    """A solve against one regression case of the reference (its ``_check_reference``,
+    ``tests/test_quadrature_grid.py:62-71``): 8 x 8 block means and sums of both signals, source-iteration count and
+    final change."""
+    assert list(np.shape(scatter)) == list(g[f"{name}_image_shape"])
+    assert rel_err(block_means(scatter), g[f"{name}_scatter_signal_blocks"]) < tolerance
+    assert rel_err(block_means(primary), g[f"{name}_primary_signal_blocks"]) < tolerance
+    s = float(np.asarray(scatter.detach().cpu().double() if hasattr(scatter, "detach") else scatter).sum())
+    p = float(np.asarray(primary.detach().cpu().double() if hasattr(primary, "detach") else primary).sum())
+    assert abs(s / float(g[f"{name}_scatter_signal_sum"]) - 1) < tolerance
+    assert abs(p / float(g[f"{name}_primary_signal_sum"]) - 1) < tolerance
+    assert int(iterations) == int(g[f"{name}_si_iterations"])
+    expected = float(g[f"{name}_si_final_change"])
+    assert abs(final_change - expected) <= max(1e-3, tolerance) * abs(expected)
+
+
 @pytest.fixture(scope="session")
 def cuda_device():
     import torch

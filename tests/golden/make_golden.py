@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the test suite by running the reference itself (cabouman/citrus v0.28.0).
 
-Run in a checkout where the reference is available (it is read from /root/reference by default, or from the path in
-CITRUS_REFERENCE). The reference imports xraylib at module level for element tables only; ``_shims/xraylib.py``
+Run in a checkout beside the reference, with CITRUS_REFERENCE set to its root (the directory that holds ``citrus/``
+and ``tests/data/``). The reference imports xraylib at module level for element tables only; ``_shims/xraylib.py``
 stands in for it (the synthetic library used here never reads those tables). Every fixture is small, float64, and
 produced by the reference's own float64 CPU path; the script is deterministic (seeded).
 
@@ -18,7 +18,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = os.environ.get("CITRUS_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("CITRUS_REFERENCE")
+if not REFERENCE:
+    sys.exit("set CITRUS_REFERENCE to the root of a cabouman/citrus v0.28.0 checkout")
 sys.path[:0] = [str(HERE / "_shims"), REFERENCE]
 
 import torch  # noqa: E402
@@ -313,6 +315,165 @@ def density_model():
          mass=mass_attenuation_at(ref, e), order=np.array(material_order(ref)),
          lib_fine_energy=lib.fine_energy, lib_fine_mu_t=lib.fine_mu_t, lib_fine_weight=lib.fine_weight,
          lib_nominal=lib.nominal_density)
+
+
+def _block_means(a: np.ndarray, b: int) -> np.ndarray:
+    """Means over b x b x b blocks of the last three axes."""
+    *lead, R, C, S = a.shape
+    return a.reshape(*lead, R // b, b, C // b, b, S // b, b).mean(axis=(-5, -3, -1))
+
+
+@case
+def config1_view():
+    """The reference's CITRUS scatter step of the single-view workload (32^3 cells of 0.5 cm, one 60 keV group, P3,
+    4 x 12 sweep directions, cone 16 x 32, flat 64 x 64 panel of 0.4 cm pixels at 150 cm, ideal counting detector):
+    ``citrus_view_step(primary=True, sweeps=1)`` from a cold start and a second step, float64 CPU. Stored: the
+    inputs' densities, both steps' scatter images and changes, the primary, the scalar-flux LD moments of the
+    collided accumulator element-wise (float32) and the cell means of all 16 moments over 2^3-cell blocks."""
+    sys.path.insert(0, str(HERE.parent.parent))
+    from citrus_gb300.workloads import single_view
+    from citrus.citrus import CitrusState, citrus_view_step
+    from citrus.scatter_solver.config import SolverConfig
+    from citrus.scatter_solver.detector import ideal_counting_response, no_grid
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.scatter_solver import ScatterSolver
+
+    w = single_view()
+    library = reference_library(w.library)
+    g = w.geometry
+    geo = ConeGeometry(g.source_iso_dist, g.source_detector_dist, g.num_det_rows, g.num_det_channels,
+                       g.delta_det_row, g.delta_det_channel)
+    grid = Grid(w.grid.shape, w.grid.delta_voxel)
+    config = SolverConfig(num_groups=1, legendre_order=w.legendre_order, num_polar=w.num_polar,
+                          num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
+                          quadrature_point_spacing_cm=0.5, cone_num_polar=w.cone_num_polar,
+                          cone_num_azimuthal=w.cone_num_azimuthal, direction_chunk=6)
+    solver = ScatterSolver(library, config, geo, SiddonProjectors(backend="torch"), ideal_counting_response(),
+                           no_grid(), device="cpu", dtype=F64)
+    rho = torch.as_tensor(w.rho, dtype=F64)
+    fields = solver.material_fields(rho, grid)
+    state = CitrusState()
+    arrays = dict(rho=rho)
+    for step in (1, 2):
+        scatter, primary, state = citrus_view_step(solver, state, fields, 0.0, primary=True)
+        phi = state.collided_moments.numpy()                                   # [G, N_sh, 4, R, C, S]
+        arrays[f"step{step}_scatter"] = scatter
+        arrays[f"step{step}_change"] = np.asarray(state.history[-1])
+        arrays[f"step{step}_scalar"] = phi[:, 0].astype(np.float32)
+        arrays[f"step{step}_means_b2"] = _block_means(phi[:, :, 0], 2).astype(np.float32)
+        arrays[f"step{step}_norms"] = np.sqrt((phi ** 2).sum(axis=(0, 2, 3, 4, 5)))
+    arrays["primary"] = primary
+    save("config1_view", **arrays)
+
+
+@case
+def pre_quadrature_synthetic():
+    """The reference's regression anchor of ``solve_view`` (its ``tests/data/pre_quadrature_reference.json``, cases
+    ``synthetic_cpu`` and ``synthetic_cuda``, checked by its ``tests/test_quadrature_grid.py``) with the inputs that
+    produce it: the seven-material synthetic library (G = 4, L = 5), the WLAB phantom on the 2 cm grid (10 x 16 x 20),
+    the CsI scintillator response, 4 cm cells (q = 2), the fine uncollided trace, view 0.4 rad. Also stored: the full
+    float64 images of the same solve run now by the reference."""
+    import json
+    from citrus.scatter_solver.config import SolverConfig
+    from citrus.scatter_solver.cross_sections import synthetic_library
+    from citrus.scatter_solver.detector import csi_response, no_grid
+    from citrus.scatter_solver.geometry import Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.scatter_solver import ScatterSolver
+    from citrus.utilities import wlab_geometry, wlab_phantom
+
+    grid = Grid((10, 16, 20), 2.0)
+    config = SolverConfig(num_groups=4, legendre_order=3, num_polar=4, num_azimuthal=8, cone_num_polar=8,
+                          cone_num_azimuthal=16, transport_cell_cm=4.0, quadrature_point_spacing_cm=2.0,
+                          source_iteration_tolerance=1e-4, max_source_iterations=40, direction_chunk=8,
+                          uncollided_trace_grid="fine")
+    library = synthetic_library(config.num_groups, 5, num_materials=7)
+    det = csi_response()
+    geo = wlab_geometry()
+    solver = ScatterSolver(library, config, geo, SiddonProjectors(backend="torch"), det, no_grid(), device="cpu",
+                           dtype=F64)
+    rho = wlab_phantom(grid, dtype=F64)
+    r = solver.solve_view(rho, grid, 0.4)
+    cases = json.loads(Path(REFERENCE, "tests", "data", "pre_quadrature_reference.json").read_text())["cases"]
+    arrays = dict(rho=rho, det_e=det.energy_kev, det_theta=det.theta_rad, det_table=det.response,
+                  geometry=np.array([geo.source_iso_dist, geo.source_detector_dist, geo.num_det_rows,
+                                     geo.num_det_channels, geo.delta_det_row, geo.delta_det_channel]),
+                  scatter_signal=r.scatter_signal, primary_signal=r.primary["signal"],
+                  si_iterations=np.asarray(r.source_iteration_result.num_iterations),
+                  si_history=np.asarray(r.source_iteration_result.history))
+    for k in ("group_edges", "group_energy", "spectrum_fraction", "mu_t", "mu_pe", "mu_s_l", "eta_grid", "mu_s_eta",
+              "fine_energy", "fine_mu_t", "fine_weight", "fine_group", "nominal_density"):
+        arrays[f"lib_{k}"] = getattr(library, k)
+    arrays["lib_materials"] = np.array(library.materials)
+    for name in ("synthetic_cpu", "synthetic_cuda"):
+        c = cases[name]
+        arrays[f"{name}_image_shape"] = np.array(c["image_shape"])
+        for k in ("scatter_signal_blocks", "primary_signal_blocks", "scatter_signal_sum", "primary_signal_sum",
+                  "si_iterations", "si_final_change"):
+            arrays[f"{name}_{k}"] = np.asarray(c[k], dtype=np.float64)
+    save("pre_quadrature_synthetic", **arrays)
+
+
+@case
+def citrus_step_sweeps():
+    """Two CITRUS steps of one view with ``sweeps=2`` (``accumulator_update_operator``: the second sweep applies K to
+    the last change of the accumulator) from a cold start, on the problem of ``citrus_step_small`` (flat panel),
+    float64 CPU."""
+    from citrus.citrus import CitrusState, citrus_view_step
+    from citrus.scatter_solver.config import SolverConfig
+    from citrus.scatter_solver.detector import DetectorResponse, no_grid
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.scatter_solver import ScatterSolver
+
+    g = torch.Generator().manual_seed(31)
+    library = reference_library(small_spectral_library())
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.zeros(2, *grid.shape, dtype=F64)
+    rho[0] = 0.9 + 0.2 * torch.rand(*grid.shape, generator=g, dtype=F64)
+    rho[1, 2:5, 3:6, 1:4] = 1.85
+    rho[0, 2:5, 3:6, 1:4] = 0.0
+    e, th, table = scintillator_table()
+    det = DetectorResponse(torch.as_tensor(e), torch.as_tensor(th), torch.as_tensor(table))
+    geo = ConeGeometry(40.0, 60.0, 12, 16, 1.2, 1.2)
+    solver = ScatterSolver(library, SolverConfig(**STEP_CONFIG), geo, SiddonProjectors(backend="torch"), det,
+                           no_grid(), device="cpu", dtype=F64)
+    fields = solver.material_fields(rho, grid)
+    state = CitrusState()
+    arrays = dict(rho=rho)
+    for step in (1, 2):
+        scatter, _, state = citrus_view_step(solver, state, fields, 0.6, primary=False, sweeps=2)
+        arrays[f"step{step}_scatter"] = scatter
+        arrays[f"step{step}_collided"] = state.collided_moments
+        arrays[f"step{step}_change"] = np.asarray(state.history[-1])
+    save("citrus_step_sweeps", **arrays)
+
+
+@case
+def state_store_codec():
+    """The reference's per-view accumulator store (``citrus.StateStore``, host location, float32 arithmetic) on a
+    seeded accumulator [G=3, N=16, 4, 4, 5, 6] with moments of decreasing size, one (group, moment) plane holding a
+    NaN cell and one all zero: the decoded accumulator and the stored float16 values."""
+    from citrus.citrus import StateStore
+    g = torch.Generator().manual_seed(8)
+    shape = (3, 16, 4, 4, 5, 6)
+    phi = (1e-6 * torch.randn(shape, generator=g, dtype=torch.float64)
+           * torch.logspace(0, -3, 16, dtype=torch.float64)[None, :, None, None, None, None]).float()
+    phi[1, 2, 0, 1, 2, 3] = float("nan")
+    phi[2, 5] = 0.0
+    store = StateStore(1, shape, "cpu", location="cpu")
+    store.put(0, phi)
+    save("state_store_codec", phi=phi, decoded=store.get(0), stored=store._data[0].float(), scale=store._scale[0])
+
+
+@case
+def library_file():
+    """A library written by the reference's own ``MultigroupLibrary.save`` (``torch.save`` of a dict of every field),
+    the two-material synthetic library with G = 3, L = 2, 21 eta nodes: the on-disk format ``load`` reads."""
+    from citrus.scatter_solver.cross_sections import synthetic_library
+    synthetic_library(3, 2, num_eta=21, num_fine_per_group=2).save(str(HERE / "reference_library.pt"))
+    print(f"reference_library.pt: {(HERE / 'reference_library.pt').stat().st_size / 1024:.1f} KiB")
 
 
 if __name__ == "__main__":

@@ -74,3 +74,20 @@ def test_fused_source_entry_points_check_their_arguments(library):
     assert status == 1 and b"quadruples" in lib.citrus_last_error_string()
     status = lib.citrus_first_collision_means(8, None, None, None, None, 1, None, None, None, None, None, 8, None)
     assert status == 1 and b"null" in lib.citrus_last_error_string()
+
+
+def test_allocation_free_sweep_checks_its_arguments(library):
+    """citrus_sweep_persistent_static refuses null plane offsets, more planes than its static scratch holds, and a
+    non-positive wait limit with CITRUS_EINVAL before any CUDA call (the pointers below are never dereferenced)."""
+    import numpy as np
+    lib = _lib.library()
+    fake = 256
+    offsets = np.zeros(9000, dtype=np.int32)
+    args = (fake, fake, fake, fake, fake, fake)
+    status = lib.citrus_sweep_persistent_static(*args, None, 4, 8, 1, 1, 1, None, 10 ** 9, None)
+    assert status == 1 and b"null plane offsets" in lib.citrus_last_error_string()
+    status = lib.citrus_sweep_persistent_static(*args, offsets.ctypes.data, 8192, 8, 1, 1, 1, None, 10 ** 9, None)
+    assert status == 1 and b"8191" in lib.citrus_last_error_string()
+    for timeout in (0, -5):
+        status = lib.citrus_sweep_persistent_static(*args, offsets.ctypes.data, 4, 8, 1, 1, 1, None, timeout, None)
+        assert status == 1 and b"timeout_ns" in lib.citrus_last_error_string()

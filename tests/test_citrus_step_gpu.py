@@ -95,3 +95,22 @@ def test_primary_signals_of_all_views(cuda_device, name):
     assert torch.allclose(planar[1], solver.primary(fields, 1.3)["planar_fluence"].sum(0))
     with pytest.raises(ValueError):
         primary_signals(solver, fields, angles, quantity="counts")
+
+
+def test_citrus_view_steps_with_two_sweeps_match_reference(cuda_device):
+    """``sweeps=2`` (the second sweep applies K to the accumulator's last change, reference ``citrus.py:192-247``):
+    two steps from a cold start against the reference's float64 run."""
+    ref = golden("citrus_step_sweeps")
+    _, solver = _solver("flat", cuda_device)
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.as_tensor(ref["rho"], dtype=torch.float32, device=cuda_device)
+    fields = solver.material_fields(rho, grid)
+    state = CitrusState()
+    for step in (1, 2):
+        scatter, primary, state = citrus_view_step(solver, state, fields, 0.6, primary=False, sweeps=2)
+        assert primary is None
+        assert rel_err(state.collided_moments, ref[f"step{step}_collided"]) < 1e-4
+        assert rel_err(scatter, ref[f"step{step}_scatter"]) < 1e-4
+        assert abs(state.history[-1] - float(ref[f"step{step}_change"])) < 1e-4
+    with pytest.raises(ValueError):
+        citrus_view_step(solver, state, fields, 0.6, sweeps=0)

@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden, rel_err
+from conftest import check_regression_case, golden, rel_err
 from citrus_gb300.geometry import Grid
 from citrus_gb300.quadrature import Quadrature, hemisphere_quadrature, product_quadrature, real_spherical_harmonics
 from citrus_gb300.transport_sweep import build_sweep_plan
@@ -220,3 +220,77 @@ def test_oracle_image_and_primary_match_reference(name):
     prim = oimage.primary(library, rho, grid_q, geo, angle, det)
     assert rel_err(prim["signal"], g[f"{name}_primary_signal"]) < 1e-12
     assert rel_err(prim["fluence"], g[f"{name}_primary_fluence"]) < 1e-12
+
+
+# ---- the reference's own regression anchor and the single-view workload ---------------------------------------------
+
+def test_pre_quadrature_fixture_reproduces_the_reference_golden_case():
+    """The fixture's solve (the reference's float64 CPU path run on the stored inputs) reproduces the reference's
+    committed regression case ``synthetic_cpu`` at its own tolerance, 1e-10: the inputs are pinned."""
+    g = golden("pre_quadrature_synthetic")
+    check_regression_case(g["scatter_signal"], g["primary_signal"], g["si_iterations"], float(g["si_history"][-1]),
+                          g, "synthetic_cpu", 1e-10)
+
+
+def test_seven_material_synthetic_library_matches_reference():
+    from citrus_gb300.cross_sections import synthetic_library
+    g = golden("pre_quadrature_synthetic")
+    lib = synthetic_library(4, 5, num_materials=7)
+    for k in ("group_edges", "group_energy", "spectrum_fraction", "mu_t", "mu_pe", "mu_s_l", "eta_grid", "mu_s_eta",
+              "fine_energy", "fine_mu_t", "fine_weight", "fine_group", "nominal_density"):
+        np.testing.assert_allclose(getattr(lib, k), g[f"lib_{k}"], rtol=0, atol=1e-15)
+    assert lib.materials == tuple(str(m) for m in g["lib_materials"])
+
+
+def test_single_view_workload_densities_match_the_fixture():
+    from citrus_gb300.workloads import single_view
+    np.testing.assert_array_equal(single_view().rho, golden("config1_view")["rho"])
+
+
+# ---- the library's on-disk format ------------------------------------------------------------------------------------
+
+def test_library_file_written_by_the_reference_loads():
+    from citrus_gb300.cross_sections import MultigroupLibrary, synthetic_library
+    from conftest import GOLDEN
+    lib = MultigroupLibrary.load(str(GOLDEN / "reference_library.pt"))
+    ours = synthetic_library(3, 2, num_eta=21, num_fine_per_group=2)
+    for k in MultigroupLibrary._FIELDS + ("nominal_density",):  # torch and numpy linspace differ in the last bit
+        np.testing.assert_allclose(getattr(lib, k), getattr(ours, k), rtol=1e-15, atol=1e-16)
+    assert lib.materials == ("water", "bone_cortical_icrp")
+
+
+def test_library_file_written_here_has_the_reference_format(tmp_path):
+    """save() writes what the reference's MultigroupLibrary.load reads: the same keys, tensor dtypes and shapes as a
+    file written by the reference's own save, and the same values; load() reads it back unchanged."""
+    import torch
+    from citrus_gb300.cross_sections import MultigroupLibrary
+    from conftest import GOLDEN
+    reference = torch.load(str(GOLDEN / "reference_library.pt"), weights_only=True)
+    lib = MultigroupLibrary.load(str(GOLDEN / "reference_library.pt"))
+    lib.save(str(tmp_path / "lib.pt"))
+    ours = torch.load(str(tmp_path / "lib.pt"), weights_only=True)
+    assert set(ours) == set(reference)
+    for k, v in reference.items():
+        if isinstance(v, torch.Tensor):
+            assert ours[k].dtype == v.dtype and ours[k].shape == v.shape and torch.equal(ours[k], v), k
+        else:
+            assert ours[k] == v, k
+    again = MultigroupLibrary.load(str(tmp_path / "lib.pt"))
+    for k in MultigroupLibrary._FIELDS:
+        np.testing.assert_array_equal(getattr(again, k), getattr(lib, k))
+
+
+def test_library_file_errors(tmp_path):
+    import torch
+    from citrus_gb300.cross_sections import MultigroupLibrary
+    from conftest import GOLDEN
+    fields = torch.load(str(GOLDEN / "reference_library.pt"), weights_only=True)
+    del fields["mu_pe"]
+    torch.save(fields, str(tmp_path / "missing.pt"))
+    with pytest.raises(KeyError):
+        MultigroupLibrary.load(str(tmp_path / "missing.pt"))
+    fields = torch.load(str(GOLDEN / "reference_library.pt"), weights_only=True)
+    fields["eta_map"] = torch.linspace(1.0, 0.0, 9, dtype=torch.float64)
+    torch.save(fields, str(tmp_path / "adaptive.pt"))
+    with pytest.raises(ValueError):
+        MultigroupLibrary.load(str(tmp_path / "adaptive.pt"))

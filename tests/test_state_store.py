@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 import torch
 
+from conftest import golden
 from citrus_gb300.state_store import StateStore
 
 SHAPE = (3, 16, 4, 4, 5, 6)  # [G, (L+1)^2 with L = 3, 4, Rc, Cc, Sc]
@@ -62,3 +63,21 @@ def test_round_trip_is_the_reference_codec(cuda_device, location):
         store.put(0, phis[0][:, :9])
     store.close()
     assert store.get(1) is None
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("location", ["gpu", "cpu"])
+def test_codec_matches_the_reference_store(cuda_device, location):
+    """The reference's own StateStore output (fixture): a seeded accumulator with a NaN cell in one (group, moment)
+    plane and one all-zero plane. Stored float16 values, scales and the decoded accumulator bit for bit (NaN where
+    the reference has NaN; the NaN plane takes the scale 1, as the reference's ``amax > 0`` test gives)."""
+    g = golden("state_store_codec")
+    shape = tuple(g["phi"].shape)
+    storage = torch.as_tensor(g["phi"]).permute(1, 3, 4, 5, 0, 2).contiguous().to(cuda_device)
+    phi = storage.permute(4, 0, 5, 1, 2, 3)                    # the sweep's cell-major storage, reference shape
+    store = StateStore(1, shape, cuda_device, location=location)
+    store.put(0, phi)
+    np.testing.assert_array_equal(store._scale[0].cpu().numpy(), g["scale"])
+    np.testing.assert_array_equal(store._data[0].float().cpu().numpy(), g["stored"])
+    np.testing.assert_array_equal(store.get(0).cpu().numpy(), g["decoded"])
+    assert float(g["scale"][1, 2].item()) == 1.0 and float(g["scale"][2, 5].item()) == 1.0
