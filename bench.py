@@ -279,16 +279,22 @@ def run_reference(args):
     if rank != 0:
         return
     if args.workload == "step":
-        cpu_baseline_step(cells=args.cells, image_directions=1, fc_directions=1, sweep_chunks=1, points=1024,
-                          slices=1)  # warm-up (imports, pages, OpenMP threads)
-        runs = [cpu_baseline_step(cells=args.cells, seed=i) for i in range(args.steps)]
+        for _ in range(max(1, args.warmup)):   # imports, pages, OpenMP threads
+            cpu_baseline_step(cells=args.cells, image_directions=1, fc_directions=1, sweep_chunks=1, points=1024,
+                              slices=1)
+        runs, wall = [], []
+        for i in range(args.steps):
+            t0 = time.perf_counter()
+            runs.append(cpu_baseline_step(cells=args.cells, seed=i))
+            wall.append(time.perf_counter() - t0)
         value = statistics.median(r["value"] for r in runs)
         base = dict(runs[0], value=value)
-        base["sample"] = f"median of {args.steps} samples; " + base["sample"]
+        base["sample"] = (f"median of {args.steps} steps, each a bounded sample of one view's stages timed and scaled "
+                          f"to the whole view (the step's own duration is ms_per_step): " + base["sample"])
         line = {"metric": STEP_METRIC, "value": value, "unit": "ms/view", "impl": "reference", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
-                "dtype": "f64", "data": "synthetic (seeded phantom and library)",
-                "config": {"workload": step_workload_name(args.cells, 60, args.batch, args.graph)}, "cpu_baseline": base,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(wall),
+                "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded phantom and library)",
+                "config": step_config(args, 60, args.batch), "cpu_baseline": base, "extrapolated": True,
                 "e2e": {"value": value, "unit": "ms/view", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -424,6 +430,23 @@ def make_step_solver(device, views: int = 0, cells: int = 64, precision: str = "
 STEP_METRIC = "scatter-step ms/view (all views of one outer iteration; cell*dir*group updates/s alongside)"
 
 
+def step_config(args, views: int, batch: int) -> dict:
+    """The ``config`` of the step's bench line, the same for both arms."""
+    return {"workload": step_workload_name(args.cells, views, batch, args.graph),
+            "l2": "inputs larger than L2 (4 GB sweep store per view)", "moment_precision": args.precision}
+
+
+def sweep_form_name(solver, w, rho_dev) -> str:
+    """The accumulator sweep's form the autotuner chose for this grid (plane wavefront or tiled schedule)."""
+    from citrus_gb300.batched import sweep_launch_config
+    fields = solver.material_fields(rho_dev, w.grid)
+    _, form = sweep_launch_config(solver, fields, 60, 0)
+    if form.tile > 0:
+        return (f"tiled: {form.tile}^3-cell tiles, {form.dirs_per_block} directions per task, thread form "
+                f"{form.thread_form}")
+    return f"plane wavefront, thread form {form.thread_form}"
+
+
 def step_workload_name(cells: int, views: int, batch: int = 1, graph: bool = False) -> str:
     how = ("citrus_view_step per view" if batch == 1 else
            "batched_view_steps, the accumulator sweeps of several views per persistent launch (views per launch "
@@ -483,9 +506,17 @@ def sweep_bytes(args) -> int:
     return 32 * views * 8 * Dc * N * G
 
 
+def tiled_sweep_bytes(args) -> int:
+    """citrus_sweep_tiled: the same 32 B per update as the plane wavefront."""
+    N, G, Dc, views = int(args[10]), int(args[11]), int(args[12]), int(args[13])
+    return 32 * views * 8 * Dc * N * G
+
+
+SWEEP_ENTRY_POINTS = ("citrus_sweep_tiled", "citrus_sweep_persistent_config", "citrus_sweep_persistent")
 STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_attenuated_emission": product_emission_bytes,
               "citrus_downstream_cumulative": downstream_bytes,
               "citrus_sweep_persistent": sweep_bytes, "citrus_sweep_persistent_config": sweep_bytes,
+              "citrus_sweep_tiled": tiled_sweep_bytes,
               "citrus_oblique_project": None, "citrus_box_blur": None, "citrus_small_k_gemm": None,
               "citrus_small_k_gemm_config": None, "citrus_small_k_gemm_bf16x3": None, "citrus_first_collision_moments": None,
               "citrus_first_collision_means": None, "citrus_source_expansion_first": None,
@@ -681,7 +712,7 @@ def learned_measurement(args, device) -> dict:
 
     def summary(rows):
         return {"ms_per_view": statistics.mean(r[0] for r in rows), "sweeps_mean": statistics.mean(r[1] for r in rows),
-                "spr_err_max": max(r[2] for r in rows), "accepted_in_two_sweeps": sum(bool(r[3]) for r in rows)}
+                "spr_err_max": max(r[2] for r in rows), "accepted": sum(bool(r[3]) for r in rows)}
 
     return {
         "workload": f"learned_proposal: {cells[0]}x{cells[1]}x{cells[2]} cells x {w.transport_cell_cm:.2f} cm, G=12 "
@@ -825,10 +856,9 @@ def run_step(args):
         "value": ms_per_view / max(1, world), "unit": "ms/view", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom and library)",
-        "config": {"workload": step_workload_name(args.cells, V, requested_batch, args.graph),
-                   "l2": "inputs larger than L2 (4 GB sweep store per view)",
-                   "moment_precision": args.precision, "views_per_sweep_launch": args.batch,
-                   "views_per_sweep_launch_autotuned": requested_batch <= 0},
+        "config": step_config(args, V, requested_batch),
+        "sweep_launch": {"views_per_launch": args.batch, "autotuned": requested_batch <= 0,
+                         "form": sweep_form_name(solver, w, rho_dev)},
         "updates_per_s": updates * V * args.steps * world / elapsed,
         "e2e": {"value": e2e * 1e3 / (args.steps * V) / max(1, world), "unit": "ms/view",
                 "h2d_bytes_per_step": rho_host.numel() * 4, "d2h_bytes_per_step": host_signals.numel() * 4},
@@ -844,13 +874,13 @@ def run_step(args):
                                     for n, t in sorted(per_entry.items(), key=lambda x: -sum(x[1]))},
         "clocks": sampler.summary(),
     }
-    sweep_name = "citrus_sweep_persistent_config" if calls.get("citrus_sweep_persistent_config") else \
-        "citrus_sweep_persistent"
-    sweep_recs = calls.get(sweep_name) or []
+    sweep_name = next((n for n in SWEEP_ENTRY_POINTS if calls.get(n)), None)
+    sweep_recs = calls.get(sweep_name) or [] if sweep_name else []
     if sweep_recs:
         sweep_s = sum(per_entry[sweep_name])
         sweep_gbs = sum(info for info, _, _ in sweep_recs) / sweep_s / 1e9
-        line["sweep_roofline"] = {"bound": "hbm", "achieved": sweep_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        line["sweep_roofline"] = {"entry_point": sweep_name, "bound": "hbm", "achieved": sweep_gbs,
+                                  "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                   "frac": sweep_gbs / peaks["hbm_gbs"], "launches": len(sweep_recs),
                                   "kernel_ms_mean": 1e3 * sweep_s / len(sweep_recs),
                                   "algorithmic_bytes_per_launch": statistics.mean(i for i, _, _ in sweep_recs)}

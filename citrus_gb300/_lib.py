@@ -28,6 +28,7 @@ SIGNATURES = {
     "citrus_sweep_persistent": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, I64, I64, P],
     "citrus_sweep_persistent_config": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, I32, I64, I64, P],
     "citrus_sweep_persistent_static": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, P, I64, P],
+    "citrus_sweep_tiled": [P, P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, P, I64, I64, I64, I64, P],
     "citrus_small_k_gemm": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P],
     "citrus_small_k_gemm_config": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, I32, I32, P],
     "citrus_source_expansion_first": [P, I64, P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I64, P],

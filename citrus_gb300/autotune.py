@@ -162,38 +162,49 @@ VIEW_CANDIDATES = (1, 2, 4, 8)
 # registers capped for 5 (form 1), 6 (form 3) or 4 (form 5) blocks of 256 threads per SM, or the loads of 2 (form 2)
 # or 4 (form 4) views issued before their solves
 UNROLL_CANDIDATES = (1, 3, 5, 2, 4)
+# the tiled schedule (one grid barrier per tile diagonal): tile edges, thread forms (1: one view at a time, 2: the
+# loads of two views first) and directions per task (1, a few, or the whole chunk, as the chunk allows)
+TILE_CANDIDATES = (4, 8)
+TILED_FORMS = (1, 2)
 
 
-def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2)) -> tuple:
-    """(views per persistent sweep launch, sweep thread form) for ``views`` views on this grid: the per-view time of
-    the sweep on a store of ones of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device
-    memory) in each lanes-per-thread form; the first (fewest views) within 3 % of the fastest."""
+def _dirs_per_block_candidates(D8: int) -> tuple:
+    return tuple(sorted({1, min(3, D8), D8}))
+
+
+def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2, 0, 1)) -> tuple:
+    """(views per sweep launch, ``kernels.SweepForm``) for ``views`` views on this grid: the per-view time of the sweep
+    on a store of ones of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device memory) in
+    each form (the plane wavefront in each lanes-per-thread form, the tiled schedule per tile edge, thread form and
+    directions per task); the first (fewest views) within 3 % of the fastest."""
     from . import kernels
 
     N, D8, Q = ctx.num_cells, ctx.directions_per_octant, 4 * num_groups
     device = ctx.device
-    # "form" names the thread forms' meaning: entries timed with the one-lane-per-(view, entry) threads are not reused
+    # "form" names the forms' meaning: entries timed before the tiled schedule existed are not reused
     key = Autotuner.key("sweep", device, N=N, D8=D8, G=num_groups, shape="x".join(map(str, ctx.shape)),
-                        form="views-per-thread")
+                        form="views-per-thread+tiles")
     entry = tuner().table.get(key)
     if entry is None and not torch.cuda.is_current_stream_capturing():
         free, _ = torch.cuda.mem_get_info(device)
         per_view = 8 * D8 * N * Q * 4
-        candidates = [[b, u] for b in VIEW_CANDIDATES if b * per_view <= free // 4 for u in UNROLL_CANDIDATES]
-        candidates = candidates or [[1, u] for u in UNROLL_CANDIDATES]
+        forms = [[u, 0, 1] for u in UNROLL_CANDIDATES] + [[u, t, d] for t in TILE_CANDIDATES for u in TILED_FORMS
+                                                          for d in _dirs_per_block_candidates(D8)]
+        candidates = [[b, *f] for b in VIEW_CANDIDATES if b * per_view <= free // 4 for f in forms]
+        candidates = candidates or [[1, *f] for f in forms]
         stores = {}
 
         def run(c):
-            b, u = c
+            b, u, t, d = c
             if b not in stores:
                 stores.clear()
                 torch.cuda.empty_cache()
                 stores[b] = torch.ones(b, 8, D8, N, Q, device=device)  # non-zero moments, as in a real step
-            kernels.sweep_planes(ctx.flat_index, stores[b], mu_cells, ctx.c, method="persistent", thread_form=u)
+            kernels.sweep_chunk(ctx, stores[b], mu_cells, ctx.c, kernels.SweepForm(u, t, d))
 
         tuner().choose(key, candidates, run, list(default), slack=0.03, per_unit=lambda c: float(c[0]))
         stores.clear()
         torch.cuda.empty_cache()
         entry = tuner().table.get(key)
-    b, u = entry["choice"] if entry is not None else default
-    return min(int(b), max(1, views)), int(u)
+    b, u, t, d = entry["choice"] if entry is not None else default
+    return min(int(b), max(1, views)), kernels.SweepForm(int(u), int(t), int(d))

@@ -107,8 +107,7 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
             else:
                 kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
             del T_all
-        syncs.append(kernels.sweep_planes(ctx.flat_index, store, mu_cells, ctx.c, method="persistent",
-                                          thread_form=form))
+        syncs.append(kernels.sweep_chunk(ctx, store, mu_cells, ctx.c, form))
         moments = torch.empty(B, N_sh, J, device=device) if store_out is None else store_out[b0:b0 + B]
         kernels.small_k_gemm(Yw_t, store.view(B, 8 * D8, J), moments, precision=precision)
         del store

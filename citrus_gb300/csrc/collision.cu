@@ -451,7 +451,17 @@ __device__ void stage_window(const Table& tb, bool valid, float ux, float uy, fl
   }
   __syncthreads();
   const int win_lo = s_window[0], win_n = s_window[1];
-  if (win_lo >= 0) {
+  if (win_lo >= 0 && G % 4 == 0 && ((uintptr_t)tb.t % 16) == 0) {
+    // whole (node, material) blocks of G x G floats as float4, one block per warp at a time: no index division per
+    // element (the padded stride G G + 4 keeps every block 16-byte aligned)
+    const int RS = window_row_stride(G), GG4 = G * G / 4;
+    for (int nm = warp; nm < win_n * tb.M; nm += nwarps) {
+      const int node = nm / tb.M, m = nm - node * tb.M;
+      const float4* src = reinterpret_cast<const float4*>(tb.t + ((int64_t)m * tb.N + win_lo + node) * G * G);
+      float4* dst = reinterpret_cast<float4*>(s_tab + (node * tb.M + m) * RS);
+      for (int r = tid & 31; r < GG4; r += 32) dst[r] = __ldg(src + r);
+    }
+  } else if (win_lo >= 0) {
     const int RS = window_row_stride(G);
     const int per = tb.M * G * G;
     for (int q = tid; q < win_n * per; q += nthreads) {
@@ -656,6 +666,245 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) emission_kernel(
     for (int q = 0; q < kWarps; ++q) acc += s_sum[dd][q][which];
     partial[((int64_t)(d0 + dd) * gridDim.x + blockIdx.x) * 2 + which] = acc;
   }
+}
+
+// ---- attenuated emission, one thread per (point, direction) with all of its groups ---------------------------------
+// A block is 32 points (the lanes, consecutive points and, for one point per cell, consecutive cells) by kEmitWarps
+// warps; warp w takes the block's directions w, w + kEmitWarps, ... . The cosine, the table position, the traced path
+// lengths, the signal sum and the write happen once per (point, direction), where the group lanes of emission_kernel
+// repeat them G times; the multiple-collision source (and per-group optical depths) of a cell are G contiguous floats,
+// read as float4 and coalesced over the warp. Only the transfer entries of incoming groups at or above the outgoing
+// one enter the sum (the reference's first-collision table is downscatter only, uncollided_kernels.py:488-550).
+// Every group value, the group sums and the per-block partial sums are formed in emission_kernel's order (its
+// sequential incoming-group sums, its xor-butterfly group sums, its warp-then-block point sums), so the two kernels
+// give the same bits on a table without upscatter entries.
+constexpr int kEmitWarps = 8;
+
+// x[0] + ... + x[n-1] in the order of an xor butterfly over n lanes read at lane 0: pairwise halves, each addition
+// rounded on its own (a butterfly's shuffles keep a product from fusing into the next addition; here __fadd_rn does)
+template <int n>
+__device__ __forceinline__ float tree_sum(const float* x) {
+  if constexpr (n == 1) {
+    return x[0];
+  } else {
+    return __fadd_rn(tree_sum<n / 2>(x), tree_sum<n / 2>(x + n / 2));
+  }
+}
+
+// sum_{gi <= g} row[gi] phi[gi], in incoming-group order; the row in shared or global memory, float4 reads when the
+// rows are 16-byte aligned (kVec)
+template <int kGP, bool kVec, bool kShared>
+__device__ __forceinline__ float dot_lower(const float* __restrict__ row, const float* phi, int g) {
+  float a = 0.f;
+  if constexpr (kVec) {
+#pragma unroll
+    for (int q = 0; q < kGP / 4; ++q) {
+      if (4 * q > g) break;
+      const float4 t = kShared ? reinterpret_cast<const float4*>(row)[q]
+                               : __ldg(reinterpret_cast<const float4*>(row) + q);
+      a = fmaf(t.x, phi[4 * q], a);
+      if (4 * q + 1 <= g) a = fmaf(t.y, phi[4 * q + 1], a);
+      if (4 * q + 2 <= g) a = fmaf(t.z, phi[4 * q + 2], a);
+      if (4 * q + 3 <= g) a = fmaf(t.w, phi[4 * q + 3], a);
+    }
+  } else {
+#pragma unroll
+    for (int gi = 0; gi < kGP; ++gi) {
+      if (gi > g) break;
+      a = fmaf(kShared ? row[gi] : __ldg(row + gi), phi[gi], a);
+    }
+  }
+  return a;
+}
+
+template <int kGP, bool kVec>
+__device__ __forceinline__ void load_groups(const float* __restrict__ p, int G, float* x) {
+  if constexpr (kVec) {
+#pragma unroll
+    for (int q = 0; q < kGP / 4; ++q) {
+      if (4 * q < G) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(p) + q);
+        x[4 * q] = t.x;
+        x[4 * q + 1] = t.y;
+        x[4 * q + 2] = t.z;
+        x[4 * q + 3] = t.w;
+      } else {
+        x[4 * q] = x[4 * q + 1] = x[4 * q + 2] = x[4 * q + 3] = 0.f;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < kGP; ++q) x[q] = q < G ? __ldg(p + q) : 0.f;
+  }
+}
+
+template <int kGP, int kMM, int kDirs, bool kVec>
+__global__ void __launch_bounds__(32 * kEmitWarps, 3) emission_warps_kernel(
+    FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, int K,
+    const float* __restrict__ tau /*[K, NC, G], or [K, NC, TM] path lengths with tau_mu*/,
+    const float* __restrict__ tau_mu /*[TM, G] or null*/, int TM, const float* __restrict__ mu /*[G, NC]*/,
+    const float* __restrict__ multiple /*[K, NC, G]*/, const float* __restrict__ heights,
+    const float* __restrict__ signal_weight /*[K, G] or null*/, float dx, float dy, float dz,
+    float* __restrict__ out, float* __restrict__ partial /*[K, nblocks, 2]*/) {
+  constexpr int kPW = 32 / kGP;  // points per warp of emission_kernel, whose partial-sum order is kept
+  constexpr int nthreads = 32 * kEmitWarps;
+  extern __shared__ float4 s_dyn4[];
+  float* s_tab = reinterpret_cast<float*>(s_dyn4);
+  __shared__ float s_om[kDirs][3];
+  __shared__ float s_sw[kDirs][kGP];
+  __shared__ float s_tmu[kMM][kGP];
+  __shared__ int s_range[2][32];
+  __shared__ int s_window[2];
+  const int G = tb.G;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int d0 = blockIdx.y * kDirs;
+  const int nd = min(kDirs, K - d0);
+  for (int i = tid; i < kDirs * 3; i += nthreads) s_om[i / 3][i % 3] = i < nd * 3 ? omegas[3 * d0 + i] : 0.f;
+  if (signal_weight != nullptr)
+    for (int i = tid; i < kDirs * kGP; i += nthreads) {
+      const int dd = i / kGP, q = i % kGP;
+      s_sw[dd][q] = (dd < nd && q < G) ? signal_weight[(int64_t)(d0 + dd) * G + q] : 0.f;
+    }
+  for (int i = tid; i < kMM * kGP; i += nthreads) {
+    const int m = i / kGP, q = i % kGP;
+    s_tmu[m][q] = (tau_mu != nullptr && m < TM && q < G) ? tau_mu[m * G + q] : 0.f;
+  }
+
+  const int64_t v = (int64_t)blockIdx.x * 32 + lane;
+  const bool valid = v < in.V;
+  const int64_t NC = (int64_t)pg.Rc * pg.Cc * pg.Sc;
+  float rho[kMM], phi[kGP], muc[kGP];
+  float ux = 0.f, uy = 0.f, uz = 0.f, h = 0.f, offx = 0.f, offy = 0.f, offz = 0.f;
+  int64_t cell = 0;
+#pragma unroll
+  for (int q = 0; q < kGP; ++q) phi[q] = muc[q] = 0.f;
+#pragma unroll
+  for (int m = 0; m < kMM; ++m) rho[m] = 0.f;
+  if (valid) {
+    int i, j, k;
+    point_rcs(v, pg, i, j, k);
+    primary_direction(__ldg(in.ax_x + j), __ldg(in.ax_y + i), __ldg(in.ax_z + k), in.r0x, in.r0y, in.r0z, ux, uy, uz);
+#pragma unroll
+    for (int m = 0; m < kMM; ++m)
+      if (m < tb.M) rho[m] = __ldg(in.rho + (int64_t)m * in.V + v);
+#pragma unroll
+    for (int q = 0; q < kGP; ++q)
+      if (q < G) phi[q] = __ldg(in.phi + (int64_t)q * in.V + v);
+    const int F = pg.f, ic = i / F, jc = j / F, kc = k / F;
+    cell = ((int64_t)ic * pg.Cc + jc) * pg.Sc + kc;
+    const float half = (F - 1) * 0.5f;
+    offy = dy * ((float)(i - ic * F) - half);
+    offx = dx * ((float)(j - jc * F) - half);
+    offz = dz * ((float)(k - kc * F) - half);
+    h = heights ? __ldg(heights + v) : 0.f;
+    if (F > 1) {
+#pragma unroll
+      for (int q = 0; q < kGP; ++q)
+        if (q < G) muc[q] = __ldg(mu + (int64_t)q * NC + cell);
+    }
+  }
+  __syncthreads();  // s_om, s_sw and s_tmu are complete
+  stage_window(tb, valid, ux, uy, uz, s_om, nd, warp, kEmitWarps, warp, kEmitWarps, tid, nthreads, s_range, s_window,
+               s_tab, emission_window_bytes(kDirs));
+  const int win_lo = s_window[0];
+  const int RS = window_row_stride(G);
+
+  auto directions = [&](auto windowed) {
+    constexpr bool kWin = decltype(windowed)::value;
+    for (int dd = warp; dd < nd; dd += kEmitWarps) {
+      const int64_t d = d0 + dd;
+      float e[kGP];
+#pragma unroll
+      for (int q = 0; q < kGP; ++q) e[q] = 0.f;
+      if (valid) {
+        const int64_t dc = d * NC + cell;
+        float smc[kGP], t[kGP];
+        load_groups<kGP, kVec>(multiple + dc * G, G, smc);  // issued first: the longest latency
+        if (tau_mu != nullptr) {  // sum_m mu[m, g] P_m, in material order
+          float P[kMM];
+#pragma unroll
+          for (int m = 0; m < kMM; ++m) P[m] = m < TM ? __ldg(tau + dc * TM + m) : 0.f;
+#pragma unroll
+          for (int q = 0; q < kGP; ++q) t[q] = 0.f;
+#pragma unroll
+          for (int m = 0; m < kMM; ++m)
+            if (m < TM) {
+#pragma unroll
+              for (int q = 0; q < kGP; ++q) t[q] = fmaf(s_tmu[m][q], P[m], t[q]);
+            }
+        } else {
+          load_groups<kGP, kVec>(tau + dc * G, G, t);
+        }
+        const float ox = s_om[dd][0], oy = s_om[dd][1], oz = s_om[dd][2];
+        const float cosine = ux * ox + uy * oy + uz * oz;
+        int i0;
+        float w;
+        table_position(tb, cosine, i0, w);
+        const float offset = pg.f > 1 ? oy * offy + ox * offx + oz * offz : 0.f;
+        float src[kGP];
+#pragma unroll
+        for (int q = 0; q < kGP; ++q) src[q] = 0.f;
+#pragma unroll
+        for (int m = 0; m < kMM; ++m) {
+          const float r = rho[m];
+          if (m >= tb.M || r == 0.f) continue;
+          const float* row0 = kWin ? s_tab + ((i0 - win_lo) * tb.M + m) * RS
+                                   : tb.t + ((int64_t)m * tb.N + i0) * G * G;
+          const float* row1 = row0 + (kWin ? tb.M * RS : G * G);
+#pragma unroll
+          for (int g = 0; g < kGP; ++g) {
+            if (g >= G) break;
+            const float a0 = dot_lower<kGP, kVec, kWin>(row0 + g * G, phi, g);
+            const float a1 = dot_lower<kGP, kVec, kWin>(row1 + g * G, phi, g);
+            src[g] = fmaf(r, a0 + (a1 - a0) * w, src[g]);
+          }
+        }
+#pragma unroll
+        for (int g = 0; g < kGP; ++g) {
+          if (g >= G) break;
+          const float depth = pg.f > 1 ? fmaxf(t[g] - muc[g] * offset, 0.f) : fmaxf(t[g], 0.f);
+          e[g] = (src[g] + smc[g]) * __expf(-depth);  // the fast exponential: within a few ulp for these depths
+        }
+      }
+      const float tot = tree_sum<kGP>(e);
+      if (signal_weight != nullptr) {
+        float sg[kGP];
+#pragma unroll
+        for (int q = 0; q < kGP; ++q) sg[q] = __fmul_rn(s_sw[dd][q], e[q]);
+        if (valid) out[d * in.V + v] = tree_sum<kGP>(sg);
+      } else if (valid) {
+        float* o = out + (d * in.V + v) * G;
+        if (kVec) {
+#pragma unroll
+          for (int q = 0; q < kGP / 4; ++q)
+            if (4 * q < G) reinterpret_cast<float4*>(o)[q] = make_float4(e[4 * q], e[4 * q + 1], e[4 * q + 2], e[4 * q + 3]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < kGP; ++q)
+            if (q < G) o[q] = e[q];
+        }
+      }
+      // emission_kernel's order: a butterfly over its kPW points per warp, then its warps in sequence
+      float a = tot, b = __fmul_rn(tot, h);
+#pragma unroll
+      for (int off = 1; off < kPW; off <<= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+      }
+      float sa = 0.f, sb = 0.f;
+#pragma unroll
+      for (int q = 0; q < kGP; ++q) {
+        sa += __shfl_sync(0xffffffffu, a, q * kPW);
+        sb += __shfl_sync(0xffffffffu, b, q * kPW);
+      }
+      if (lane == 0) {
+        partial[(d * gridDim.x + blockIdx.x) * 2] = sa;
+        partial[(d * gridDim.x + blockIdx.x) * 2 + 1] = sb;
+      }
+    }
+  };
+  if (win_lo >= 0) directions(std::true_type{});
+  else directions(std::false_type{});
 }
 
 // ---- sampling correction over the sweep directions, with the source values kept -----------------------------------
@@ -1272,6 +1521,61 @@ int launch_emission(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const 
                                                harmonics, moments, NS, heights, signal_weight, deltas, out, partial);
 }
 
+template <int kGP, int kMM, int kDirs, bool kVec>
+int launch_emission_warps_d(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                            const float* omegas, int K, const float* tau, const float* tau_mu, int TM,
+                            const float* mu, const float* multiple, const float* heights, const float* signal_weight,
+                            const double* deltas, float* out, float* partial) {
+  constexpr int bytes = emission_window_bytes(kDirs);
+  cudaError_t e = cudaFuncSetAttribute(emission_warps_kernel<kGP, kMM, kDirs, kVec>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "emission window: %s", cudaGetErrorString(e));
+  grid.y = (unsigned)cdiv(K, kDirs);
+  emission_warps_kernel<kGP, kMM, kDirs, kVec><<<grid, 32 * kEmitWarps, bytes, s>>>(
+      in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, heights, signal_weight, (float)deltas[0],
+      (float)deltas[1], (float)deltas[2], out, partial);
+  note_launches();
+  return CITRUS_OK;
+}
+
+template <int kGP, int kMM, bool kVec>
+int launch_emission_warps_v(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                            const float* omegas, int K, const float* tau, const float* tau_mu, int TM,
+                            const float* mu, const float* multiple, const float* heights, const float* signal_weight,
+                            const double* deltas, float* out, float* partial) {
+  if (K >= 64)
+    return launch_emission_warps_d<kGP, kMM, 64, kVec>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                                       heights, signal_weight, deltas, out, partial);
+  return launch_emission_warps_d<kGP, kMM, 32, kVec>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                                     heights, signal_weight, deltas, out, partial);
+}
+
+// the (point, direction) kernel for G <= 16 with the multiple-collision source read (not fused); float4 group rows
+// when G is a multiple of 4 and the table, the per-group inputs and the output are 16-byte aligned
+template <int kGP>
+int launch_emission_warps(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                          const float* omegas, int K, const float* tau, const float* tau_mu, int TM, const float* mu,
+                          const float* multiple, const float* heights, const float* signal_weight,
+                          const double* deltas, float* out, float* partial) {
+  const auto aligned = [](const void* p) { return ((uintptr_t)p % 16) == 0; };
+  const bool vec = tb.G % 4 == 0 && aligned(tb.t) && aligned(multiple) && (tau_mu != nullptr || aligned(tau)) &&
+                   (signal_weight != nullptr || aligned(out));
+  constexpr bool kCanVec = kGP >= 4;  // G < 4 has no float4 rows
+#define CITRUS_EW(MM, VEC)                                                                                         \
+  launch_emission_warps_v<kGP, MM, VEC>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, heights,    \
+                                        signal_weight, deltas, out, partial)
+  if (tb.M <= 2 && TM <= 2) return vec ? CITRUS_EW(2, kCanVec) : CITRUS_EW(2, false);
+  return vec ? CITRUS_EW(kMaxM, kCanVec) : CITRUS_EW(kMaxM, false);
+#undef CITRUS_EW
+}
+
+// CITRUS_EMISSION_KERNEL=groups selects the group-lane kernel (emission_kernel) for the product form too; read at
+// every call, for measurements and for the test that the two kernels agree
+inline bool emission_by_groups() {
+  const char* v = getenv("CITRUS_EMISSION_KERNEL");
+  return v != nullptr && v[0] == 'g';
+}
+
 template <int kGP>
 int emission_for(int64_t V, int K, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
                  const float* omegas, const float* tau, const float* tau_mu, int TM, const float* mu,
@@ -1281,13 +1585,16 @@ int emission_for(int64_t V, int K, cudaStream_t s, const FCInputs& in, const Tab
                  float* height_sums) {
   const int64_t nblocks = cdiv(V, kEmitPoints);
   dim3 grid((unsigned)nblocks, 1u);  // grid.y: the direction blocks, set by the launcher
-  const int st = moments != nullptr
-                     ? launch_emission<kGP, true>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
-                                                  multiple, harmonics, moments, NS, heights, signal_weight, deltas,
-                                                  out, partial)
-                     : launch_emission<kGP, false>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
-                                                   multiple, harmonics, moments, NS, heights, signal_weight, deltas,
-                                                   out, partial);
+  int st;
+  if (moments == nullptr && kGP <= 16 && !emission_by_groups())
+    st = launch_emission_warps<(kGP <= 16 ? kGP : 16)>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                                       heights, signal_weight, deltas, out, partial);
+  else
+    st = moments != nullptr
+             ? launch_emission<kGP, true>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                          harmonics, moments, NS, heights, signal_weight, deltas, out, partial)
+             : launch_emission<kGP, false>(grid, tb.G, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple,
+                                           harmonics, moments, NS, heights, signal_weight, deltas, out, partial);
   if (st) return st;
   reduce_partials_kernel<<<K, dim3(256, 2), 0, s>>>(partial, nblocks, K, height_sums);
   note_launches();

@@ -37,15 +37,14 @@ struct LaneCoef {
   uint32_t at, ax, ay, az;
 };
 
-// lane = (e - start) Dc G + d G + g and every float4 position of a view are below 2^31 (checked on the host)
+// The lane of entry e, direction d and group g; every float4 position of a view is below 2^31 (checked on the host)
 template <int kG>
-__device__ __forceinline__ void lane_coef(uint32_t lane, LaneCoef& k, const float* __restrict__ mu,
-                                          const float* __restrict__ c, const int* __restrict__ octant,
-                                          const int* __restrict__ cell, const int* __restrict__ upstream,
-                                          uint32_t start, uint32_t N, int G_runtime, uint32_t Dc) {
+__device__ __forceinline__ void lane_coef_edg(uint32_t e, uint32_t d, uint32_t g, LaneCoef& k,
+                                              const float* __restrict__ mu, const float* __restrict__ c,
+                                              const int* __restrict__ octant, const int* __restrict__ cell,
+                                              const int* __restrict__ upstream, uint32_t N, int G_runtime,
+                                              uint32_t Dc) {
   const uint32_t G = kG > 0 ? kG : G_runtime;
-  const uint32_t g = lane % G, t = lane / G;
-  const uint32_t d = t % Dc, e = start + t / Dc;
   const int o = __ldg(octant + e);
   const uint32_t n = __ldg(cell + e);
   const uint32_t ux = __ldg(upstream + 3 * e), uy = __ldg(upstream + 3 * e + 1), uz = __ldg(upstream + 3 * e + 2);
@@ -76,6 +75,17 @@ __device__ __forceinline__ void lane_coef(uint32_t lane, LaneCoef& k, const floa
   k.qsx = __fmul_rn(sx, qx);
   k.qsy = __fmul_rn(sy, qy);
   k.qsz = __fmul_rn(sz, qz);
+}
+
+// lane = (e - start) Dc G + d G + g of a plane starting at entry start
+template <int kG>
+__device__ __forceinline__ void lane_coef(uint32_t lane, LaneCoef& k, const float* __restrict__ mu,
+                                          const float* __restrict__ c, const int* __restrict__ octant,
+                                          const int* __restrict__ cell, const int* __restrict__ upstream,
+                                          uint32_t start, uint32_t N, int G_runtime, uint32_t Dc) {
+  const uint32_t G = kG > 0 ? kG : G_runtime;
+  const uint32_t g = lane % G, t = lane / G;
+  lane_coef_edg<kG>(start + t / Dc, t % Dc, g, k, mu, c, octant, cell, upstream, N, G_runtime, Dc);
 }
 
 // The store moments a lane reads in one view: the source (s) and (psi0, psi_x, psi_y, psi_z) of the x, y, z upstream
@@ -170,6 +180,59 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) persistent_kernel(
   }
 }
 
+// The tiled schedule: in each octant's sweep frame the cells are cut into tiles of T^3; the tiles with the same sum
+// of tile coordinates (a tile diagonal) depend only on earlier diagonals, so the grid barrier runs once per tile
+// diagonal instead of once per plane. A block takes one task (a tile of one octant and a block of up to dpb
+// directions) and walks the tile's 3 T - 2 sub-planes (cells with the same sum of in-tile coordinates) with a block
+// barrier between them: the upstream reads of a sub-plane are the block's own writes one sub-plane earlier (L2 hits),
+// and only the reads across a tile face come from an earlier diagonal. Every lane is the per-plane kernel's lane with
+// the same inputs, so the store comes out bit for bit the same.
+//
+// Tables (host-built, transport_sweep.build_tiled_plan): entries (octant, cell, upstream) ordered by task and
+// sub-plane; sub_offsets [tasks, num_sub + 1] the entry range of each sub-plane of each task; diagonal_offsets
+// [num_diagonals + 1] the task range of each diagonal.
+template <int kG, int kVB, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) tiled_kernel(
+    float4* __restrict__ store, const float* __restrict__ mu, const float* __restrict__ c,
+    const int* __restrict__ octant, const int* __restrict__ cell, const int* __restrict__ upstream,
+    const int* __restrict__ diagonal_offsets, const int* __restrict__ sub_offsets, int num_diagonals, int num_sub,
+    uint32_t N, int G_runtime, uint32_t Dc, uint32_t dpb, int views, int64_t view_stride, unsigned* sync,
+    uint64_t timeout_ns, int skip) {
+  const uint32_t G = kG > 0 ? kG : G_runtime;
+  const uint32_t dir_blocks = (Dc + dpb - 1) / dpb;
+  for (int D = 0; D < num_diagonals; ++D) {
+    const uint32_t t0 = __ldg(diagonal_offsets + D);
+    const uint32_t work = (__ldg(diagonal_offsets + D + 1) - t0) * dir_blocks;
+    for (uint32_t w = blockIdx.x; w < work; w += gridDim.x) {
+      const uint32_t task = t0 + w / dir_blocks, d0 = (w % dir_blocks) * dpb;
+      const uint32_t nd = min(dpb, Dc - d0);
+      const int* so = sub_offsets + (size_t)task * (num_sub + 1);
+      for (int sp = 0; sp < num_sub; ++sp) {
+        const uint32_t start = __ldg(so + sp), count = __ldg(so + sp + 1) - start;
+        if (count == 0) continue;  // the same for every thread of the block
+        const uint32_t total = count * nd * G;
+        for (uint32_t lane = threadIdx.x; lane < total; lane += kThreads) {
+          const uint32_t g = lane % G, t = lane / G;
+          LaneCoef k;
+          lane_coef_edg<kG>(start + t / nd, d0 + t % nd, g, k, mu, c, octant, cell, upstream, N, G_runtime, Dc);
+          float4* view = store;
+          for (int v0 = 0; v0 < views; v0 += kVB, view += kVB * view_stride) {
+            LaneIn in[kVB];
+#pragma unroll
+            for (int j = 0; j < kVB; ++j)
+              if (v0 + j < views) gather_view<true>(k, view + j * view_stride, in[j]);
+#pragma unroll
+            for (int j = 0; j < kVB; ++j)
+              if (v0 + j < views) solve_view(k, in[j], view + j * view_stride);
+          }
+        }
+        __syncthreads();  // the sub-plane's outputs are written before the next sub-plane reads them
+      }
+    }
+    if (D + 1 < num_diagonals && !grid_barrier(sync, gridDim.x, timeout_ns, skip)) return;
+  }
+}
+
 template <int kG>
 int launch_planes(float* store, const float* mu, const float* c, const int* octant, const int* cell,
                   const int* upstream, const int64_t* offsets, int64_t num_planes, int64_t N, int G, int64_t Dc,
@@ -212,6 +275,51 @@ int launch_persistent_u(float* store, const float* mu, const float* c, const int
   if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_persistent: %s", cudaGetErrorString(e));
   note_launches();
   return CITRUS_OK;
+}
+
+template <int kG, int kVB, int kMinBlocks>
+int launch_tiled_u(float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                   const int* upstream, const int* diagonal_offsets, const int* sub_offsets, int num_diagonals,
+                   int num_sub, int64_t N, int G, int64_t Dc, int64_t dpb, int64_t views, unsigned* sync,
+                   int64_t max_blocks, uint64_t timeout_ns, int skip, cudaStream_t stream) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tiled_kernel<kG, kVB, kMinBlocks>, kThreads,
+                                                                0);
+  if (e != cudaSuccess || per_sm < 1) return set_error(CITRUS_ECUDA, "citrus_sweep_tiled: occupancy query failed");
+  int64_t blocks = (int64_t)per_sm * num_sms();
+  if (max_blocks > 0 && max_blocks < blocks) blocks = max_blocks;
+  if (skip >= blocks) skip = (int)blocks - 1;
+  float4* store4 = reinterpret_cast<float4*>(store);
+  uint32_t n32 = (uint32_t)N, dc32 = (uint32_t)Dc, dpb32 = (uint32_t)dpb;
+  int views32 = (int)views;
+  int64_t view_stride = 8 * Dc * N * (int64_t)G;  // float4 per view
+  cudaError_t z = cudaMemsetAsync(sync, 0, 4 * sizeof(unsigned), stream);
+  if (z != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_sweep_tiled: %s", cudaGetErrorString(z));
+  void* args[] = {&store4, &mu, &c, &octant, &cell, &upstream, &diagonal_offsets, &sub_offsets, &num_diagonals,
+                  &num_sub, &n32, &G, &dc32, &dpb32, &views32, &view_stride, &sync, &timeout_ns, &skip};
+  e = cudaLaunchCooperativeKernel((const void*)tiled_kernel<kG, kVB, kMinBlocks>, dim3((unsigned)blocks),
+                                  dim3(kThreads), args, 0, stream);
+  if (e != cudaSuccess) return set_error(CITRUS_ELAUNCH, "citrus_sweep_tiled: %s", cudaGetErrorString(e));
+  note_launches();
+  return CITRUS_OK;
+}
+
+// the thread forms of the tiled launch: one view at a time (four blocks per SM), or the loads of two views issued
+// before their solves (three blocks per SM)
+template <int kG>
+int launch_tiled(float* store, const float* mu, const float* c, const int* octant, const int* cell,
+                 const int* upstream, const int* diagonal_offsets, const int* sub_offsets, int num_diagonals,
+                 int num_sub, int64_t N, int G, int64_t Dc, int64_t dpb, int64_t views, unsigned* sync,
+                 int64_t max_blocks, uint64_t timeout_ns, int skip, cudaStream_t stream, int form) {
+  if (form == 2)
+    return launch_tiled_u<kG, 2, 3>(store, mu, c, octant, cell, upstream, diagonal_offsets, sub_offsets,
+                                    num_diagonals, num_sub, N, G, Dc, dpb, views, sync, max_blocks, timeout_ns, skip,
+                                    stream);
+  if (form == 1)
+    return launch_tiled_u<kG, 1, 4>(store, mu, c, octant, cell, upstream, diagonal_offsets, sub_offsets,
+                                    num_diagonals, num_sub, N, G, Dc, dpb, views, sync, max_blocks, timeout_ns, skip,
+                                    stream);
+  return set_error(CITRUS_EINVAL, "citrus_sweep_tiled: thread form %d (1 or 2)", form);
 }
 
 constexpr int kDefaultUnroll = 1;
@@ -331,6 +439,43 @@ extern "C" int citrus_sweep_persistent(float* store, const float* mu_cells, cons
   return citrus_sweep_persistent_config(store, mu_cells, c, octant, cell, upstream, plane_offsets_dev, num_planes,
                                         num_cells, num_groups, dc, views, sync, max_blocks, 0, timeout_ns, skip_block,
                                         stream);
+}
+
+extern "C" int citrus_sweep_tiled(float* store, const float* mu_cells, const float* c, const int32_t* octant,
+                                  const int32_t* cell, const int32_t* upstream, const int32_t* diagonal_offsets,
+                                  const int32_t* sub_offsets, int64_t num_diagonals, int64_t num_sub,
+                                  int64_t num_cells, int64_t num_groups, int64_t dc, int64_t views,
+                                  int64_t dirs_per_block, uint32_t* sync, int64_t max_blocks, int64_t thread_form,
+                                  int64_t timeout_ns, int64_t skip_block, void* stream) {
+  int status = check_sweep_args(store, mu_cells, c, octant, cell, upstream, num_diagonals, num_cells, num_groups, dc,
+                                views);
+  if (status) return status;
+  CITRUS_REQUIRE(diagonal_offsets && sub_offsets && sync, "citrus_sweep_tiled: null tables or sync words");
+  CITRUS_REQUIRE(num_sub >= 1 && num_sub <= 4096 && num_diagonals <= (1 << 20),
+                 "citrus_sweep_tiled: bad table sizes (diagonals %lld, sub-planes %lld)", (long long)num_diagonals,
+                 (long long)num_sub);
+  CITRUS_REQUIRE(dirs_per_block >= 1 && dirs_per_block <= dc, "citrus_sweep_tiled: directions per block %lld outside "
+                 "[1, %lld]", (long long)dirs_per_block, (long long)dc);
+  CITRUS_REQUIRE(timeout_ns > 0, "citrus_sweep_tiled: timeout_ns must be positive");
+  const int G = (int)num_groups, ND = (int)num_diagonals, NS = (int)num_sub, form = (int)thread_form;
+  const uint64_t t = (uint64_t)timeout_ns;
+  const int skip = (int)skip_block;
+  unsigned* sy = reinterpret_cast<unsigned*>(sync);
+  cudaStream_t s = as_stream(stream);
+#define CITRUS_TILED(KG)                                                                                           \
+  launch_tiled<KG>(store, mu_cells, c, octant, cell, upstream, diagonal_offsets, sub_offsets, ND, NS, num_cells, G, \
+                   dc, dirs_per_block, views, sy, max_blocks, t, skip, s, form)
+  switch (G) {
+    case 1: status = CITRUS_TILED(1); break;
+    case 2: status = CITRUS_TILED(2); break;
+    case 4: status = CITRUS_TILED(4); break;
+    case 8: status = CITRUS_TILED(8); break;
+    case 16: status = CITRUS_TILED(16); break;
+    default: status = CITRUS_TILED(0); break;
+  }
+#undef CITRUS_TILED
+  if (status) return status;
+  return launch_status("citrus_sweep_tiled");
 }
 
 // ---- allocation-free persistent sweep ----------------------------------------------------------------------------

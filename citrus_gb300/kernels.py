@@ -71,6 +71,93 @@ class FlatPlaneIndex:
         return len(self.offsets) - 1
 
 
+@dataclass(frozen=True)
+class TiledIndex:
+    """A sweep plan's int32 entry tables in tile-diagonal order on the sweep device (``transport_sweep.TiledPlan``).
+
+    Attributes:
+        tile: tile edge T in cells.
+        num_sub: sub-planes per tile, 3 T - 2.
+        octant, cell, upstream: the entries ([E], [E], [E * 3] with N for vacuum) by task and sub-plane.
+        sub_offsets: [tasks, num_sub + 1] entry ranges of the tasks' sub-planes.
+        diagonal_offsets: [num_diagonals + 1] task ranges of the diagonals.
+    """
+
+    tile: int
+    num_sub: int
+    octant: Tensor
+    cell: Tensor
+    upstream: Tensor
+    sub_offsets: Tensor
+    diagonal_offsets: Tensor
+
+    @property
+    def num_diagonals(self) -> int:
+        return int(self.diagonal_offsets.numel() - 1)
+
+
+@dataclass(frozen=True)
+class SweepForm:
+    """How an accumulator sweep runs: ``tile`` 0 is the plane wavefront (one grid barrier per plane) with the thread
+    form ``thread_form`` of ``sweep_planes``; a tile edge T > 0 is the tiled schedule (``sweep_tiled``: one grid barrier
+    per tile diagonal) with ``dirs_per_block`` directions per task and thread form 1 or 2."""
+
+    thread_form: int = 1
+    tile: int = 0
+    dirs_per_block: int = 1
+
+
+def sweep_tiled(index: TiledIndex, store: Tensor, mu_cells: Tensor, c: Tensor, *, dirs_per_block: int = 1,
+                thread_form: int = 1, sync: Optional[Tensor] = None, max_blocks: int = 0,
+                timeout_ns: int = DEFAULT_BARRIER_TIMEOUT_NS, skip_block: int = -1) -> Tensor:
+    """Sweep one direction chunk in place with the tiled schedule: the same store as ``sweep_planes``, bit for bit.
+
+    Args:
+        index: the tile-diagonal entry tables of the grid.
+        store, mu_cells, c: as ``sweep_planes``.
+        dirs_per_block: directions of a chunk that one block sweeps through a tile (1 to Dc).
+        thread_form: 1 (one view at a time, four blocks per SM) or 2 (the loads of two views before their solves).
+        sync, max_blocks, timeout_ns, skip_block: as the persistent launch of ``sweep_planes``.
+
+    Returns:
+        The sync words (``sync[2] != 0`` means a barrier wait ran out).
+    """
+    views, Dc, N, G = _sweep_shape(store, mu_cells, c)
+    if index.octant.numel() != 8 * N:
+        raise ValueError("the tiled index does not belong to this grid")
+    if not 1 <= int(dirs_per_block) <= Dc:
+        raise ValueError(f"dirs_per_block must be in [1, {Dc}], got {dirs_per_block}")
+    if sync is None:
+        sync = torch.empty(4, dtype=torch.int32, device=store.device)
+    _lib.call("citrus_sweep_tiled", store.data_ptr(), mu_cells.data_ptr(), c.data_ptr(), index.octant.data_ptr(),
+              index.cell.data_ptr(), index.upstream.data_ptr(), index.diagonal_offsets.data_ptr(),
+              index.sub_offsets.data_ptr(), index.num_diagonals, index.num_sub, N, G, Dc, views,
+              int(dirs_per_block), sync.data_ptr(), int(max_blocks), int(thread_form), int(timeout_ns),
+              int(skip_block), _lib.stream_handle(store.device))
+    return sync
+
+
+def _sweep_shape(store: Tensor, mu_cells: Tensor, c: Tensor) -> tuple:
+    """(views, Dc, N, G) of a sweep store, after the checks of ``sweep_planes``."""
+    if store.dim() == 4:
+        views, (_, Dc, N, Q) = 1, store.shape
+    elif store.dim() == 5:
+        views, _, Dc, N, Q = store.shape
+    else:
+        raise ValueError(f"store must be [8, Dc, N, 4G] or [V, 8, Dc, N, 4G], got {tuple(store.shape)}")
+    if store.shape[-4] != 8 or Q % 4:
+        raise ValueError(f"store must be [.., 8, Dc, N, 4G], got {tuple(store.shape)}")
+    G = Q // 4
+    _check_cuda_f32("store", store)
+    _check_cuda_f32("mu_cells", mu_cells)
+    _check_cuda_f32("c", c)
+    if tuple(mu_cells.shape) != (N, G):
+        raise ValueError(f"mu_cells must be [{N}, {G}], got {tuple(mu_cells.shape)}")
+    if tuple(c.shape) != (8, Dc, 3):
+        raise ValueError(f"c must be [8, {Dc}, 3], got {tuple(c.shape)}")
+    return int(views), int(Dc), int(N), int(G)
+
+
 def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tensor, *, method: str = "persistent",
                  sync: Optional[Tensor] = None, max_blocks: int = 0,
                  timeout_ns: int = DEFAULT_BARRIER_TIMEOUT_NS, skip_block: int = -1,
@@ -95,22 +182,7 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
     Returns:
         The sync words of the persistent launch (``sync[2] != 0`` means a barrier wait ran out), or None.
     """
-    if store.dim() == 4:
-        views, (_, Dc, N, Q) = 1, store.shape
-    elif store.dim() == 5:
-        views, _, Dc, N, Q = store.shape
-    else:
-        raise ValueError(f"store must be [8, Dc, N, 4G] or [V, 8, Dc, N, 4G], got {tuple(store.shape)}")
-    if store.shape[-4] != 8 or Q % 4:
-        raise ValueError(f"store must be [.., 8, Dc, N, 4G], got {tuple(store.shape)}")
-    G = Q // 4
-    _check_cuda_f32("store", store)
-    _check_cuda_f32("mu_cells", mu_cells)
-    _check_cuda_f32("c", c)
-    if tuple(mu_cells.shape) != (N, G):
-        raise ValueError(f"mu_cells must be [{N}, {G}], got {tuple(mu_cells.shape)}")
-    if tuple(c.shape) != (8, Dc, 3):
-        raise ValueError(f"c must be [8, {Dc}, 3], got {tuple(c.shape)}")
+    views, Dc, N, G = _sweep_shape(store, mu_cells, c)
     if index.octant.numel() != 8 * N:
         raise ValueError("the plane index does not belong to this grid")
     stream = _lib.stream_handle(store.device)
@@ -128,6 +200,16 @@ def sweep_planes(index: FlatPlaneIndex, store: Tensor, mu_cells: Tensor, c: Tens
               index.num_planes, N, G, Dc, views, sync.data_ptr(), int(max_blocks), int(thread_form),
               int(timeout_ns), int(skip_block), stream)
     return sync
+
+
+def sweep_chunk(ctx, store: Tensor, mu_cells: Tensor, c: Tensor, form: SweepForm, **kwargs) -> Optional[Tensor]:
+    """Sweep a chunk in the form ``form``: the plane wavefront of ``sweep_planes`` (persistent) or the tiled schedule
+    of ``sweep_tiled`` on the context's tables (``ctx.flat_index`` / ``ctx.tiled_index(T)``)."""
+    if form.tile > 0:
+        return sweep_tiled(ctx.tiled_index(form.tile), store, mu_cells, c, dirs_per_block=min(form.dirs_per_block,
+                           int(c.shape[1])), thread_form=form.thread_form, **kwargs)
+    return sweep_planes(ctx.flat_index, store, mu_cells, c, method="persistent", thread_form=form.thread_form,
+                        **kwargs)
 
 
 # =====================================================================================================================

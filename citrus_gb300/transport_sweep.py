@@ -79,6 +79,85 @@ def build_sweep_plan(shape) -> SweepPlan:
 
 
 @dataclass(frozen=True, eq=False)
+class TiledPlan:
+    """The entries of a sweep plan in tile-diagonal order (no counterpart in the reference, whose plan is one launch
+    per plane): in each octant's sweep frame the cells are cut into tiles of ``tile``^3; a task is one tile of one
+    octant, the tasks of a diagonal (equal sums of tile coordinates) are independent, and within a task the entries run
+    by sub-plane (equal sums of in-tile coordinates).
+
+    Attributes:
+        octant, cell, upstream: the entries (as in ``SweepPlan``), ordered by task and sub-plane.
+        sub_offsets: [tasks, num_sub + 1] entry range of each sub-plane of each task.
+        diagonal_offsets: [num_diagonals + 1] task range of each diagonal.
+    """
+
+    shape: tuple
+    tile: int
+    num_sub: int
+    octant: np.ndarray
+    cell: np.ndarray
+    upstream: np.ndarray
+    sub_offsets: np.ndarray
+    diagonal_offsets: np.ndarray
+
+    @property
+    def num_diagonals(self) -> int:
+        return int(self.diagonal_offsets.size - 1)
+
+    @property
+    def num_tasks(self) -> int:
+        return int(self.sub_offsets.shape[0])
+
+
+def build_tiled_plan(shape, tile: int) -> TiledPlan:
+    """The plan's entries in tile-diagonal order: a cell's octant-frame coordinates (as in ``build_sweep_plan``) split
+    into tile coordinates (the diagonal is their sum) and in-tile coordinates (the sub-plane is their sum); every
+    upstream neighbour of a cell is on the same sub-plane minus one of its tile or on an earlier diagonal."""
+    R, C, S = (int(v) for v in shape)
+    T = int(tile)
+    if T < 1:
+        raise ValueError("tile must be >= 1")
+    i, j, k = (a.reshape(-1) for a in np.meshgrid(np.arange(R), np.arange(C), np.arange(S), indexing="ij"))
+    flat = (i * C + j) * S + k
+    n = flat.size
+    nt = [-(-C // T), -(-R // T), -(-S // T)]                      # tiles along x (cols), y (rows), z (slices)
+    num_sub = 3 * T - 2
+    octs, cells, ups, keys, subs, diags = [], [], [], [], [], []
+    for o in range(8):
+        sx, sy, sz = OCTANT_SIGNS[o]
+        px = j if sx > 0 else C - 1 - j
+        py = i if sy > 0 else R - 1 - i
+        pz = k if sz > 0 else S - 1 - k
+        nj, ni, nk = j - sx, i - sy, k - sz
+        ux = np.where((nj >= 0) & (nj < C), (i * C + nj) * S + k, -1)
+        uy = np.where((ni >= 0) & (ni < R), (ni * C + j) * S + k, -1)
+        uz = np.where((nk >= 0) & (nk < S), (i * C + j) * S + nk, -1)
+        tx, ty, tz = px // T, py // T, pz // T
+        diag = tx + ty + tz
+        keys.append(((diag * 8 + o) * nt[0] + tx) * nt[1] * nt[2] + ty * nt[2] + tz)
+        subs.append(px % T + py % T + pz % T)
+        diags.append(diag)
+        octs.append(np.full(n, o, dtype=np.int64))
+        cells.append(flat)
+        ups.append(np.stack([ux, uy, uz], axis=1))
+    key, sub, diag, octant, cell, upstream = (np.concatenate(a) for a in (keys, subs, diags, octs, cells, ups))
+    task_keys, task = np.unique(key, return_inverse=True)          # ascending key: diagonals in order
+    order = np.lexsort((cell, sub, task))
+    octant, cell, upstream, sub, task = octant[order], cell[order], upstream[order], sub[order], task[order]
+    num_tasks = task_keys.size
+    counts = np.bincount(task * num_sub + sub, minlength=num_tasks * num_sub).reshape(num_tasks, num_sub)
+    sub_offsets = np.zeros((num_tasks, num_sub + 1), dtype=np.int64)
+    sub_offsets[:, 1:] = np.cumsum(counts, axis=1)
+    sub_offsets += np.concatenate([[0], np.cumsum(counts.sum(1))[:-1]])[:, None]
+    task_diag = np.zeros(num_tasks, dtype=np.int64)
+    task_diag[task] = diag[order]
+    num_diagonals = int(task_diag.max()) + 1
+    diagonal_offsets = np.zeros(num_diagonals + 1, dtype=np.int64)
+    diagonal_offsets[1:] = np.cumsum(np.bincount(task_diag, minlength=num_diagonals))
+    return TiledPlan((R, C, S), T, num_sub, octant, cell, upstream, sub_offsets, diagonal_offsets)
+
+
+@dataclass(frozen=True, eq=False)
 class SweepContext:
     """Everything the sweep needs that depends only on the grid and the quadrature (reference
     ``transport_sweep.py:77-153``); device tables are float32 / int32 on ``device``."""
@@ -103,6 +182,20 @@ class SweepContext:
     @property
     def num_cells(self) -> int:
         return self.shape[0] * self.shape[1] * self.shape[2]
+
+    def tiled_index(self, tile: int) -> kernels.TiledIndex:
+        """The entry tables in tile-diagonal order for tiles of ``tile``^3 cells (built once per tile size)."""
+        cache = self.__dict__.setdefault("_tiled", {})
+        index = cache.get(int(tile))
+        if index is None:
+            plan = build_tiled_plan(self.shape, int(tile))
+            up = np.where(plan.upstream < 0, self.num_cells, plan.upstream)
+            dev = lambda a: torch.as_tensor(np.ascontiguousarray(a).astype(np.int32)).to(self.device)  # noqa: E731
+            index = kernels.TiledIndex(tile=int(tile), num_sub=plan.num_sub, octant=dev(plan.octant),
+                                       cell=dev(plan.cell), upstream=dev(up.reshape(-1)),
+                                       sub_offsets=dev(plan.sub_offsets), diagonal_offsets=dev(plan.diagonal_offsets))
+            cache[int(tile)] = index
+        return index
 
     @property
     def num_planes(self) -> int:

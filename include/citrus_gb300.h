@@ -74,6 +74,22 @@ int citrus_sweep_persistent_config(float* store, const float* mu_cells, const fl
                                    int64_t views, uint32_t* sync, int64_t max_blocks, int32_t thread_form,
                                    int64_t timeout_ns, int64_t skip_block, void* stream);
 
+/* The accumulator sweep of one chunk in the tiled schedule (no counterpart in the reference, whose sweep_planes,
+ * citrus/scatter_solver/kernels/sweep_kernels.py:265-290, launches once per plane): the same lanes and the same store
+ * as citrus_sweep_planes, bit for bit, in one cooperative launch whose grid barrier runs once per tile diagonal. The
+ * entries (octant, cell, upstream; num_cells for vacuum) are ordered by task (one tile of T^3 cells of one octant) and
+ * sub-plane; sub_offsets [tasks, num_sub + 1] (num_sub = 3 T - 2) holds each task's sub-plane entry ranges and
+ * diagonal_offsets [num_diagonals + 1] each diagonal's task range (int32 device tables). A block sweeps one task for
+ * dirs_per_block directions of the chunk (1..dc) through its sub-planes with block barriers. thread_form: 1 one view
+ * at a time, 2 the loads of two views before their solves. sync: 4 device words (sync[2] != 0 after the launch: a
+ * barrier wait ran past timeout_ns and the store is invalid); skip_block >= 0 is a test hook (that block never
+ * arrives). */
+int citrus_sweep_tiled(float* store, const float* mu_cells, const float* c, const int32_t* octant, const int32_t* cell,
+                       const int32_t* upstream, const int32_t* diagonal_offsets, const int32_t* sub_offsets,
+                       int64_t num_diagonals, int64_t num_sub, int64_t num_cells, int64_t num_groups, int64_t dc,
+                       int64_t views, int64_t dirs_per_block, uint32_t* sync, int64_t max_blocks, int64_t thread_form,
+                       int64_t timeout_ns, int64_t skip_block, void* stream);
+
 /* The persistent sweep without any allocation: no counterpart in the reference, which always runs the sweep through
  * torch's allocator. The barrier words and the plane offsets live in a static device array of this library (33 KB
  * per device, at most 8191 planes, i.e. R + C + S - 2 <= 8191; more planes return CITRUS_EINVAL). The call clears

@@ -98,6 +98,59 @@ def test_persistent_barrier_timeout_is_reported(cuda_device):
     assert int(ok[2]) == 0
 
 
+@pytest.mark.parametrize("shape, G, V, tile", [((5, 7, 6), 3, 2, 2), ((12, 9, 10), 8, 3, 4), ((9, 8, 17), 1, 1, 8),
+                                              ((16, 16, 16), 4, 2, 8), ((6, 5, 7), 2, 2, 3)])
+def test_tiled_sweep_equals_per_plane_sweep_bitwise(cuda_device, shape, G, V, tile):
+    """The tiled schedule (grid barrier per tile diagonal, block barrier per sub-plane) gives the per-plane kernel's
+    store bit for bit, for tiles that divide the grid or not, every thread form and directions per task."""
+    rng = np.random.default_rng(sum(shape) + G)
+    ctx = make_sweep_context(Grid(shape, 0.5), product_quadrature(4, 12), 2, cuda_device)
+    N, D8 = ctx.num_cells, ctx.directions_per_octant
+    mu = torch.as_tensor(rng.random((N, G)) + 0.1, dtype=torch.float32, device=cuda_device)
+    c = ctx.c.contiguous()
+    stores = torch.as_tensor(rng.standard_normal((V, 8, D8, N, 4 * G)), dtype=torch.float32, device=cuda_device)
+    expected = stores.clone()
+    for v in range(V):
+        kernels.sweep_planes(ctx.flat_index, expected[v], mu, c, method="planes")
+    for form in (1, 2):
+        for dpb in sorted({1, 2, D8}):
+            got = stores.clone()
+            sync = kernels.sweep_tiled(ctx.tiled_index(tile), got, mu, c, dirs_per_block=dpb, thread_form=form)
+            assert torch.equal(got, expected), (form, dpb)
+            assert int(sync[2]) == 0
+
+
+def test_tiled_sweep_inside_the_accumulator_step_form(cuda_device):
+    """kernels.sweep_chunk with a tiled form on one view equals the plane wavefront's persistent form."""
+    rng = np.random.default_rng(9)
+    shape, G = (10, 8, 9), 4
+    ctx = make_sweep_context(Grid(shape, 0.5), product_quadrature(4, 8), 2, cuda_device)
+    N, D8 = ctx.num_cells, ctx.directions_per_octant
+    mu = torch.as_tensor(rng.random((N, G)) + 0.1, dtype=torch.float32, device=cuda_device)
+    store = torch.as_tensor(rng.standard_normal((2, 8, D8, N, 4 * G)), dtype=torch.float32, device=cuda_device)
+    a, b = store.clone(), store.clone()
+    kernels.sweep_chunk(ctx, a, mu, ctx.c, kernels.SweepForm(1, 0, 1))
+    kernels.sweep_chunk(ctx, b, mu, ctx.c, kernels.SweepForm(2, 4, 2))
+    assert torch.equal(a, b)
+
+
+def test_tiled_barrier_timeout_is_reported(cuda_device):
+    """A block of the tiled launch that never arrives makes every diagonal's barrier wait run out after the bounded
+    timeout; the kernel returns, the sync word records it, and the next launch runs normally."""
+    ctx = make_sweep_context(Grid((8, 8, 8), 1.0), product_quadrature(2, 4), 1, cuda_device)
+    N, G = ctx.num_cells, 2
+    store = torch.zeros(8, 1, N, 4 * G, device=cuda_device)
+    mu = torch.ones(N, G, device=cuda_device)
+    index = ctx.tiled_index(4)
+    sync = kernels.sweep_tiled(index, store, mu, ctx.c.contiguous(), max_blocks=4, timeout_ns=20_000_000,
+                               skip_block=1)
+    torch.cuda.synchronize()
+    assert int(sync[2]) != 0
+    ok = kernels.sweep_tiled(index, store, mu, ctx.c.contiguous(), max_blocks=4)
+    torch.cuda.synchronize()
+    assert int(ok[2]) == 0
+
+
 @pytest.mark.parametrize("M, K, J, batch, accumulate", [(120, 36, 4096, 1, False), (36, 120, 1028, 1, True),
                                                         (5, 7, 64, 3, True), (240, 64, 512, 2, False),
                                                         (1, 1, 4, 1, False), (133, 36, 515, 1, True),
