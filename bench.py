@@ -545,6 +545,7 @@ def spr_error(w, solver, angles, device) -> dict:
     import torch
 
     from citrus_gb300.citrus_step import CitrusState, citrus_view_step
+    from citrus_gb300.view_sharding import gather_signals
     from citrus_gb300.scatter_solver import ScatterSolver
 
     ref_solver = ScatterSolver(solver.library, dataclasses.replace(solver.config, moment_precision="fp32"),
@@ -750,7 +751,8 @@ def run_step(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=device)
     w, solver, angles = make_step_solver(device, args.views, args.cells, args.precision)
-    # weak scaling: every rank runs its own set of views (offset by the rank) of the same phantom
+    # weak scaling: every rank owns V views of the V x world views of the outer iteration, round-robin (views rank,
+    # rank + world, ...: the angles of the first V views offset by the rank), as view_sharding.owned_views assigns
     angles = angles + rank * (2 * math.pi / len(angles)) / max(1, world)
     V = len(angles)
     rho_host = torch.as_tensor(w.rho, dtype=torch.float32).pin_memory()
@@ -768,20 +770,27 @@ def run_step(args):
             out, _, new_states = batched_view_steps(solver, states, fields, [float(a) for a in angles],
                                                     batch=args.batch)
             states[:] = new_states
-            if signals is not None:
-                signals.copy_(out, non_blocking=True)
-            return
-        for v, angle in enumerate(angles):
-            scatter, _, states[v] = citrus_view_step(solver, states[v], fields, float(angle), primary=False)
-            if signals is not None:
-                signals[v].copy_(scatter, non_blocking=True)
+        else:
+            outs = []
+            for v, angle in enumerate(angles):
+                scatter, _, states[v] = citrus_view_step(solver, states[v], fields, float(angle), primary=False)
+                outs.append(scatter)
+            out = torch.stack(outs)
+        finish(out, signals)
+
+    def finish(out, signals):
+        # with several ranks, every rank's views (round-robin shares of the V x world views) are all-gathered in view
+        # order, the outer iteration's one collective (view_sharding.gather_signals); rank 0 copies them out
+        if dist:
+            out = gather_signals(out, V * world)
+        if signals is not None:
+            signals.copy_(out[:V] if dist else out, non_blocking=True)
 
     def one_step(rho, signals=None):
         if graphed is None:
             return eager_step(rho, signals)
         out, _ = graphed.step(rho)
-        if signals is not None:
-            signals.copy_(out, non_blocking=True)
+        finish(out, signals)
 
     sampler = ClockSampler(local)  # started before the warm-up: its first nvidia-smi call is slow
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -33,6 +33,7 @@ SIGNATURES = {
     "citrus_small_k_gemm_config": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, I32, I32, P],
     "citrus_source_expansion_first": [P, I64, P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I64, P],
     "citrus_small_k_gemm_bf16x3": [P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I32, P, P],
+    "citrus_source_expansion_first_bf16x3": [P, I64, P, I64, P, I64, P, I64, I64, I64, I64, I64, I64, I64, I64, P, P],
     "citrus_state_encode": [P, I64, I64, I64, I64, I64, I64, P, P, P],
     "citrus_state_decode": [P, P, I64, I64, I64, P, I64, I64, I64, I64, P],
     "citrus_attenuation_to_density": [P, I64, P, P, P, I64, I64, P, P],

@@ -162,14 +162,9 @@ VIEW_CANDIDATES = (1, 2, 4, 8)
 # registers capped for 5 (form 1), 6 (form 3) or 4 (form 5) blocks of 256 threads per SM, or the loads of 2 (form 2)
 # or 4 (form 4) views issued before their solves
 UNROLL_CANDIDATES = (1, 3, 5, 2, 4)
-# the tiled schedule (one grid barrier per tile diagonal): tile edges, thread forms (1: one view at a time, 2: the
-# loads of two views first) and directions per task (1, a few, or the whole chunk, as the chunk allows)
-TILE_CANDIDATES = (4, 8)
-TILED_FORMS = (1, 2)
-
-
-def _dirs_per_block_candidates(D8: int) -> tuple:
-    return tuple(sorted({1, min(3, D8), D8}))
+# the tiled schedule (one grid barrier per tile diagonal) in the forms that came closest to the plane wavefront on the
+# 64^3 x 120-direction grid: (thread form, tile edge, directions per task); directions per task are capped by the chunk
+TILED_CANDIDATES = ((2, 4, 5), (2, 8, 3), (1, 4, 5), (1, 8, 3))
 
 
 def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2, 0, 1)) -> tuple:
@@ -188,8 +183,7 @@ def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2, 0, 1
     if entry is None and not torch.cuda.is_current_stream_capturing():
         free, _ = torch.cuda.mem_get_info(device)
         per_view = 8 * D8 * N * Q * 4
-        forms = [[u, 0, 1] for u in UNROLL_CANDIDATES] + [[u, t, d] for t in TILE_CANDIDATES for u in TILED_FORMS
-                                                          for d in _dirs_per_block_candidates(D8)]
+        forms = [[u, 0, 1] for u in UNROLL_CANDIDATES] + [[u, t, min(d, D8)] for u, t, d in TILED_CANDIDATES]
         candidates = [[b, *f] for b in VIEW_CANDIDATES if b * per_view <= free // 4 for f in forms]
         candidates = candidates or [[1, *f] for f in forms]
         stores = {}

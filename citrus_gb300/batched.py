@@ -102,7 +102,7 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
                     kernels.scattering_moments(fields.mu_s_l_coarse, p, "cell_major",
                                                out=T_all[j].view((N_sh,) + shape + (G, 4)))
             if fused:
-                kernels.source_expansion_first(Y, T_all, store.view(B, 8 * D8, J), means)
+                kernels.source_expansion_first(Y, T_all, store.view(B, 8 * D8, J), means, precision=precision)
                 del means
             else:
                 kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)

@@ -30,13 +30,17 @@ constexpr int kTcMaxK = 128;     // inner dimension, padded to a multiple of 16
 // kT = false: the MMA's A is the small matrix (rows of C), its B the 128-column tile, D = C[:, tile] in 128 x 128
 // accumulator columns. kT = true (M <= 64): the roles swap, D = C[:, tile]^T with the tile's 128 columns as the MMA
 // rows and the (M rounded up to 16) rows of C as its N: each accumulator lane is one column of C, stored directly.
+// F (the first-collision means of the source expansion, [M, J / 4] per batch, ldf floats per row and stride_f floats
+// between batches) is added to the first of every four columns of C when not null (with accumulate 0).
 template <bool kT>
 __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __restrict__ A, int64_t lda,
                                                              const float* __restrict__ B, int64_t ldb,
                                                              float* __restrict__ C, int64_t ldc, int M, int K,
                                                              int64_t J, int64_t stride_b, int64_t stride_c,
                                                              int accumulate, int64_t tiles_per_batch,
-                                                             int64_t num_tiles, uint32_t* __restrict__ error_word) {
+                                                             int64_t num_tiles, uint32_t* __restrict__ error_word,
+                                                             const float* __restrict__ F, int64_t ldf,
+                                                             int64_t stride_f) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int KS = (K + 15) / 16;            // K steps
   const uint32_t a_step = kTcM * 16 * 2;   // bytes of one K step of A (4 KB)
@@ -95,6 +99,7 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
     const float* Bz = B + bz * stride_b;
     float* Cz = C + bz * stride_c;
+    const float* Fz = F != nullptr ? F + bz * stride_f : nullptr;
     // B tile: column n0 + tid, split into the K-major layout
     const int64_t col = n0 + tid;
     const bool cvalid = col < J;
@@ -169,10 +174,14 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
           if (accumulate) {
 #pragma unroll
             for (int q = 0; q < 16; ++q) prev[q] = q < rows ? out[(int64_t)q * ldc] : 0.f;
+          } else if (Fz != nullptr && (col & 3) == 0) {  // the mean of the quadruple's first column
+#pragma unroll
+            for (int q = 0; q < 16; ++q) prev[q] = q < rows ? __ldg(Fz + (int64_t)(m0 + q) * ldf + (col >> 2)) : 0.f;
           }
+          const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
 #pragma unroll
           for (int q = 0; q < 16; ++q)
-            if (q < rows) out[(int64_t)q * ldc] = accumulate ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
+            if (q < rows) out[(int64_t)q * ldc] = add ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -207,10 +216,15 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
         if (accumulate) {  // every load issued before the first store
 #pragma unroll
           for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? out[(int64_t)rr * ldc] : 0.f;
+        } else if (Fz != nullptr && (col & 3) == 0) {  // the mean of the quadruple's first column
+          const float* f = Fz + (int64_t)(warp * 32) * ldf + (col >> 2);
+#pragma unroll
+          for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? __ldg(f + (int64_t)rr * ldf) : 0.f;
         }
+        const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
 #pragma unroll
         for (int rr = 0; rr < 32; ++rr)
-          if (rr < rows) out[(int64_t)rr * ldc] = accumulate ? prev[rr] + stage[rr][lane] : stage[rr][lane];
+          if (rr < rows) out[(int64_t)rr * ldc] = add ? prev[rr] + stage[rr][lane] : stage[rr][lane];
       }
       __syncwarp();
     }
@@ -227,15 +241,18 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
 
 using namespace citrus;
 
-extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
-                                          int64_t ldc, int64_t M, int64_t K, int64_t J, int64_t batch,
-                                          int64_t stride_b, int64_t stride_c, int32_t accumulate,
-                                          uint32_t* error_word, void* stream) {
-  CITRUS_REQUIRE(A && B && C, "citrus_small_k_gemm_bf16x3: null pointer argument");
+namespace citrus {
+namespace {
+
+int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                   int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
+                   int32_t accumulate, uint32_t* error_word, const float* F, int64_t ldf, int64_t stride_f,
+                   void* stream) {
+  CITRUS_REQUIRE(A && B && C, "%s: null pointer argument", name);
   CITRUS_REQUIRE(M >= 1 && M <= kTcM && K >= 1 && K <= kTcMaxK && J >= 0 && batch >= 1,
-                 "citrus_small_k_gemm_bf16x3: M %lld (<= %d) or K %lld (<= %d) out of range", (long long)M, kTcM,
-                 (long long)K, kTcMaxK);
-  CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "citrus_small_k_gemm_bf16x3: leading dimensions too small");
+                 "%s: M %lld (<= %d) or K %lld (<= %d) out of range", name, (long long)M, kTcM, (long long)K,
+                 kTcMaxK);
+  CITRUS_REQUIRE(lda >= K && ldb >= J && ldc >= J, "%s: leading dimensions too small", name);
   if (J == 0) return CITRUS_OK;
   const int KS = (int)((K + 15) / 16);
   // A and B operands (the epilogue's staging, 128 x 33 floats, reuses the B region), and at least 50 KB so that no
@@ -248,7 +265,7 @@ extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const flo
   // all of the unified L1 / shared-memory capacity as shared memory, so that four CTAs fit an SM
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_small_k_gemm_bf16x3: %s", cudaGetErrorString(e));
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "%s: %s", name, cudaGetErrorString(e));
   const int64_t tiles_per_batch = cdiv(J, kTcN);
   const int64_t num_tiles = tiles_per_batch * batch;
   // four CTAs per SM: the shared-memory floor keeps a fifth from becoming resident (tensor memory holds four
@@ -257,11 +274,34 @@ extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const flo
   if (swapped)
     gemm_tc_kernel<true><<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
         A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-        error_word);
+        error_word, F, ldf, stride_f);
   else
     gemm_tc_kernel<false><<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
         A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-        error_word);
+        error_word, F, ldf, stride_f);
   note_launches();
-  return launch_status("citrus_small_k_gemm_bf16x3");
+  return launch_status(name);
+}
+
+}  // namespace
+}  // namespace citrus
+
+extern "C" int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                                          int64_t ldc, int64_t M, int64_t K, int64_t J, int64_t batch,
+                                          int64_t stride_b, int64_t stride_c, int32_t accumulate,
+                                          uint32_t* error_word, void* stream) {
+  return launch_gemm_tc("citrus_small_k_gemm_bf16x3", A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b, stride_c,
+                        accumulate, error_word, nullptr, 0, 0, stream);
+}
+
+extern "C" int citrus_source_expansion_first_bf16x3(const float* A, int64_t lda, const float* B, int64_t ldb,
+                                                    float* C, int64_t ldc, const float* F, int64_t ldf, int64_t M,
+                                                    int64_t K, int64_t J, int64_t batch, int64_t stride_b,
+                                                    int64_t stride_c, int64_t stride_f, uint32_t* error_word,
+                                                    void* stream) {
+  CITRUS_REQUIRE(F != nullptr, "citrus_source_expansion_first_bf16x3: null means");
+  CITRUS_REQUIRE(J % 4 == 0 && ldf >= J / 4, "citrus_source_expansion_first_bf16x3: the columns must come in "
+                 "quadruples (J %lld) and ldf >= J / 4", (long long)J);
+  return launch_gemm_tc("citrus_source_expansion_first_bf16x3", A, lda, B, ldb, C, ldc, M, K, J, batch, stride_b,
+                        stride_c, 0, error_word, F, ldf, stride_f, stream);
 }

@@ -216,18 +216,24 @@ def sweep_chunk(ctx, store: Tensor, mu_cells: Tensor, c: Tensor, form: SweepForm
 # small-K products
 # =====================================================================================================================
 
-def source_expansion_first(A: Tensor, B: Tensor, C: Tensor, F: Tensor) -> Tensor:
+def source_expansion_first(A: Tensor, B: Tensor, C: Tensor, F: Tensor, precision: str = "fp32",
+                           error_word: Optional[Tensor] = None) -> Tensor:
     """``C[b] = A @ B[b]`` plus the LD quadruples ``(F[b], 0, 0, 0)``: the source of an accumulator sweep (the
     expansion ``Y @ T`` of ``transport_sweep.py:524`` added to first-collision moments of one point per cell, given by
-    their means) in one float32 pass that writes C without reading it; the same values as writing the quadruples into
-    C and accumulating ``small_k_gemm(A, B, C)`` over them.
+    their means) in one pass that writes C without reading it. In "fp32" the float32 CUDA-core product gives the same
+    values as writing the quadruples into C and accumulating ``small_k_gemm(A, B, C)`` over them; in "bf16x3" the
+    product runs on the tcgen05 tensor cores with the bfloat16 hi/lo split (``small_k_gemm``'s mixed precision) and
+    the means are added in its epilogue, 128 rows of A per launch (``error_word`` as in ``small_k_gemm``).
 
     Args:
         A: [M, K] float32 contiguous, K <= 64.
         B: [batch, K, J] float32 contiguous, J a multiple of 4.
         C: [batch, M, J] float32 contiguous output.
         F: [batch, M, J // 4] float32 contiguous means.
+        precision: "fp32" or "bf16x3".
     """
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
     for name, t in (("A", A), ("B", B), ("C", C), ("F", F)):
         _check_cuda_f32(name, t)
     if A.dim() != 2 or B.dim() != 3 or C.dim() != 3 or F.dim() != 3:
@@ -239,8 +245,17 @@ def source_expansion_first(A: Tensor, B: Tensor, C: Tensor, F: Tensor) -> Tensor
                          "do not chain")
     if J % 4 or K > 64:
         raise ValueError("J must be a multiple of 4 and K at most 64")
+    stream = _lib.stream_handle(C.device)
+    if precision == "bf16x3":
+        err = None if error_word is None else error_word.data_ptr()
+        for r0 in range(0, M, 128):
+            rows = min(128, M - r0)
+            _lib.call("citrus_source_expansion_first_bf16x3", A[r0:].data_ptr(), K, B.data_ptr(), J,
+                      C.data_ptr() + 4 * r0 * J, J, F.data_ptr() + 4 * r0 * (J // 4), J // 4, rows, K, J, batch,
+                      K * J, M * J, M * (J // 4), err, stream)
+        return C
     _lib.call("citrus_source_expansion_first", A.data_ptr(), K, B.data_ptr(), J, C.data_ptr(), J, F.data_ptr(),
-              J // 4, M, K, J, batch, K * J, M * J, M * (J // 4), _lib.stream_handle(C.device))
+              J // 4, M, K, J, batch, K * J, M * J, M * (J // 4), stream)
     return C
 
 

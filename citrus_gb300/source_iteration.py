@@ -63,10 +63,11 @@ def scatter_source_function(ctx: SweepContext, T: Tensor, precision: str = "fp32
 
     def with_means(direction_index: Tensor, means: Tensor, out: Tensor) -> Tensor:
         """``out`` = the same expansion plus the LD quadruples ``(means, 0, 0, 0)`` (means ``[Dsel, R, C, S, G]``)
-        in one float32 pass that writes ``out`` without reading it."""
+        in one pass that writes ``out`` without reading it (in the moment precision)."""
         Y_sel = ctx.Y.index_select(0, direction_index.to(ctx.Y.device)).contiguous()
         D = Y_sel.shape[0]
-        kernels.source_expansion_first(Y_sel, matrix.unsqueeze(0), out.view(1, D, -1), means.reshape(1, D, -1))
+        kernels.source_expansion_first(Y_sel, matrix.unsqueeze(0), out.view(1, D, -1), means.reshape(1, D, -1),
+                                       precision=precision)
         return out
 
     source.cell_major = True  # type: ignore[attr-defined]

@@ -42,12 +42,18 @@ def gather_signals(local: torch.Tensor, num_views: int, group=None) -> torch.Ten
 
 
 def sharded_scatter_stage(view_step: Callable[[int, float], torch.Tensor], angles: Sequence[float],
-                          group=None) -> torch.Tensor:
-    """Run ``view_step(view_index, angle) -> [Rd, Cd]`` on this rank's views and all-gather every view's signal."""
+                          image_shape: Sequence[int], device=None, group=None) -> torch.Tensor:
+    """Run ``view_step(view_index, angle) -> [Rd, Cd]`` on this rank's views and all-gather every view's signal.
+
+    ``image_shape`` is the panel's (Rd, Cd) and ``device`` the device of the signals (the collective's): a rank
+    that owns no view (more ranks than views) joins the all-gather with an empty block of that shape."""
     rank, world = dist.get_rank(group), dist.get_world_size(group)
     mine = owned_views(len(angles), rank, world)
-    local = torch.stack([view_step(v, float(angles[v])) for v in mine]) if mine else None
-    if local is None:
-        probe = view_step(0, float(angles[0]))  # shape only; a rank without views still joins the collective
-        local = probe.new_zeros((0,) + tuple(probe.shape))
+    Rd, Cd = (int(n) for n in image_shape)
+    if mine:
+        local = torch.stack([view_step(v, float(angles[v])) for v in mine])
+        if tuple(local.shape[1:]) != (Rd, Cd):
+            raise ValueError(f"view_step returned [{tuple(local.shape[1:])}], expected the panel's [{Rd}, {Cd}]")
+    else:
+        local = torch.zeros(0, Rd, Cd, device=device)
     return gather_signals(local, len(angles), group)

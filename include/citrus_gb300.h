@@ -145,6 +145,15 @@ int citrus_small_k_gemm_bf16x3(const float* A, int64_t lda, const float* B, int6
                                int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
                                int32_t accumulate, uint32_t* error_word, void* stream);
 
+/* The source of an accumulator sweep (citrus_source_expansion_first: C[b] = A B[b] + the quadruples (F[b], 0, 0, 0),
+ * C written without being read) on the tcgen05 tensor cores in the same bfloat16 hi/lo split, M <= 128, K <= 128, J a
+ * multiple of 4: the scattering-source expansion Y @ T of transport_sweep.py:524 and source_iteration.py:94-103 in
+ * the mixed precision, with the first-collision means added in its epilogue. error_word as above. */
+int citrus_source_expansion_first_bf16x3(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                                         int64_t ldc, const float* F, int64_t ldf, int64_t M, int64_t K, int64_t J,
+                                         int64_t batch, int64_t stride_b, int64_t stride_c, int64_t stride_f,
+                                         uint32_t* error_word, void* stream);
+
 /* ------------------------------------------------------------------------------------------------------------------
  * Spherical-harmonic moments of the scattering source,
  * T[g, n, k, x] = sum_g' transfer[g', g, l(n), x] phi[g', n, k, x], phi and T through element strides.

@@ -214,6 +214,31 @@ def test_bf16x3_tensor_core_gemm_error_against_float64(cuda_device, M, K, J, bat
     assert np.abs(C.cpu().numpy() - expected).max() / scale < 3e-5
 
 
+@pytest.mark.parametrize("M, K, J, batch", [(120, 36, 4096, 2), (240, 64, 1032, 1), (48, 16, 516, 3),
+                                            (5, 7, 64, 1), (128, 36, 2052, 1)])
+def test_tensor_core_source_expansion_with_means_against_float64(cuda_device, M, K, J, batch):
+    """The source of an accumulator sweep in the mixed precision (tcgen05, bfloat16 hi/lo split, the first-collision
+    means added in the epilogue): C = A B + (F, 0, 0, 0) against float64 within the split's ~1e-5 of the largest
+    term, over 128-row launches (M = 240), the swapped form (M <= 64) and partial column tiles."""
+    rng = np.random.default_rng(M + 3 * K + J)
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((batch, K, J))
+    F = rng.standard_normal((batch, M, J // 4))
+    expected = np.einsum("mk,bkj->bmj", A, B)
+    expected.reshape(batch, M, J // 4, 4)[..., 0] += F
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    C = torch.full((batch, M, J), float("nan"), device=cuda_device)   # written, never read
+    err = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+    kernels.source_expansion_first(dev(A), dev(B), C, dev(F), precision="bf16x3", error_word=err)
+    torch.cuda.synchronize()
+    assert int(err[0]) == 0
+    scale = np.abs(A).max() * np.abs(B).max() * K
+    assert np.abs(C.cpu().numpy() - expected).max() / scale < 3e-5
+    fp32 = torch.empty_like(C)
+    kernels.source_expansion_first(dev(A), dev(B), fp32, dev(F))
+    assert float((C - fp32).abs().max()) / scale < 3e-5
+
+
 def test_scattering_moments_match_reference_fixture(cuda_device):
     g = golden("scatter_moments_small")
     dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731

@@ -30,7 +30,7 @@ def _worker(rank: int, world: int, port: int, num_views: int, queue):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=30))
     angles = [0.1 * v for v in range(num_views)]
-    out = sharded_scatter_stage(_fake_view, angles)
+    out = sharded_scatter_stage(_fake_view, angles, (3, 4))
     queue.put((rank, out))
     dist.destroy_process_group()
 
@@ -40,11 +40,11 @@ def _failing_worker(rank: int, world: int, port: int, queue):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=3))
     angles = [0.0, 1.0, 2.0, 3.0]
-    sharded_scatter_stage(_fake_view, angles)  # step 1 succeeds on both ranks
+    sharded_scatter_stage(_fake_view, angles, (3, 4))  # step 1 succeeds on both ranks
     if rank == 1:
         os._exit(0)  # leaves between steps, nothing in flight
     try:
-        sharded_scatter_stage(_fake_view, angles)
+        sharded_scatter_stage(_fake_view, angles, (3, 4))
         queue.put((rank, "no error"))
     except Exception as e:  # noqa: BLE001
         queue.put((rank, f"error: {type(e).__name__}"))
