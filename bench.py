@@ -37,9 +37,12 @@ def _parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="step", choices=["step", "sweep", "learned"],
+    p.add_argument("--workload", default="step", choices=["step", "sweep", "learned", "sweep-form"],
                    help="step: the scatter step of every view (the headline); sweep: the accumulator sweep alone; "
-                        "learned: the learned proposal alone (training and converged steps)")
+                        "learned: the learned proposal alone (training and converged steps); sweep-form: one sweep "
+                        "form on a store of ones of --views views at --cells (profiling)")
+    p.add_argument("--sweep-form", default="1,0,1",
+                   help="sweep-form workload: thread form, tile edge (0: plane wavefront), directions per task")
     p.add_argument("--views", type=int, default=0, help="views per step (0: the workload's 60)")
     p.add_argument("--method", default="persistent", choices=["persistent", "planes"])
     p.add_argument("--dc", type=int, default=0, help="directions per octant per sweep chunk (0: all)")
@@ -272,6 +275,46 @@ def cpu_baseline_sweep(budget_s: float = 20.0) -> dict:
     return {"value": 8 * done * N * G / elapsed, "unit": "updates/s", "cores": os.cpu_count(), "kind": "port",
             "sample": f"{done} of 15 direction chunks (8 directions each) of one 64^3 x G=8 view sweep, float64 C "
                       f"restatement, OpenMP"}
+
+
+def run_sweep_form(args):
+    """One accumulator-sweep form (``kernels.SweepForm``) on the batched-views grid at --cells, a store of ones of
+    --views views: CUDA-event time per launch and the algorithmic HBM fraction (32 B per update). For profiling."""
+    import numpy as np
+    import torch
+
+    from citrus_gb300 import kernels
+    from citrus_gb300.quadrature import product_quadrature
+    from citrus_gb300.transport_sweep import make_sweep_context
+    from citrus_gb300.workloads import batched_views
+
+    device = torch.device("cuda")
+    w = batched_views(cells=args.cells)
+    ctx = make_sweep_context(w.grid, product_quadrature(w.num_polar, w.num_azimuthal), w.legendre_order, device)
+    G, N, D8 = w.library.num_groups, ctx.num_cells, ctx.directions_per_octant
+    mu = torch.as_tensor(np.einsum("mg,mijk->gijk", w.library.mu_t, w.rho).reshape(G, N).T.copy(),
+                         dtype=torch.float32, device=device)
+    V = max(1, args.views)
+    form = kernels.SweepForm(*(int(x) for x in args.sweep_form.split(",")))
+    store = torch.ones(V, 8, D8, N, 4 * G, device=device)
+    for _ in range(args.warmup):
+        kernels.sweep_chunk(ctx, store, mu, ctx.c, form)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        kernels.sweep_chunk(ctx, store, mu, ctx.c, form)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    algorithmic = 32 * V * 8 * D8 * N * G
+    peaks = _peaks()
+    print(json.dumps({"workload": f"sweep form {args.sweep_form} on {args.cells}^3 cells, G={G}, {8 * D8} directions, "
+                                  f"{V} views per launch", "ms_per_launch": ms, "ms_per_view": ms / V,
+                      "algorithmic_bytes": algorithmic, "frac": algorithmic / ms / 1e6 / peaks["hbm_gbs"]}),
+          flush=True)
 
 
 def run_reference(args):
@@ -537,9 +580,10 @@ def count_launches(fn) -> dict:
 
 
 def spr_error(w, solver, angles, device) -> dict:
-    """Scatter-to-primary ratio of the first step of a few views in the solver's moment precision against the float32
-    products: max over panel pixels of |SPR - SPR_fp32| / SPR_fp32, and the scatter signal's error relative to its
-    maximum."""
+    """Scatter-to-primary ratio after two steps of a few views (the second one warm: the scattering-source expansion,
+    the moment accumulation and the image product all run in the solver's moment precision) against the same steps
+    with float32 products: max over panel pixels of |SPR - SPR_fp32| / SPR_fp32, and the scatter signal's error
+    relative to its maximum."""
     import dataclasses
 
     import torch
@@ -555,13 +599,15 @@ def spr_error(w, solver, angles, device) -> dict:
     fields, ref_fields = solver.material_fields(rho, w.grid), ref_solver.material_fields(rho, w.grid)
     worst_spr, worst_signal = 0.0, 0.0
     for angle in angles:
-        s, p, _ = citrus_view_step(solver, CitrusState(), fields, float(angle), primary=True)
-        s_ref, _, _ = citrus_view_step(ref_solver, CitrusState(), ref_fields, float(angle), primary=False)
+        _, _, state = citrus_view_step(solver, CitrusState(), fields, float(angle), primary=False)
+        _, _, ref_state = citrus_view_step(ref_solver, CitrusState(), ref_fields, float(angle), primary=False)
+        s, p, _ = citrus_view_step(solver, state, fields, float(angle), primary=True)
+        s_ref, _, _ = citrus_view_step(ref_solver, ref_state, ref_fields, float(angle), primary=False)
         mask = p > 1e-3 * p.max()
         spr, spr_ref = s[mask] / p[mask], s_ref[mask] / p[mask]
         worst_spr = max(worst_spr, float(((spr - spr_ref).abs() / spr_ref.abs().clamp_min(1e-30)).max()))
         worst_signal = max(worst_signal, float((s - s_ref).abs().max() / s_ref.abs().max()))
-    return {"against": "the same step with float32 spherical-harmonic products", "views": len(angles),
+    return {"against": "the same two steps with float32 spherical-harmonic products", "views": len(angles),
             "spr_max_rel": worst_spr, "signal_max_rel": worst_signal}
 
 
@@ -930,5 +976,7 @@ if __name__ == "__main__":
         run_step(a)
     elif a.workload == "learned":
         run_learned(a)
+    elif a.workload == "sweep-form":
+        run_sweep_form(a)
     else:
         run_gb300(a)

@@ -1043,6 +1043,197 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_correction_kernel(
   beta[gv] = (float)b;
 }
 
+// ---- sampling correction, one thread per (point, direction) with all of its groups --------------------------------
+// The correction of fc_correction_kernel with the emission's thread layout: a block is 32 points (the lanes) by
+// kFcWarps warps; per batch of kFcDirBatch directions (in the order of their cosine with the block's first point, so
+// that a batch touches few table nodes) warp w takes the batch's directions w, w + kFcWarps, ... . A thread forms the
+// cosine and the table position of its (point, direction) once and the source of every group from float4 rows
+// (incoming groups at or above the outgoing one), adds the weighted source to its own partial sums I0, I1, I2 and
+// writes the source values to the cache; the warps' partial sums are then added in warp order, and the float64
+// factors formed as fc_correction_kernel forms them. The sums differ from fc_correction_kernel's at rounding level
+// (another order of the same terms).
+constexpr int kFcWarps = 8;
+constexpr int kFcDirBatch = 32;
+
+template <int kGP, int kMM, bool kVec>
+__global__ void __launch_bounds__(32 * kFcWarps, 2) fc_correction_warps_kernel(
+    FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, const float* __restrict__ weights, int K,
+    const float* __restrict__ moments /*[M, 2, G, G]*/, float* __restrict__ sums /*[5, G, V] or null*/,
+    float* __restrict__ scale, float* __restrict__ beta, float* __restrict__ cache /*[K, G, V] or null*/) {
+  constexpr int nthreads = 32 * kFcWarps;
+  extern __shared__ float4 s_dyn4[];
+  float* s_tab = reinterpret_cast<float*>(s_dyn4);
+  __shared__ float s_key[kMaxSorted];
+  __shared__ int s_order[kMaxSorted];
+  __shared__ float s_om[kFcDirBatch][3];
+  __shared__ float s_w[kFcDirBatch];
+  __shared__ int s_d[kFcDirBatch];
+  __shared__ int s_range[2][32];
+  __shared__ int s_window[2];
+  __shared__ float s_u0[3];
+  // after the direction loop the window's shared memory holds the warps' partial sums [kFcWarps][3][kGP][32]
+  static_assert(kFcWarps * 3 * kGP * 32 * 4 <= emission_window_bytes(kFcDirBatch), "partial sums exceed the window");
+  const int G = tb.G;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t v = (int64_t)blockIdx.x * 32 + lane;
+  const bool valid = v < in.V;
+  float rho[kMM], phi[kGP];
+  float ux = 0.f, uy = 0.f, uz = 0.f;
+#pragma unroll
+  for (int q = 0; q < kGP; ++q) phi[q] = 0.f;
+#pragma unroll
+  for (int m = 0; m < kMM; ++m) rho[m] = 0.f;
+  if (valid) {
+    int i, j, k;
+    point_rcs(v, pg, i, j, k);
+    primary_direction(__ldg(in.ax_x + j), __ldg(in.ax_y + i), __ldg(in.ax_z + k), in.r0x, in.r0y, in.r0z, ux, uy, uz);
+#pragma unroll
+    for (int m = 0; m < kMM; ++m)
+      if (m < tb.M) rho[m] = __ldg(in.rho + (int64_t)m * in.V + v);
+#pragma unroll
+    for (int q = 0; q < kGP; ++q)
+      if (q < G) phi[q] = __ldg(in.phi + (int64_t)q * in.V + v);
+  }
+  if (tid == 0) {
+    s_u0[0] = ux;
+    s_u0[1] = uy;
+    s_u0[2] = uz;
+  }
+  __syncthreads();
+  const bool sorted = K <= kMaxSorted;
+  if (sorted) {
+    for (int d = tid; d < K; d += nthreads)
+      s_key[d] = s_u0[0] * __ldg(omegas + 3 * d) + s_u0[1] * __ldg(omegas + 3 * d + 1) +
+                 s_u0[2] * __ldg(omegas + 3 * d + 2);
+    __syncthreads();
+    for (int d = tid; d < K; d += nthreads) {
+      const float key = s_key[d];
+      int rank = 0;
+      for (int q = 0; q < K; ++q) {
+        const float other = s_key[q];
+        rank += (other < key) || (other == key && q < d);
+      }
+      s_order[rank] = d;
+    }
+    __syncthreads();
+  }
+  float I0[kGP], I1[kGP], I2[kGP];
+#pragma unroll
+  for (int q = 0; q < kGP; ++q) I0[q] = I1[q] = I2[q] = 0.f;
+  const int RS = window_row_stride(G);
+  for (int b0 = 0; b0 < K; b0 += kFcDirBatch) {
+    const int nb = min(kFcDirBatch, K - b0);
+    if (tid < nb) {
+      const int d = sorted ? s_order[b0 + tid] : b0 + tid;
+      s_d[tid] = d;
+      s_om[tid][0] = __ldg(omegas + 3 * d);
+      s_om[tid][1] = __ldg(omegas + 3 * d + 1);
+      s_om[tid][2] = __ldg(omegas + 3 * d + 2);
+      s_w[tid] = __ldg(weights + d);
+    }
+    __syncthreads();
+    stage_window(tb, valid, ux, uy, uz, s_om, nb, warp, kFcWarps, warp, kFcWarps, tid, nthreads, s_range, s_window,
+                 s_tab, emission_window_bytes(kFcDirBatch));
+    const int win_lo = s_window[0];
+    if (valid) {
+      for (int i = warp; i < nb; i += kFcWarps) {
+        const float cosine = ux * s_om[i][0] + uy * s_om[i][1] + uz * s_om[i][2];
+        int i0;
+        float w;
+        table_position(tb, cosine, i0, w);
+        float S[kGP];
+#pragma unroll
+        for (int q = 0; q < kGP; ++q) S[q] = 0.f;
+        const bool win = win_lo >= 0;
+#pragma unroll
+        for (int m = 0; m < kMM; ++m) {
+          const float r = rho[m];
+          if (m >= tb.M || r == 0.f) continue;
+          const float* row0 = win ? s_tab + ((i0 - win_lo) * tb.M + m) * RS : tb.t + ((int64_t)m * tb.N + i0) * G * G;
+          const float* row1 = row0 + (win ? tb.M * RS : G * G);
+#pragma unroll
+          for (int g = 0; g < kGP; ++g) {
+            if (g >= G) break;
+            float a0, a1;
+            if (win) {
+              a0 = dot_lower<kGP, kVec, true>(row0 + g * G, phi, g);
+              a1 = dot_lower<kGP, kVec, true>(row1 + g * G, phi, g);
+            } else {
+              a0 = dot_lower<kGP, kVec, false>(row0 + g * G, phi, g);
+              a1 = dot_lower<kGP, kVec, false>(row1 + g * G, phi, g);
+            }
+            S[g] = fmaf(r, a0 + (a1 - a0) * w, S[g]);
+          }
+        }
+        const float wt = s_w[i], c2 = cosine * cosine;
+        const int64_t d = s_d[i];
+#pragma unroll
+        for (int g = 0; g < kGP; ++g) {
+          if (g >= G) break;
+          const float ws = S[g] * wt;
+          I0[g] += ws;
+          I1[g] += ws * cosine;
+          I2[g] += ws * c2;
+          if (cache != nullptr) cache[(d * G + g) * in.V + v] = S[g];
+        }
+      }
+    }
+    __syncthreads();  // the batch's directions and window are replaced next
+  }
+  float* s_part = s_tab;  // free: the last batch's barrier above ended every read of the window
+#pragma unroll
+  for (int q = 0; q < kGP; ++q) {
+    s_part[((warp * 3 + 0) * kGP + q) * 32 + lane] = I0[q];
+    s_part[((warp * 3 + 1) * kGP + q) * 32 + lane] = I1[q];
+    s_part[((warp * 3 + 2) * kGP + q) * 32 + lane] = I2[q];
+  }
+  __syncthreads();
+  // warp g forms the factors of group g of its lane's point (every warp holds the point's densities and fluence)
+  for (int g = warp; g < G && g < kGP; g += kFcWarps) {
+    if (!valid) break;
+    float i0s = 0.f, i1s = 0.f, i2s = 0.f;
+#pragma unroll
+    for (int q = 0; q < kFcWarps; ++q) {
+      i0s += s_part[((q * 3 + 0) * kGP + g) * 32 + lane];
+      i1s += s_part[((q * 3 + 1) * kGP + g) * 32 + lane];
+      i2s += s_part[((q * 3 + 2) * kGP + g) * 32 + lane];
+    }
+    // exact l = 0, 1 moments of the source (downscatter rows of the moment table)
+    float E0 = 0.f, E1 = 0.f;
+    for (int m = 0; m < tb.M && m < kMM; ++m) {
+      const float* r0 = moments + (((int64_t)m * 2 + 0) * G + g) * G;
+      const float* r1 = moments + (((int64_t)m * 2 + 1) * G + g) * G;
+      float a0 = 0.f, a1 = 0.f;
+      for (int gi = 0; gi <= g; ++gi) {
+        a0 = fmaf(__ldg(r0 + gi), phi[gi], a0);
+        a1 = fmaf(__ldg(r1 + gi), phi[gi], a1);
+      }
+      E0 = fmaf(rho[m], a0, E0);
+      E1 = fmaf(rho[m], a1, E1);
+    }
+    const int64_t gv = (int64_t)g * in.V + v;
+    if (sums) {
+      const int64_t GV = (int64_t)G * in.V;
+      sums[gv] = i0s;
+      sums[GV + gv] = i1s;
+      sums[2 * GV + gv] = i2s;
+      sums[3 * GV + gv] = E0;
+      sums[4 * GV + gv] = E1;
+    }
+    // factors in float64 (uncollided.py:611-636)
+    const double i0d = i0s, i1d = i1s, i2d = i2s, e0 = E0, e1 = E1;
+    const bool pos = e0 > 0;
+    const double c = pos ? e1 / e0 : 0.0;
+    const double den = i2d - c * i1d;
+    const bool ok = pos && fabs(den) > 1e-12 * fabs(i0d);
+    double b = ok ? (c * i0d - i1d) / den : 0.0;
+    b = fmin(fmax(b, -1.0), 1.0);
+    const double d0 = i0d + b * i1d;
+    scale[gv] = (float)(d0 > 0 ? e0 / d0 : 1.0);
+    beta[gv] = (float)b;
+  }
+}
+
 // ---- LD moments of the corrected source from the kept source values ---------------------------------------------
 // A block is 32 cells by the G groups by kFcBatch directions of the chunk: S_FC read from cache [K, G, V] at the
 // chunk direction's cache_index, corrected (scale (1 + beta cos)) and restricted to the cell's LD moments; the
@@ -1320,11 +1511,47 @@ int launch_fc_correction_m(dim3 grid, int G, cudaStream_t s, const FCInputs& in,
   return CITRUS_OK;
 }
 
-// materials held in registers: two (the common water and bone case) or up to eight
+template <int kGP, int kMM, bool kVec>
+int launch_fc_correction_warps(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                               const float* omegas, const float* weights, int K, const float* moments, float* sums,
+                               float* scale, float* beta, float* cache) {
+  constexpr int bytes = emission_window_bytes(kFcDirBatch);
+  cudaError_t e = cudaFuncSetAttribute(fc_correction_warps_kernel<kGP, kMM, kVec>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "first-collision window: %s", cudaGetErrorString(e));
+  fc_correction_warps_kernel<kGP, kMM, kVec><<<grid, 32 * kFcWarps, bytes, s>>>(in, tb, pg, omegas, weights, K,
+                                                                                moments, sums, scale, beta, cache);
+  note_launches();
+  return CITRUS_OK;
+}
+
+// CITRUS_FC_KERNEL=groups selects the group-lane correction kernel (fc_correction_kernel); read at every call
+inline bool fc_by_groups() {
+  const char* v = getenv("CITRUS_FC_KERNEL");
+  return v != nullptr && v[0] == 'g';
+}
+
+// materials held in registers: two (the common water and bone case) or up to eight; G <= 16 takes the (point,
+// direction) kernel
 template <int kGP>
 int launch_fc_correction(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
                          const float* omegas, const float* weights, int K, const float* moments, float* sums,
                          float* scale, float* beta, float* cache) {
+  if constexpr (kGP <= 16) {
+    if (!fc_by_groups()) {
+      const bool vec = kGP >= 4 && G % 4 == 0 && ((uintptr_t)tb.t % 16) == 0;
+      constexpr bool kCanVec = kGP >= 4;
+      if (tb.M <= 2)
+        return vec ? launch_fc_correction_warps<kGP, 2, kCanVec>(grid, s, in, tb, pg, omegas, weights, K, moments,
+                                                                 sums, scale, beta, cache)
+                   : launch_fc_correction_warps<kGP, 2, false>(grid, s, in, tb, pg, omegas, weights, K, moments,
+                                                               sums, scale, beta, cache);
+      return vec ? launch_fc_correction_warps<kGP, kMaxM, kCanVec>(grid, s, in, tb, pg, omegas, weights, K, moments,
+                                                                   sums, scale, beta, cache)
+                 : launch_fc_correction_warps<kGP, kMaxM, false>(grid, s, in, tb, pg, omegas, weights, K, moments,
+                                                                 sums, scale, beta, cache);
+    }
+  }
   if (tb.M <= 2)
     return launch_fc_correction_m<kGP, 2>(grid, G, s, in, tb, pg, omegas, weights, K, moments, sums, scale, beta,
                                           cache);

@@ -17,6 +17,7 @@
 //     bounded by a wall-clock limit, after which the CTA records the error and leaves.
 //   * The four warps read their 32 lanes of the accumulator (tcgen05.ld 32x32b) and store or add the rows of C.
 #include <algorithm>
+#include <stdlib.h>
 
 #include "tcgen05.cuh"
 
@@ -236,6 +237,330 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
 }
 
+// ---- the warp-specialised form ------------------------------------------------------------------------------------
+// The same product as gemm_tc_kernel with its stages overlapped, one CTA per SM walking its tiles in order:
+//
+//   * loader (one thread of warp 13): the K rows of a 128-column tile of B are contiguous 512-byte runs, each fetched
+//     by one bulk asynchronous copy (cp.async.bulk, completing on the stage's mbarrier with its byte count) into a
+//     ring of kWsRaw float32 stages;
+//   * converters (warps 8 to 11): thread t splits column t of a raw stage into the bfloat16 high and low operand
+//     tiles in the K-major core-matrix layout (kWsOps stages), then frees the raw stage;
+//   * MMA issuer (one thread of warp 12): 3 x (K / 16) tcgen05.mma per tile into one of two float32 accumulators in
+//     tensor memory, committed to the operand stage (freed once read) and to the accumulator (full);
+//   * epilogue (warps 0 to 7): warp w reads accumulator lanes 32 (w % 4) .. + 31 and half of the columns, and writes
+//     (or adds to) C, so that the stores of one tile overlap the loads, splits and MMAs of the next.
+//
+// The MMAs run in gemm_tc_kernel's order and the epilogue adds in its order: the two forms give the same bits. Every
+// mbarrier wait is bounded by kTcTimeoutNs; a role whose wait runs out records the error and stops, the others then
+// stop at their own bounded waits, the issuer waits (bounded) for its last MMAs, and the CTA frees its tensor memory.
+constexpr int kWsRaw = 3;                 // float32 stages of B
+constexpr int kWsOps = 2;                 // bf16 hi/lo operand stages
+constexpr int kWsThreads = 14 * 32;       // 8 epilogue, 4 converter, 1 MMA and 1 loader warps
+constexpr int kWsEpilogueWarps = 8;
+constexpr int kWsConverterWarp0 = 8;
+constexpr int kWsMmaWarp = 12;
+constexpr int kWsLoaderWarp = 13;
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+template <bool kT>
+__global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __restrict__ A, int64_t lda,
+                                                                const float* __restrict__ B, int64_t ldb,
+                                                                float* __restrict__ C, int64_t ldc, int M, int K,
+                                                                int64_t J, int64_t stride_b, int64_t stride_c,
+                                                                int accumulate, int64_t tiles_per_batch,
+                                                                int64_t num_tiles, uint32_t* __restrict__ error_word,
+                                                                const float* __restrict__ F, int64_t ldf,
+                                                                int64_t stride_f) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int KS = (K + 15) / 16;
+  const uint32_t a_step = kTcM * 16 * 2, b_step = kTcN * 16 * 2;
+  const uint32_t raw_bytes = (uint32_t)K * kTcN * 4;
+  const uint32_t raw_stride = (raw_bytes + 1023u) & ~1023u;
+  uint8_t* a_hi = smem;
+  uint8_t* a_lo = a_hi + KS * a_step;
+  uint8_t* ops = a_lo + KS * a_step;                                 // kWsOps x (hi, lo)
+  const uint32_t op_bytes = 2u * KS * b_step;
+  float* raw = reinterpret_cast<float*>(ops + kWsOps * op_bytes);   // kWsRaw x [K][128]
+  float (*stage)[33] = reinterpret_cast<float (*)[33]>(reinterpret_cast<uint8_t*>(raw) + kWsRaw * raw_stride);
+  __shared__ __align__(8) uint64_t bar[2 * kWsRaw + 2 * kWsOps + 5];
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int abort_flag;
+  uint64_t* raw_full = bar;
+  uint64_t* raw_empty = bar + kWsRaw;
+  uint64_t* op_full = bar + 2 * kWsRaw;
+  uint64_t* op_empty = op_full + kWsOps;
+  uint64_t* acc_full = op_empty + kWsOps;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* mma_done = acc_empty + 2;  // the issuer's last commit: its MMAs are complete before the CTA frees TMEM
+  const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+
+  // A, split once (threads 0..127), rows r of every K step, 8 columns at a time
+  for (int r = tid; r < kTcM; r += kWsThreads)
+    for (int s = 0; s < KS; ++s)
+      for (int k8 = 0; k8 < 16; k8 += 8) {
+        float x[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int k = s * 16 + k8 + q;
+          x[q] = (r < M && k < K) ? A[(int64_t)r * lda + k] : 0.f;
+        }
+        uint4 hi, lo;
+        split_pair(x[0], x[1], hi.x, lo.x);
+        split_pair(x[2], x[3], hi.y, lo.y);
+        split_pair(x[4], x[5], hi.z, lo.z);
+        split_pair(x[6], x[7], hi.w, lo.w);
+        const uint32_t off = s * a_step + core_offset(r, k8);
+        *reinterpret_cast<uint4*>(a_hi + off) = hi;
+        *reinterpret_cast<uint4*>(a_lo + off) = lo;
+      }
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int i = 0; i < kWsRaw; ++i) {
+      mbar_init(smem_u32(raw_full + i), 1);
+      mbar_init(smem_u32(raw_empty + i), 128);
+    }
+    for (int i = 0; i < kWsOps; ++i) {
+      mbar_init(smem_u32(op_full + i), 128);
+      mbar_init(smem_u32(op_empty + i), 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(smem_u32(acc_full + i), 1);
+      mbar_init(smem_u32(acc_empty + i), 32 * kWsEpilogueWarps);
+    }
+    mbar_init(smem_u32(mma_done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  constexpr uint32_t kCols = kT ? 64u : (uint32_t)kTcN;  // one accumulator; two are allocated
+  const int n_t = ((M + 15) / 16) * 16;
+  const uint32_t idesc = kT ? idesc_bf16(n_t) : idesc_bf16(kTcN);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(2 * kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the split A, visible to the tensor cores
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const int64_t my_tiles = num_tiles > (int64_t)blockIdx.x ? (num_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const auto fail = [&]() {
+    if (error_word != nullptr) atomicExch(error_word, 1u);
+    abort_flag = 1;
+  };
+
+  if (warp == kWsLoaderWarp) {
+    if (lane == 0) {
+      for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
+        const int st = (int)(i % kWsRaw);
+        if (!mbar_wait(smem_u32(raw_empty + st), (uint32_t)((i / kWsRaw) & 1) ^ 1u, global_timer_ns())) {
+          fail();
+          break;
+        }
+        const int64_t tile = blockIdx.x + i * gridDim.x;
+        const int64_t bz = tile / tiles_per_batch;
+        const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
+        const uint32_t bytes = (uint32_t)((J - n0 < kTcN ? J - n0 : (int64_t)kTcN) * 4);
+        const uint32_t mb = smem_u32(raw_full + st);
+        mbar_expect_tx(mb, bytes * (uint32_t)K);
+        const float* src = B + bz * stride_b + n0;
+        const uint32_t dst = smem_u32(reinterpret_cast<uint8_t*>(raw) + st * raw_stride);
+        for (int k = 0; k < K; ++k) bulk_copy_g2s(dst + (uint32_t)k * kTcN * 4, src + (int64_t)k * ldb, bytes, mb);
+      }
+    }
+  } else if (warp >= kWsConverterWarp0 && warp < kWsConverterWarp0 + 4) {
+    const int t = tid - kWsConverterWarp0 * 32;  // the tile column this thread splits
+    for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
+      const int st = (int)(i % kWsRaw), op = (int)(i % kWsOps);
+      if (!mbar_wait(smem_u32(raw_full + st), (uint32_t)((i / kWsRaw) & 1), global_timer_ns()) ||
+          !mbar_wait(smem_u32(op_empty + op), (uint32_t)((i / kWsOps) & 1) ^ 1u, global_timer_ns())) {
+        fail();
+        break;
+      }
+      const float* col = reinterpret_cast<const float*>(reinterpret_cast<uint8_t*>(raw) + st * raw_stride) + t;
+      uint8_t* o_hi = ops + op * op_bytes;
+      uint8_t* o_lo = o_hi + KS * b_step;
+      for (int s = 0; s < KS; ++s)
+        for (int k8 = 0; k8 < 16; k8 += 8) {
+          float x[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int k = s * 16 + k8 + q;
+            x[q] = k < K ? col[k * kTcN] : 0.f;
+          }
+          uint4 hi, lo;
+          split_pair(x[0], x[1], hi.x, lo.x);
+          split_pair(x[2], x[3], hi.y, lo.y);
+          split_pair(x[4], x[5], hi.z, lo.z);
+          split_pair(x[6], x[7], hi.w, lo.w);
+          const uint32_t off = s * b_step + core_offset(t, k8);
+          *reinterpret_cast<uint4*>(o_hi + off) = hi;
+          *reinterpret_cast<uint4*>(o_lo + off) = lo;
+        }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the operands, visible to the tensor cores
+      mbar_arrive(smem_u32(raw_empty + st));
+      mbar_arrive(smem_u32(op_full + op));
+    }
+  } else if (warp == kWsMmaWarp) {
+    if (lane == 0) {
+      for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
+        const int op = (int)(i % kWsOps), ac = (int)(i & 1);
+        if (!mbar_wait(smem_u32(op_full + op), (uint32_t)((i / kWsOps) & 1), global_timer_ns()) ||
+            !mbar_wait(smem_u32(acc_empty + ac), (uint32_t)((i >> 1) & 1) ^ 1u, global_timer_ns())) {
+          fail();
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)ac * kCols;
+        uint8_t* o_hi = ops + op * op_bytes;
+        uint8_t* o_lo = o_hi + KS * b_step;
+        for (int s = 0; s < KS; ++s) {
+          const uint64_t ah = smem_desc(smem_u32(a_hi + s * a_step), 128, 256);
+          const uint64_t al = smem_desc(smem_u32(a_lo + s * a_step), 128, 256);
+          const uint64_t bh = smem_desc(smem_u32(o_hi + s * b_step), 128, 256);
+          const uint64_t bl = smem_desc(smem_u32(o_lo + s * b_step), 128, 256);
+          if (kT) {
+            mma_bf16(d, bh, ah, idesc, s > 0 ? 1u : 0u);
+            mma_bf16(d, bh, al, idesc, 1u);
+            mma_bf16(d, bl, ah, idesc, 1u);
+          } else {
+            mma_bf16(d, ah, bh, idesc, s > 0 ? 1u : 0u);
+            mma_bf16(d, ah, bl, idesc, 1u);
+            mma_bf16(d, al, bh, idesc, 1u);
+          }
+        }
+        tc_commit(smem_u32(op_empty + op));
+        tc_commit(smem_u32(acc_full + ac));
+      }
+      tc_commit(smem_u32(mma_done));  // tracks every MMA issued above
+      if (!mbar_wait(smem_u32(mma_done), 0u, global_timer_ns())) fail();
+    }
+  } else {  // epilogue warps 0 .. 7
+    const int quarter = warp % 4, half = warp / 4;
+    for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
+      const int ac = (int)(i & 1);
+      if (!mbar_wait(smem_u32(acc_full + ac), (uint32_t)((i >> 1) & 1), global_timer_ns())) {
+        fail();
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int64_t tile = blockIdx.x + i * gridDim.x;
+      const int64_t bz = tile / tiles_per_batch;
+      const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
+      float* Cz = C + bz * stride_c;
+      const float* Fz = F != nullptr ? F + bz * stride_f : nullptr;
+      const uint32_t taddr = tmem + (uint32_t)ac * kCols + ((uint32_t)(quarter * 32) << 16);
+      if (kT) {
+        // accumulator lane 32 quarter + lane is column n0 + 32 quarter + lane of C; its columns are the rows of C,
+        // split in 16-row steps between the two halves of the epilogue warps
+        const int64_t col = n0 + quarter * 32 + lane;
+        for (int m0 = half * 16; m0 < n_t; m0 += 32) {
+          uint32_t r[16];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+              "%14, %15}, [%16];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+              : "r"(taddr + (uint32_t)m0)
+              : "memory");
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (col < J) {
+            const int rows = min(16, M - m0);
+            float* out = Cz + (int64_t)m0 * ldc + col;
+            float prev[16];
+            const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
+            if (accumulate) {
+#pragma unroll
+              for (int q = 0; q < 16; ++q) prev[q] = q < rows ? out[(int64_t)q * ldc] : 0.f;
+            } else if (add) {
+#pragma unroll
+              for (int q = 0; q < 16; ++q) prev[q] = q < rows ? __ldg(Fz + (int64_t)(m0 + q) * ldf + (col >> 2)) : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+              if (q < rows) out[(int64_t)q * ldc] = add ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
+          }
+        }
+      } else {
+        // rows 32 quarter .. + 31 of C, columns 64 half .. + 63 of the tile, 32 at a time turned through shared
+        // memory so that every store covers 32 consecutive columns of one row
+        float (*stg)[33] = stage + warp * 32;
+        const int rows = min(32, M - quarter * 32);
+        for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+          uint32_t r[32];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+              "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+                "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                "=r"(r[30]), "=r"(r[31])
+              : "r"(taddr + (uint32_t)c0)
+              : "memory");
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 32; ++q) stg[lane][q] = __uint_as_float(r[q]);
+          __syncwarp();
+          const int64_t col = n0 + c0 + lane;
+          if (col < J && rows > 0) {
+            float* out = Cz + (int64_t)(quarter * 32) * ldc + col;
+            float prev[32];
+            const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
+            if (accumulate) {
+#pragma unroll
+              for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? out[(int64_t)rr * ldc] : 0.f;
+            } else if (add) {
+              const float* f = Fz + (int64_t)(quarter * 32) * ldf + (col >> 2);
+#pragma unroll
+              for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? __ldg(f + (int64_t)rr * ldf) : 0.f;
+            }
+#pragma unroll
+            for (int rr = 0; rr < 32; ++rr)
+              if (rr < rows) out[(int64_t)rr * ldc] = add ? prev[rr] + stg[rr][lane] : stg[rr][lane];
+          }
+          __syncwarp();
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(smem_u32(acc_empty + ac));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kCols) : "memory");
+}
+
+// shared memory of the warp-specialised form: A hi/lo, kWsOps operand stages, kWsRaw float32 stages (1 KB aligned),
+// the epilogue's transposes
+size_t ws_smem_bytes(int K) {
+  const size_t KS = (size_t)(K + 15) / 16;
+  const size_t raw_stride = (((size_t)K * kTcN * 4) + 1023) & ~(size_t)1023;
+  return KS * 2 * kTcM * 16 * 2 + kWsOps * KS * 2 * kTcN * 16 * 2 + kWsRaw * raw_stride +
+         (size_t)kWsEpilogueWarps * 32 * 33 * 4;
+}
+
 }  // namespace
 }  // namespace citrus
 
@@ -243,6 +568,13 @@ using namespace citrus;
 
 namespace citrus {
 namespace {
+
+// CITRUS_TC_FORM=single keeps the single-stage kernel (measurements, and the check that both forms agree); read at
+// every call
+inline bool ws_disabled() {
+  const char* v = getenv("CITRUS_TC_FORM");
+  return v != nullptr && v[0] == 's';
+}
 
 int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
                    int64_t M, int64_t K, int64_t J, int64_t batch, int64_t stride_b, int64_t stride_c,
@@ -260,6 +592,27 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
   const size_t b_bytes = std::max<size_t>((size_t)KS * 2 * kTcN * 16 * 2, (size_t)kTcM * 33 * sizeof(float));
   const size_t smem = std::max<size_t>((size_t)KS * 2 * kTcM * 16 * 2 + b_bytes, 50 * 1024);
   const bool swapped = M <= 64;
+  // the warp-specialised form when B's rows are runs of 16-byte units (bulk copies) and its stages fit one CTA
+  const size_t ws_smem = ws_smem_bytes((int)K);
+  if (J % 4 == 0 && ldb % 4 == 0 && stride_b % 4 == 0 && ((uintptr_t)B % 16) == 0 && ws_smem <= 227 * 1024 &&
+      !ws_disabled()) {
+    const void* wfn = swapped ? (const void*)gemm_ws_kernel<true> : (const void*)gemm_ws_kernel<false>;
+    cudaError_t we = cudaFuncSetAttribute(wfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem);
+    if (we != cudaSuccess) return set_error(CITRUS_ECUDA, "%s: %s", name, cudaGetErrorString(we));
+    const int64_t tiles_per_batch = cdiv(J, kTcN);
+    const int64_t num_tiles = tiles_per_batch * batch;
+    const int64_t grid = std::min<int64_t>(num_tiles, (int64_t)num_sms());
+    if (swapped)
+      gemm_ws_kernel<true><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
+          A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
+          error_word, F, ldf, stride_f);
+    else
+      gemm_ws_kernel<false><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
+          A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
+          error_word, F, ldf, stride_f);
+    note_launches();
+    return launch_status(name);
+  }
   const void* fn = swapped ? (const void*)gemm_tc_kernel<true> : (const void*)gemm_tc_kernel<false>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   // all of the unified L1 / shared-memory capacity as shared memory, so that four CTAs fit an SM

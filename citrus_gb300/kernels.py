@@ -267,10 +267,10 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, prec
     """``C (=|+=) A @ B`` for A [M, K] and B, C [.., K or M, J] row-major 2-D (or batched 3-D) views.
 
     B and C may be strided views whose last axis is contiguous. ``precision`` "fp32" multiplies in float32 on the CUDA
-    cores; "bf16x3" allows the tcgen05 tensor-core product, which splits both operands into bfloat16 high and low
+    cores; "bf16x3" runs the tcgen05 tensor-core product, which splits both operands into bfloat16 high and low
     parts and accumulates A_hi B_hi + A_hi B_lo + A_lo B_hi in float32 (``error_word``, an int32 device tensor,
-    becomes non-zero if a wait for the tensor cores ran out), where the autotuner finds it faster than the float32
-    forms for the shape; ``tensor_cores_only`` takes it whatever the timing (for checks of that kernel).
+    becomes non-zero if a wait for the tensor cores ran out); ``tensor_cores_only`` only checks that the precision
+    asks for it.
     """
     if precision not in PRECISIONS:
         raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
@@ -305,20 +305,15 @@ def small_k_gemm(A: Tensor, B: Tensor, C: Tensor, accumulate: bool = False, prec
                           B[:, k0:].data_ptr(), B.stride(1), out.data_ptr() + 4 * r0 * ld_out, ld_out, rows, inner,
                           J, batch, sb, s_out, int(bool(accumulate) or k0 > 0), err, stream)
 
-    if tensor_cores_only:
-        if precision != "bf16x3":
-            raise ValueError("tensor_cores_only needs precision='bf16x3'")
+    if tensor_cores_only and precision != "bf16x3":
+        raise ValueError("tensor_cores_only needs precision='bf16x3'")
+    if precision == "bf16x3":   # the mixed precision: every spherical-harmonic product on the tensor cores
         tensor_cores(C, C.stride(1), sc)
         return C
     from .autotune import small_k_gemm_config
 
-    # the kernel: the autotuner's choice for this shape among the float32 forms, and in "bf16x3" also the
-    # tensor-core product (a float32 form is at least as accurate, so it may serve the bf16x3 precision too)
-    variant, tile = small_k_gemm_config(A, B, C, M, K, J, batch, sb, sc, accumulate,
-                                        tensor_cores=tensor_cores if precision == "bf16x3" else None)
-    if variant == 3:
-        tensor_cores(C, C.stride(1), sc)
-        return C
+    # the kernel: the autotuner's choice for this shape among the float32 forms
+    variant, tile = small_k_gemm_config(A, B, C, M, K, J, batch, sb, sc, accumulate)
     _lib.call("citrus_small_k_gemm_config", A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(1), C.data_ptr(),
               C.stride(1), M, K, J, batch, sb, sc, int(bool(accumulate)), int(variant), int(tile), stream)
     return C

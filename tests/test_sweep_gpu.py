@@ -239,6 +239,46 @@ def test_tensor_core_source_expansion_with_means_against_float64(cuda_device, M,
     assert float((C - fp32).abs().max()) / scale < 3e-5
 
 
+@pytest.mark.parametrize("M, K, J, batch, accumulate, means", [(120, 36, 4096, 2, False, True),
+                                                               (36, 64, 2052, 1, True, False),
+                                                               (64, 36, 1024, 3, False, False),
+                                                               (100, 48, 132, 1, False, True),
+                                                               (17, 20, 260, 2, True, False)])
+def test_warp_specialised_tensor_core_product_equals_single_stage(cuda_device, monkeypatch, M, K, J, batch,
+                                                                  accumulate, means):
+    """The warp-specialised tcgen05 product (bulk-copy loader, converters, MMA issuer, double-buffered accumulators,
+    epilogue warps) performs the single-stage kernel's MMAs in the same order and the same epilogue: the same bits,
+    in both roles (M <= 64 swapped), with accumulation, with the first-collision means and a partial last tile."""
+    rng = np.random.default_rng(M * 5 + K + J)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    A, B = dev(rng.standard_normal((M, K))), dev(rng.standard_normal((batch, K, J)))
+    C0, F = dev(rng.standard_normal((batch, M, J))), dev(rng.standard_normal((batch, M, J // 4)))
+    results = []
+    for form in ("ws", "single"):
+        if form == "single":
+            monkeypatch.setenv("CITRUS_TC_FORM", "single")
+        else:
+            monkeypatch.delenv("CITRUS_TC_FORM", raising=False)
+        C = C0.clone()
+        err = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+        if means:
+            kernels.source_expansion_first(A, B, C, F, precision="bf16x3", error_word=err)
+        else:
+            kernels.small_k_gemm(A, B, C, accumulate=accumulate, precision="bf16x3", error_word=err,
+                                 tensor_cores_only=True)
+        torch.cuda.synchronize()
+        assert int(err[0]) == 0
+        results.append(C)
+    assert torch.equal(results[0], results[1])
+    expected = np.einsum("mk,bkj->bmj", A.double().cpu().numpy(), B.double().cpu().numpy())
+    if accumulate:
+        expected += C0.double().cpu().numpy()
+    if means:
+        expected.reshape(batch, M, J // 4, 4)[..., 0] += F.double().cpu().numpy()
+    scale = float(A.abs().max() * B.abs().max()) * K
+    assert np.abs(results[0].double().cpu().numpy() - expected).max() / scale < 3e-5
+
+
 def test_scattering_moments_match_reference_fixture(cuda_device):
     g = golden("scatter_moments_small")
     dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731

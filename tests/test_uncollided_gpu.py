@@ -86,3 +86,37 @@ def test_config_library_first_collision_on_refined_grid(cuda_device):
     ref_rows = physics.first_collision_moments(library, rho, phi, grid, geo, 1.1, q.omega[rows.cpu().numpy()], scale,
                                                beta, 3)
     assert rel_err(cached, ref_rows) < 2e-5
+
+
+@pytest.mark.parametrize("groups", [8, 3, 12])
+def test_direction_warp_correction_equals_group_lane_correction(cuda_device, monkeypatch, groups):
+    """The (point, direction) form of the sampling correction against the group-lane form
+    (CITRUS_FC_KERNEL=groups): the kept source values bit for bit (same terms in the same order), the quadrature sums
+    and the factors to rounding (the sums over the directions run in another order)."""
+    from citrus_gb300.cross_sections import BONE, WATER, spectral_library
+    from citrus_gb300.geometry import ConeGeometry, Grid
+    from citrus_gb300.quadrature import product_quadrature
+    from citrus_gb300.workloads import bremsstrahlung_spectrum
+    library = spectral_library(np.linspace(120.0, 30.0, groups + 1), bremsstrahlung_spectrum(seed=0), [WATER, BONE],
+                               1, num_eta=201, fine_per_group=2)
+    grid = Grid((9, 7, 11), 0.6)
+    geo = ConeGeometry(100.0, 150.0, 64, 64, 0.4, 0.4)
+    rng = np.random.default_rng(groups)
+    rho = rng.random((2, *grid.shape)) * np.array([1.0, 0.0])[:, None, None, None]
+    rho[1, 2:5, 1:4, 3:8] = 1.85
+    q = product_quadrature(6, 20)
+    dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
+    phi = dev(rng.random((groups, *grid.shape)) * 1e-3 + 1e-4)
+    out = []
+    for form in ("warps", "groups"):
+        if form == "groups":
+            monkeypatch.setenv("CITRUS_FC_KERNEL", "groups")
+        else:
+            monkeypatch.delenv("CITRUS_FC_KERNEL", raising=False)
+        out.append(first_collision_sampling_correction(library, dev(rho), phi, grid, geo, 0.9, dev(q.omega),
+                                                       dev(q.weight), keep_sums=True, keep_cache=True))
+    a, b = out
+    assert torch.equal(a.cache, b.cache)
+    assert rel_err(a.sums, b.sums) < 1e-6
+    assert rel_err(a.scale, b.scale) < 1e-5
+    assert float((a.beta - b.beta).abs().max()) < 1e-5
