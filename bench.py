@@ -37,10 +37,12 @@ def _parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="step", choices=["step", "sweep", "learned", "sweep-form"],
+    p.add_argument("--workload", default="step", choices=["step", "sweep", "learned", "sweep-form", "mixed"],
                    help="step: the scatter step of every view (the headline); sweep: the accumulator sweep alone; "
                         "learned: the learned proposal alone (training and converged steps); sweep-form: one sweep "
-                        "form on a store of ones of --views views at --cells (profiling)")
+                        "form on a store of ones of --views views at --cells (profiling); mixed: --views views "
+                        "(default 4) of the 128x128x96, G=16, P7, 240-direction workload in float32 and bf16x3 "
+                        "products")
     p.add_argument("--sweep-form", default="1,0,1",
                    help="sweep-form workload: thread form, tile edge (0: plane wavefront), directions per task")
     p.add_argument("--views", type=int, default=0, help="views per step (0: the workload's 60)")
@@ -317,6 +319,79 @@ def run_sweep_form(args):
           flush=True)
 
 
+def run_mixed(args):
+    """The mixed-precision workload (``workloads.mixed_precision_views``: 128 x 128 x 96 cells of 0.25 cm, G = 16,
+    P7, 240 directions, curved 512 x 384 panel) on ``--views`` views (default 4) of the 90: two outer iterations (a
+    cold start and a warm step) of ``batched_view_steps`` (eager) with float32 and with bf16x3 tensor-core products.
+    Reports ms per view of the warm step (CUDA events) in each precision and, per view, the bf16x3 step's error
+    against the float32 step: collided scalar flux (cells above 1e-3 of the maximum), scatter image and SPR (pixels
+    whose primary exceeds 1e-3 of its maximum), element-wise maxima."""
+    import dataclasses
+
+    # one view's accumulator is 25.8 GB here: growable segments keep the allocator's free blocks reusable
+    os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "expandable_segments:True")
+    import torch
+
+    from citrus_gb300.batched import batched_view_steps, direction_chunk
+    from citrus_gb300.citrus_step import CitrusState
+    from citrus_gb300.responses import ideal_counting_response, no_grid
+    from citrus_gb300.scatter_solver import ScatterSolver, SolverConfig
+    from citrus_gb300.workloads import mixed_precision_views
+
+    device = torch.device("cuda")
+    cells = (args.cells * 2, args.cells * 2, args.cells * 3 // 2) if args.cells != 64 else (128, 128, 96)
+    w = mixed_precision_views(cells=cells)
+    V = args.views if args.views > 0 else 4
+    angles = [float(a) for a in w.angles()[:: max(1, w.num_views // V)][:V]]
+    base = SolverConfig(num_groups=w.library.num_groups, legendre_order=w.legendre_order, num_polar=w.num_polar,
+                        num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
+                        quadrature_point_spacing_cm=0.5, cone_num_polar=w.cone_num_polar,
+                        cone_num_azimuthal=w.cone_num_azimuthal)
+    rho = torch.as_tensor(w.rho, dtype=torch.float32, device=device)
+    results = {}
+    for precision in ("fp32", "bf16x3"):
+        solver = ScatterSolver(w.library, dataclasses.replace(base, moment_precision=precision), w.geometry,
+                               detector=ideal_counting_response(), grid_response=no_grid(), device=device)
+        fields = solver.material_fields(rho, w.grid)
+        _, _, states = batched_view_steps(solver, [CitrusState() for _ in angles], fields, angles, batch=0)  # cold
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        signals, _, states = batched_view_steps(solver, states, fields, angles, batch=0)                 # warm
+        e1.record()
+        e1.synchronize()
+        primaries = torch.stack([solver.primary(solver.material_fields(rho, w.grid), a)["signal"] for a in angles])
+        results[precision] = {"ms_per_view": e0.elapsed_time(e1) / V, "signals": signals.clone(),
+                              "scalar": [s.collided_moments[:, 0, 0].clone() for s in states],
+                              "primary": primaries}
+        ctx = solver.sweep_context(solver.material_fields(rho, w.grid).grid_coarse)
+        results[precision]["chunk"] = direction_chunk(ctx.num_cells, w.library.num_groups, ctx.directions_per_octant)
+        del states, signals, fields
+        torch.cuda.empty_cache()
+    a, b = results["fp32"], results["bf16x3"]
+    per_view = []
+    for v in range(V):
+        p = a["primary"][v]
+        mask = p > 1e-3 * p.max()
+        s32, s16 = a["signals"][v], b["signals"][v]
+        f32, f16 = a["scalar"][v], b["scalar"][v]
+        cells_mask = f32.abs() > 1e-3 * f32.abs().max()
+        per_view.append({
+            "collided_scalar_max_rel": float(((f16 - f32).abs()[cells_mask] / f32.abs()[cells_mask]).max()),
+            "scatter_max_rel": float(((s16 - s32).abs()[mask] / s32.abs()[mask]).max()),
+            "spr_max_rel": float(((s16[mask] / p[mask]) / (s32[mask] / p[mask]) - 1).abs().max())})
+    N = w.grid.num_voxels
+    print(json.dumps({
+        "workload": f"mixed_precision_views: {cells[0]}x{cells[1]}x{cells[2]} cells x {w.transport_cell_cm:g} cm, "
+                    f"G=16 (20-140 keV), P7 (64 moments), 240 sweep directions (10x24), cone 16x32, curved 512x384 "
+                    f"panel, {V} of the 90 views",
+        "directions_per_octant_per_chunk": results["fp32"]["chunk"],
+        "ms_per_view_warm_step": {"fp32": a["ms_per_view"], "bf16x3": b["ms_per_view"]},
+        "updates_per_view": 240 * N * 16,
+        "bf16x3_against_fp32_per_view": per_view,
+        "note": "the float64 comparison of the mixed precision is the single-view workload's (the reference's own "
+                "float64 run; mixed_precision_bf16x3.float64_reference_error of the step bench)"}), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -483,11 +558,12 @@ def sweep_form_name(solver, w, rho_dev) -> str:
     """The accumulator sweep's form the autotuner chose for this grid (plane wavefront or tiled schedule)."""
     from citrus_gb300.batched import sweep_launch_config
     fields = solver.material_fields(rho_dev, w.grid)
-    _, form = sweep_launch_config(solver, fields, 60, 0)
+    _, form, dc = sweep_launch_config(solver, fields, 60, 0)
+    chunks = f", {dc} directions per octant per chunk"
     if form.tile > 0:
         return (f"tiled: {form.tile}^3-cell tiles, {form.dirs_per_block} directions per task, thread form "
-                f"{form.thread_form}")
-    return f"plane wavefront, thread form {form.thread_form}"
+                f"{form.thread_form}{chunks}")
+    return f"plane wavefront, thread form {form.thread_form}{chunks}"
 
 
 def step_workload_name(cells: int, views: int, batch: int = 1, graph: bool = False) -> str:
@@ -611,6 +687,50 @@ def spr_error(w, solver, angles, device) -> dict:
             "spr_max_rel": worst_spr, "signal_max_rel": worst_signal}
 
 
+def float64_reference_error(device) -> dict:
+    """The single-view workload (32^3 cells of 0.5 cm, one 60 keV group, P3, 48 sweep directions, cone 16 x 32, flat
+    64 x 64 panel) stepped twice by ``citrus_view_step`` in float32 and in bf16x3 products, against the reference's
+    own float64 run of the same two steps (the committed fixture ``tests/golden/config1_view.npz``, made by
+    ``tests/golden/make_golden.py``): the worst per-pixel relative error of the scatter image and of the SPR over the
+    pixels whose primary exceeds 1e-3 of its maximum, and of the collided scalar flux over the cells above 1e-3 of its
+    maximum."""
+    import numpy as np
+    import torch
+
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step
+    from citrus_gb300.responses import ideal_counting_response, no_grid
+    from citrus_gb300.scatter_solver import ScatterSolver, SolverConfig
+    from citrus_gb300.workloads import single_view
+
+    with np.load(ROOT / "tests" / "golden" / "config1_view.npz") as d:
+        ref = {k: d[k] for k in d.files}
+    w = single_view()
+    out = {"workload": "single_view: 32^3 x 0.5 cm, G=1 (60 keV), P3, 48 sweep directions, cone 16x32, flat 64x64",
+           "against": "the reference's float64 CPU run of the same two citrus_view_step calls"}
+    for precision in ("fp32", "bf16x3"):
+        config = SolverConfig(num_groups=1, legendre_order=w.legendre_order, num_polar=w.num_polar,
+                              num_azimuthal=w.num_azimuthal, transport_cell_cm=w.transport_cell_cm,
+                              quadrature_point_spacing_cm=0.5, cone_num_polar=w.cone_num_polar,
+                              cone_num_azimuthal=w.cone_num_azimuthal, direction_chunk=6, moment_precision=precision)
+        solver = ScatterSolver(w.library, config, w.geometry, detector=ideal_counting_response(),
+                               grid_response=no_grid(), device=device)
+        fields = solver.material_fields(torch.as_tensor(w.rho, dtype=torch.float32, device=device), w.grid)
+        state = CitrusState()
+        for _ in range(2):
+            scatter, primary, state = citrus_view_step(solver, state, fields, 0.0, primary=True)
+        s = scatter.double().cpu().numpy()
+        p = primary.double().cpu().numpy()
+        phi = state.collided_moments[:, 0, 0].double().cpu().numpy()
+        s_ref, p_ref, phi_ref = ref["step2_scatter"], ref["primary"], ref["step2_scalar"][:, 0].astype(np.float64)
+        mask = p_ref > 1e-3 * p_ref.max()
+        cells = np.abs(phi_ref) > 1e-3 * np.abs(phi_ref).max()
+        out[precision] = {
+            "scatter_max_rel": float((np.abs(s - s_ref)[mask] / np.abs(s_ref)[mask]).max()),
+            "spr_max_rel": float(np.abs((s[mask] / p[mask]) / (s_ref[mask] / p_ref[mask]) - 1).max()),
+            "collided_scalar_max_rel": float((np.abs(phi - phi_ref)[cells] / np.abs(phi_ref)[cells]).max())}
+    return out
+
+
 def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
     """The same step with the spherical-harmonic products on the tcgen05 tensor cores (bfloat16 hi/lo split, float32
     accumulation): ms/view over ``args.steps`` steps after one warm-up step, and its scatter-to-primary error against
@@ -655,7 +775,8 @@ def mixed_precision_step(args, w, solver, angles, rho_dev, device) -> dict:
     del graphed, states
     torch.cuda.empty_cache()
     return {"value": value, "unit": "ms/view", "steps": args.steps, "cuda_graph": bool(args.graph),
-            "spr_error": spr_error(w, mixed, angles[:2], device)}
+            "spr_error": spr_error(w, mixed, angles[:2], device),
+            "float64_reference_error": float64_reference_error(device)}
 
 
 def plain_single_view_step(w, solver, angles, rho_dev, device) -> dict:
@@ -777,7 +898,117 @@ def learned_measurement(args, device) -> dict:
         "converged_to_spr_error_estimate": 0.005,
         "plain": summary(results["plain"]),
         "learned": summary(results["learned"]),
+        "combined_outer_iterations": combined_measurement(args, device, w, solver, proposal),
     }
+
+
+def combined_measurement(args, device, w, solver, proposal, views: int = 12, seed: int = 5100,
+                         tolerance: float = 0.005, max_iterations: int = 16) -> dict:
+    """The scatter step of every view of one phantom (``views`` views over 360 degrees) iterated over outer iterations
+    until every view's scatter-to-primary ratio is within ``tolerance`` of its converged value (a Neumann series to
+    1e-6, computed before the timing), in two forms: the plain one, ``citrus_view_step`` per view from a cold start,
+    eager, float32 products; and the combined one, every view seeded with the learned proposal (one sweep of the
+    first-collision source and the network, timed) and stepped by ``GraphedOuterIteration`` (the views' sweeps
+    batched per persistent launch, the outer iteration replayed from a CUDA graph) with the bf16x3 tensor-core
+    products. CUDA-event times of every step; the error is checked between steps, outside the timed spans."""
+    import dataclasses
+
+    import numpy as np
+    import torch
+
+    from citrus_gb300 import learned
+    from citrus_gb300.batched import GraphedOuterIteration, resolve_batch
+    from citrus_gb300.citrus_step import CitrusState, citrus_view_step, project_scatter
+    from citrus_gb300.scatter_solver import ScatterSolver
+    from citrus_gb300.workloads import ellipsoid_phantom
+
+    angles = [2 * math.pi * v / views for v in range(views)]
+    rho = torch.as_tensor(ellipsoid_phantom(w.grid, seed), dtype=torch.float32, device=device)
+    fields = solver.material_fields(rho, w.grid)
+    refs, masks = [], []
+    for a in angles:
+        _, total = learned.collided_orders(solver, fields, a, tolerance=1e-6)
+        phi_uc = solver.uncollided_fluence(fields, a)
+        cone = solver.cone_quadrature(w.grid, a)
+        refs.append(project_scatter(solver, None, w.grid, a, phi_uc, total, fields, cone, signal_only=True)["signal"])
+        p = solver.primary(fields, a)["signal"]
+        masks.append(p > 1e-3 * p.max())
+
+    def worst(signals) -> float:
+        return max(float(((s - r)[m].abs() / r[m].abs()).max()) for s, r, m in zip(signals, refs, masks))
+
+    stream = torch.cuda.current_stream(device)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    # plain: cold start, one eager citrus_view_step per view and outer iteration
+    states = [CitrusState() for _ in angles]
+    plain_ms, plain_errors = [], []
+
+    def plain_step():
+        out = []
+        for v, a in enumerate(angles):
+            s, _, states[v] = citrus_view_step(solver, states[v], fields, a, primary=False)
+            out.append(s)
+        return out
+
+    plain_step()                                       # warm-up of tables and contexts, not counted
+    states = [CitrusState() for _ in angles]
+    for _ in range(max_iterations):
+        signals, ms = timed(plain_step)
+        plain_ms.append(ms)
+        plain_errors.append(worst(signals))
+        if plain_errors[-1] <= tolerance:
+            break
+    # combined: learned seeds, batched sweeps, graph replays, bf16x3 products
+    mixed = ScatterSolver(solver.library, dataclasses.replace(solver.config, moment_precision="bf16x3"),
+                          solver.geometry, detector=solver.detector, grid_response=solver.grid_response, device=device)
+    mixed.direction_context_cache_size = max(mixed.direction_context_cache_size, views)
+    mfields = mixed.material_fields(rho, w.grid)
+    batch = resolve_batch(mixed, mfields, views, 0)
+
+    def seeds():
+        out = []
+        for a in angles:
+            _, first = learned.first_collided(mixed, mfields, a)
+            out.append(proposal.propose(mfields.rho_coarse, first))
+        return out
+
+    seeds()                                            # warm-up, not counted
+    graphed = GraphedOuterIteration(mixed, w.grid, angles, batch=batch)
+    accumulators, seed_ms = timed(seeds)
+    graphed.seed(rho, accumulators)
+    combined_ms, combined_errors = [], []
+    for _ in range(max_iterations):
+        (signals, _), ms = timed(lambda: graphed.step(rho))
+        combined_ms.append(ms)
+        combined_errors.append(worst(list(signals)))
+        if combined_errors[-1] <= tolerance:
+            break
+    plain_total, combined_total = sum(plain_ms), seed_ms + sum(combined_ms)
+    # the first combined iteration also records the CUDA graph (once per run of outer iterations); its replays are
+    # what every further outer iteration costs
+    replay = statistics.mean(combined_ms[1:]) if len(combined_ms) > 1 else combined_ms[0]
+    steady_total = seed_ms + replay * len(combined_ms)
+    return {"views": views, "phantom_seed": seed, "spr_tolerance": tolerance,
+            "plain": {"outer_iterations": len(plain_ms), "ms_per_view": plain_total / views,
+                      "ms_per_view_per_iteration": [round(m / views, 3) for m in plain_ms],
+                      "spr_err_per_iteration": [round(e, 5) for e in plain_errors]},
+            "combined": {"outer_iterations": len(combined_ms), "ms_per_view": combined_total / views,
+                         "seed_ms_per_view": seed_ms / views, "views_per_sweep_launch": batch,
+                         "ms_per_view_per_iteration": [round(m / views, 3) for m in combined_ms],
+                         "spr_err_per_iteration": [round(e, 5) for e in combined_errors],
+                         "form": "learned seeds + GraphedOuterIteration (batched sweeps, CUDA graph) + bf16x3"},
+            "speedup": plain_total / combined_total,
+            "speedup_graph_recorded": plain_total / steady_total,
+            "note": "the combined form's first iteration includes recording the CUDA graph; speedup_graph_recorded "
+                    "counts every iteration at the replay time (the graph is recorded once per run)"}
 
 
 def run_step(args):
@@ -978,5 +1209,7 @@ if __name__ == "__main__":
         run_learned(a)
     elif a.workload == "sweep-form":
         run_sweep_form(a)
+    elif a.workload == "mixed":
+        run_mixed(a)
     else:
         run_gb300(a)

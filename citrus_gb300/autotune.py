@@ -167,14 +167,17 @@ UNROLL_CANDIDATES = (1, 3, 5, 2, 4)
 TILED_CANDIDATES = ((2, 4, 5), (2, 8, 3), (1, 4, 5), (1, 8, 3))
 
 
-def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2, 0, 1)) -> tuple:
-    """(views per sweep launch, ``kernels.SweepForm``) for ``views`` views on this grid: the per-view time of the sweep
-    on a store of ones of 1, 2, 4 or 8 views (those whose store takes at most a quarter of the free device memory) in
-    each form (the plane wavefront in each lanes-per-thread form, the tiled schedule per tile edge, thread form and
-    directions per task); the first (fewest views) within 3 % of the fastest."""
+def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2, 0, 1), dc: int = 0) -> tuple:
+    """(views per sweep launch, ``kernels.SweepForm``) for ``views`` views on this grid and chunks of ``dc``
+    directions per octant (0: all): the per-view time of the sweep on a store of ones of 1, 2, 4 or 8 views (those
+    whose store takes at most a quarter of the free device memory) in each form (the plane wavefront in each
+    lanes-per-thread form, the tiled schedule per tile edge, thread form and directions per task); the first (fewest
+    views) within 3 % of the fastest."""
     from . import kernels
 
-    N, D8, Q = ctx.num_cells, ctx.directions_per_octant, 4 * num_groups
+    N, Q = ctx.num_cells, 4 * num_groups
+    D8 = ctx.directions_per_octant if dc <= 0 else min(int(dc), ctx.directions_per_octant)
+    c_chunk = ctx.c if D8 == ctx.directions_per_octant else ctx.c[:, :D8].contiguous()
     device = ctx.device
     # "form" names the forms' meaning: entries timed before the tiled schedule existed are not reused
     key = Autotuner.key("sweep", device, N=N, D8=D8, G=num_groups, shape="x".join(map(str, ctx.shape)),
@@ -194,7 +197,7 @@ def sweep_config(ctx, mu_cells, num_groups: int, views: int, default=(4, 2, 0, 1
                 stores.clear()
                 torch.cuda.empty_cache()
                 stores[b] = torch.ones(b, 8, D8, N, Q, device=device)  # non-zero moments, as in a real step
-            kernels.sweep_chunk(ctx, stores[b], mu_cells, ctx.c, kernels.SweepForm(u, t, d))
+            kernels.sweep_chunk(ctx, stores[b], mu_cells, c_chunk, kernels.SweepForm(u, t, d))
 
         tuner().choose(key, candidates, run, list(default), slack=0.03, per_unit=lambda c: float(c[0]))
         stores.clear()

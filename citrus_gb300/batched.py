@@ -33,16 +33,44 @@ def _check_states(states: Sequence[CitrusState], angles: Sequence[float]) -> Non
             raise ValueError(f"state {v} belongs to angle {state.angle}, got {angle}")
 
 
+SWEEP_STORE_BUDGET_BYTES = 40 * 2 ** 30   # the store of one view's chunk: 8 x directions x N x 4G floats
+
+
+def direction_chunk(num_cells: int, num_groups: int, directions_per_octant: int,
+                    budget: Optional[int] = None) -> int:
+    """Directions per octant swept together in one view's chunk: all of them when the store fits ``budget``
+    (``SWEEP_STORE_BUDGET_BYTES`` when None) and the sweep's 32-bit lane positions (8 N dc G float4 below 2^31),
+    else as many as do."""
+    budget = SWEEP_STORE_BUDGET_BYTES if budget is None else int(budget)
+    per_direction = 8 * num_cells * 4 * num_groups * 4
+    lanes = (2 ** 31 - 1) // (8 * num_cells * num_groups)
+    return max(1, min(directions_per_octant, budget // per_direction, lanes))
+
+
 def sweep_launch_config(solver: ScatterSolver, fields: MaterialFields, views: int, batch: int) -> tuple:
-    """(views per sweep launch, form of the sweep threads): the autotuner's choice for this grid, with ``batch``
-    views when it is positive."""
+    """(views per sweep launch, form of the sweep threads, directions per octant per chunk): the autotuner's choice
+    for this grid and chunk, with ``batch`` views when it is positive."""
     from .autotune import sweep_config
 
     ctx = solver.sweep_context(fields.grid_coarse)
     G = solver.num_groups
+    dc = direction_chunk(ctx.num_cells, G, ctx.directions_per_octant)
     mu_cells = fields.mu_t_coarse.reshape(G, ctx.num_cells).t().contiguous()
-    tuned_views, form = sweep_config(ctx, mu_cells, G, views)
-    return (min(int(batch), max(1, views)) if batch > 0 else tuned_views), form
+    tuned_views, form = sweep_config(ctx, mu_cells, G, views, dc=dc)
+    chosen = min(int(batch), max(1, views)) if batch > 0 else tuned_views
+    return min(chosen, views_that_fit(ctx, G, dc, solver.device)), form, dc
+
+
+def views_that_fit(ctx, num_groups: int, dc: int, device, share: float = 0.6) -> int:
+    """Views per sweep launch whose working set fits ``share`` of the free device memory: per view its scattering
+    moments and new accumulator (N_sh x N x 4G floats each), the chunk's store (8 x dc x N x 4G) and first-collision
+    means (8 x dc x N x G)."""
+    N, J = ctx.num_cells, ctx.num_cells * 4 * num_groups
+    per_view = 4 * (2 * ctx.num_moments * J + 8 * dc * J + 8 * dc * N * num_groups)
+    if torch.cuda.is_current_stream_capturing():
+        return 1 << 30
+    free, _ = torch.cuda.mem_get_info(device)
+    return max(1, int(share * free) // per_view)
 
 
 def resolve_batch(solver: ScatterSolver, fields: MaterialFields, views: int, batch: int) -> int:
@@ -65,16 +93,12 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
     Rd, Cd = solver.geometry.image_shape
     V = len(angles)
     primaries = torch.empty(V, Rd, Cd, device=device) if primary else None
-    index = ctx.direction_indices(0, D8)
-    Y = ctx.Y.index_select(0, index).contiguous()                  # [8 D8, N_sh]
-    Yw_t = ctx.Y_weighted.index_select(0, index).t().contiguous()  # [N_sh, 8 D8]
     mu_cells = fields.mu_t_coarse.reshape(G, N).t().contiguous()
     syncs, norms, accumulators = [], [], []
-    batch, form = sweep_launch_config(solver, fields, V, batch)
+    batch, form, dc = sweep_launch_config(solver, fields, V, batch)
     for b0 in range(0, V, batch):
         views = list(range(b0, min(V, b0 + batch)))
         B = len(views)
-        store = torch.empty(B, 8, D8, N, Q, device=device)
         phi_uc, firsts = [], []
         for v in views:
             uc = solver.uncollided_fluence(fields, float(angles[v]))
@@ -88,29 +112,37 @@ def _launch_views(solver: ScatterSolver, states: Sequence[CitrusState], fields: 
         # source expansion's output pass instead of being written into the store and read back by it (in either
         # moment precision: the single pass moves less than half the bytes of the two, whichever form the product takes)
         fused = warm and N_sh <= 64 and all(f.means is not None for f in firsts)
-        if fused:
-            means = torch.empty(B, 8 * D8, N * G, device=device)
-            for j, first in enumerate(firsts):
-                first.means(index, out=means[j])
-        else:
-            for j, first in enumerate(firsts):
-                first(index, out=store[j].view((8 * D8,) + shape + (G, 4)))
-        if warm:
+        T_all = None
+        if warm:  # the scattering moments of every view, formed before any chunk overwrites an accumulator
             T_all = torch.zeros(B, N_sh, J, device=device)
             for j, p in enumerate(previous):
                 if p is not None:
                     kernels.scattering_moments(fields.mu_s_l_coarse, p, "cell_major",
                                                out=T_all[j].view((N_sh,) + shape + (G, 4)))
+        moments = torch.empty(B, N_sh, J, device=device) if store_out is None else store_out[b0:b0 + B]
+        for d0 in range(0, D8, dc):   # direction chunks (one, unless a view's store outgrows the budget)
+            d1 = min(D8, d0 + dc)
+            k = d1 - d0
+            index = ctx.direction_indices(d0, d1)
+            Y = ctx.Y.index_select(0, index).contiguous()                  # [8 k, N_sh]
+            Yw_t = ctx.Y_weighted.index_select(0, index).t().contiguous()  # [N_sh, 8 k]
+            store = torch.empty(B, 8, k, N, Q, device=device)
             if fused:
-                kernels.source_expansion_first(Y, T_all, store.view(B, 8 * D8, J), means, precision=precision)
+                means = torch.empty(B, 8 * k, N * G, device=device)
+                for j, first in enumerate(firsts):
+                    first.means(index, out=means[j])
+                kernels.source_expansion_first(Y, T_all, store.view(B, 8 * k, J), means, precision=precision)
                 del means
             else:
-                kernels.small_k_gemm(Y, T_all, store.view(B, 8 * D8, J), accumulate=True, precision=precision)
-            del T_all
-        syncs.append(kernels.sweep_chunk(ctx, store, mu_cells, ctx.c, form))
-        moments = torch.empty(B, N_sh, J, device=device) if store_out is None else store_out[b0:b0 + B]
-        kernels.small_k_gemm(Yw_t, store.view(B, 8 * D8, J), moments, precision=precision)
-        del store
+                for j, first in enumerate(firsts):
+                    first(index, out=store[j].view((8 * k,) + shape + (G, 4)))
+                if warm:
+                    kernels.small_k_gemm(Y, T_all, store.view(B, 8 * k, J), accumulate=True, precision=precision)
+            c = ctx.c if k == D8 else ctx.c[:, d0:d1].contiguous()
+            syncs.append(kernels.sweep_chunk(ctx, store, mu_cells, c, form))
+            kernels.small_k_gemm(Yw_t, store.view(B, 8 * k, J), moments, accumulate=d0 > 0, precision=precision)
+            del store
+        del T_all
         for j, v in enumerate(views):
             new = moments[j].view(N_sh, N, G, 4).permute(2, 0, 3, 1).reshape(G, N_sh, 4, *shape)
             signals[v] = project_scatter(solver, None, fields.grid_fine, float(angles[v]), phi_uc[j], new, fields,
@@ -220,6 +252,25 @@ class GraphedOuterIteration:
                 self.solver, warm, self.fields, self.angles, self.batch, False, self.store, self.signals, cones)
         torch.cuda.current_stream(self.solver.device).wait_stream(stream)
         self._cones = cones
+
+    def seed(self, rho: Tensor, accumulators: Sequence[Tensor]) -> None:
+        """Start every view from a given accumulator ``[G, N_sh, 4, Rc, Cc, Sc]`` (the learned proposal, say)
+        instead of the cold start: the accumulators are copied into the store, and the next ``step`` runs warm (and
+        records the graph)."""
+        if len(accumulators) != len(self.angles):
+            raise ValueError(f"need one accumulator per view ({len(self.angles)}), got {len(accumulators)}")
+        self._refresh_fields(rho)
+        ctx = self.solver.sweep_context(self.fields.grid_coarse)
+        G, N_sh, shape = self.solver.num_groups, ctx.num_moments, ctx.shape
+        if self.store is None:
+            self.store = torch.empty(len(self.angles), N_sh, ctx.num_cells * 4 * G, device=self.solver.device)
+        self.graph = None
+        for v, acc in enumerate(accumulators):
+            view = self.store[v].view(N_sh, *shape, G, 4).permute(4, 0, 5, 1, 2, 3)   # [G, N_sh, 4, Rc, Cc, Sc]
+            if tuple(acc.shape) != tuple(view.shape):
+                raise ValueError(f"accumulator {v} must be {tuple(view.shape)}, got {tuple(acc.shape)}")
+            view.copy_(acc)
+            self.states[v] = CitrusState(angle=self.angles[v], collided_moments=view)
 
     def step(self, rho: Tensor) -> tuple:
         """One outer iteration's scatter step of every view from fine densities ``rho`` [M, R, C, S]."""

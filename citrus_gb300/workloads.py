@@ -8,6 +8,8 @@ from seeds):
   source at 100 cm, a flat 64 x 64 panel of 0.4 cm pixels at 150 cm, P3 and a 4 x 12 = 48 direction sweep set.
   Water 0.206 and bone 0.315 cm^2/g total; scattering albedo 0.923 (water) and 0.611 (bone), split 85 % Compton
   (Klein-Nishina shape) and 15 % Rayleigh (Thomson shape).
+* ``mixed_precision_views``: 128 x 128 x 96 cells of 0.25 cm, 16 groups over 20-140 keV, P7, 240 directions, 90
+  views, a curved 512 x 384 panel (the configuration the mixed-precision products are measured on).
 * ``batched_views``: 64^3 cells of 0.4 cm, an axial water cylinder of radius 11 cm with two bone cylinders of radius
   1.5 cm at seeded offsets, 8 groups from 30 to 120 keV of a seeded bremsstrahlung-like spectrum (Kramers shape with
   2 mm of aluminium), power-law photoelectric plus Klein-Nishina Compton and Rayleigh cross sections, P5, a 6 x 20 =
@@ -113,6 +115,21 @@ def batched_views(seed: int = 1, cells: int = 64) -> Workload:
     geo = ConeGeometry(100.0, 150.0, 192, 256, 0.16, 0.16, use_curved_detector=True)
     return Workload("batched_views", grid, geo, cylinder_phantom(grid, 11.0, 1.5, seed), lib, 6, 20, 5, 25.6 / cells,
                     60)
+
+
+def mixed_precision_views(seed: int = 1, cells: tuple = (128, 128, 96)) -> Workload:
+    """The mixed-precision workload: 128 x 128 x 96 cells of 0.25 cm (32 x 32 x 24 cm), the water cylinder of radius
+    11 cm with two bone cylinders, 16 groups from 140 to 20 keV of a 140 kVp spectrum, P7 (64 moments), a 10 x 24 =
+    240 direction sweep set (8 x 30 would leave the octants unbalanced), cone 16 x 32, 90 views over 360 degrees and a
+    curved 512-channel x 384-row panel of 0.08 cm pixels. Smaller ``cells`` give the same scene on coarser cells."""
+    rows, cols, slices = (int(c) for c in cells)
+    cell = 32.0 / rows
+    grid = Grid((rows, cols, slices), cell)
+    edges = np.linspace(140.0, 20.0, 17)
+    lib = spectral_library(edges, bremsstrahlung_spectrum(kvp=140.0, seed=0), [WATER, BONE], legendre_order=7)
+    geo = ConeGeometry(100.0, 150.0, 384, 512, 0.08, 0.08, use_curved_detector=True)
+    return Workload("mixed_precision_views", grid, geo, cylinder_phantom(grid, 11.0, 1.5, seed), lib, 10, 24, 7,
+                    cell, 90)
 
 
 INSERT_DENSITIES = (0.0012, 1.04, 1.85)   # air, soft tissue (water material), bone

@@ -97,3 +97,57 @@ def test_graphed_outer_iterations_equal_batched_steps(cuda_device, name):
             assert rel_err(states[v].collided_moments, eager[v].collided_moments) < 1e-6, (step, v)
             assert abs(states[v].history[-1] - eager[v].history[-1]) < 1e-6
     assert graphed.replays == 3
+
+
+def test_graphed_outer_iteration_seeded_with_accumulators(cuda_device):
+    """GraphedOuterIteration.seed starts every view from given accumulators (as the learned proposal does): seeded
+    with the accumulators of an eager cold step, its next steps (the first eager, the rest replayed from the graph)
+    equal the eager batched steps that follow that cold step."""
+    g, solver = _solver("flat", cuda_device)
+    grid = Grid((8, 8, 6), 1.0)
+    rho = torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device)
+    angles = [0.3, 1.7, 4.0]
+    fields = solver.material_fields(rho, grid)
+    _, _, eager = batched_view_steps(solver, [CitrusState() for _ in angles], fields, angles, batch=2)
+    graphed = GraphedOuterIteration(solver, grid, angles, batch=2)
+    graphed.seed(rho, [s.collided_moments.clone() for s in eager])
+    for step in range(3):
+        signals, states = graphed.step(rho)
+        ref, _, eager = batched_view_steps(solver, eager, fields, angles, batch=2)
+        for v in range(len(angles)):
+            assert rel_err(signals[v], ref[v]) < 1e-6, (step, v)
+            assert rel_err(states[v].collided_moments, eager[v].collided_moments) < 1e-6, (step, v)
+    assert graphed.replays == 2
+    with pytest.raises(ValueError):
+        graphed.seed(rho, [eager[0].collided_moments])
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_direction_chunks_of_the_batched_step(cuda_device, monkeypatch, precision):
+    """A store budget that forces direction chunks (1 and 3 directions per octant of the 4 x 8 set's 4) gives the
+    unchunked batched steps' signals and accumulators to rounding (the moment product accumulates over the chunks;
+    in bf16x3 each chunk's product carries the split's own ~1e-5), cold and warm."""
+    import citrus_gb300.batched as batched
+    g, solver = _solver("curved", cuda_device, moment_precision=precision)
+    grid = Grid((8, 8, 6), 1.0)
+    fields = solver.material_fields(torch.as_tensor(g["rho"], dtype=torch.float32, device=cuda_device), grid)
+    angles = [0.3, 1.7, 4.0]
+    ctx = solver.sweep_context(fields.grid_coarse)
+    per_direction = 8 * ctx.num_cells * 4 * solver.num_groups * 4
+    runs = []
+    for budget in (batched.SWEEP_STORE_BUDGET_BYTES, per_direction, 3 * per_direction):
+        monkeypatch.setattr(batched, "SWEEP_STORE_BUDGET_BYTES", budget)
+        states = [CitrusState() for _ in angles]
+        out = []
+        for _ in range(2):
+            signals, _, states = batched_view_steps(solver, states, fields, angles, batch=2)
+            out.append((signals.clone(), [s.collided_moments.clone() for s in states]))
+        runs.append(out)
+    assert batched.direction_chunk(ctx.num_cells, solver.num_groups, ctx.directions_per_octant,
+                                   per_direction) == 1
+    tol = 1e-6 if precision == "fp32" else 2e-5   # bf16x3: the hi/lo split's ~1e-5, chunk partials added in float32
+    for other in runs[1:]:
+        for (sa, aa), (sb, ab) in zip(runs[0], other):
+            assert rel_err(sb, sa) < tol
+            for x, y in zip(ab, aa):
+                assert rel_err(x, y) < tol
