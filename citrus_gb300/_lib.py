@@ -44,6 +44,7 @@ SIGNATURES = {
     "citrus_oblique_project": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P],
     "citrus_group_transmission": [P, I64, I64, P, P, P, I64, I64, P, P, P, P, P],
     "citrus_source_weight": [P, P, P, P, P, P, I64, I32, P, P],
+    "citrus_source_field": [P, P, P, P, I64, F64, P, P, I64, P, P, P, P, P, I64, I32, P, P, P],
     "citrus_first_collision_source": [P, I64, P, I64, P, P, P, P, I64, F64, F64, P, I64, P, P],
     "citrus_first_collision_moments": [P, I64, P, I64, P, P, I64, P, P, I64, F64, F64, P, I64, P, P, P, P, P, I64,
                                        P],
@@ -58,6 +59,7 @@ SIGNATURES = {
     "citrus_weighted_group_sum": [P, P, I64, I64, I64, I64, I64, P, P],
     "citrus_sum_directions": [P, I64, I64, I64, P, I32, P],
     "citrus_weighted_direction_sum": [P, I64, I64, I64, I64, I64, I64, I64, I64, P, I64, I64, P, I32, P],
+    "citrus_grid_signal_sum": [P, I64, I64, I64, I64, I64, I64, I64, I64, P, I64, P, I64, P, P, P, P, P, P, P, P, I32, I32, P],
     "citrus_conv3d_forward": [P, I64, P, I64, I32, P, P, P, I64, I64, I64, I64, I64, I32, I32, P],
     "citrus_conv3d_backward_input": [P, I64, P, P, I64, P, P, I64, I64, I64, I64, I64, I32, P],
     "citrus_conv3d_forward_config": [P, I64, P, I64, I32, P, P, P, I64, I64, I64, I64, I64, I32, I32, I32, P, P],

@@ -70,6 +70,9 @@ def views_that_fit(ctx, num_groups: int, dc: int, device, share: float = 0.6) ->
     if torch.cuda.is_current_stream_capturing():
         return 1 << 30
     free, _ = torch.cuda.mem_get_info(device)
+    # memory the caching allocator holds but no tensor uses counts as free: the count then does not depend on what
+    # the previous step left cached, and the views per launch (and the products' tuned shapes) stay the same
+    free += torch.cuda.memory_reserved(device) - torch.cuda.memory_allocated(device)
     return max(1, int(share * free) // per_view)
 
 

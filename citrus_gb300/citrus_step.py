@@ -172,8 +172,9 @@ def primary_signals(solver: ScatterSolver, fields: MaterialFields, angles, out: 
     present = present_materials(rho)                                   # once for all views
     traced = (rho if present is None else rho[list(present)]).contiguous()
     for v, angle in enumerate(angle_array):
-        path = primary_path_lengths(solver.projectors, traced, fields.grid_fine, solver.geometry, float(angle))
+        path = primary_path_lengths(solver.projectors, traced, fields.grid_fine, solver.geometry, float(angle),
+                                    solver.primary_samples_per_pixel_axis)
         image = primary_from_path_lengths(solver.library, path, present, solver.geometry, float(angle), solver.source,
-                                          solver.detector, solver.grid_response)
+                                          *solver.responses())
         out[v] = image["signal"] if quantity == "signal" else image["planar_fluence"].sum(0)
     return out

@@ -154,7 +154,39 @@ struct Field {
   double off_u, off_v, half_u, half_v, margin_u, margin_v;
 };
 
-__device__ __forceinline__ float source_weight(const Field& fd, float x, float y, float z, int squared) {
+// Emission profile, off-focal table and beam filter of the source (all optional; float64 tables on the device).
+struct SourceExtras {
+  const double* profile;    // [rows, channels] relative emission toward each pixel centre, or null
+  const double* thickness;  // [t_rows, channels] filter thickness in cm at the pixel centres, or null
+  int t_rows;
+  const double* off_nodes;  // [n_off] ascending distances past the field edge in cm, or null
+  const double* off_values; // [n_off] emission there relative to the field edge
+  int n_off;
+  int rows, channels;
+  double d_row, d_ch, off_row, off_ch;
+  double filter_density;
+};
+
+// Bilinear at panel coordinates, held at the outermost pixel centres (source.py:484-510)
+__device__ double panel_interpolate(const double* __restrict__ img, int img_rows, const SourceExtras& ex, double u,
+                                    double v) {
+  const double xc = fmin(fmax((u + ex.off_ch) / ex.d_ch + (ex.channels - 1) * 0.5, 0.0), ex.channels - 1.0);
+  const double xr = fmin(fmax((v + ex.off_row) / ex.d_row + (ex.rows - 1) * 0.5, 0.0), ex.rows - 1.0);
+  const int c0 = min(max((int)floor(xc), 0), max(ex.channels - 2, 0)), c1 = min(c0 + 1, ex.channels - 1);
+  int r0 = min(max((int)floor(xr), 0), max(ex.rows - 2, 0)), r1 = min(r0 + 1, ex.rows - 1);
+  if (img_rows == 1) r0 = r1 = 0;
+  const double wc = fmin(fmax(xc - c0, 0.0), 1.0), wr = fmin(fmax(xr - r0, 0.0), 1.0);
+  const double* a = img + (int64_t)r0 * ex.channels;
+  const double* b = img + (int64_t)r1 * ex.channels;
+  const double top = a[c0] + (a[c1] - a[c0]) * wc;
+  const double bottom = b[c0] + (b[c1] - b[c0]) * wc;
+  return top + (bottom - top) * wr;
+}
+
+// b(Omega) (/ |r - r0|^2) and the filter path rho_f t(Omega) of the ray from the focal spot through (x, y, z)
+// (source.py:289-430)
+__device__ __forceinline__ float source_field(const Field& fd, const SourceExtras& ex, float x, float y, float z,
+                                              int squared, float* filter_path) {
   const double dx = x - fd.r0[0], dy = y - fd.r0[1], dz = z - fd.r0[2];
   double t;
   if (!fd.curved) {
@@ -166,7 +198,7 @@ __device__ __forceinline__ float source_weight(const Field& fd, float x, float y
     const double a = dx * dx + dy * dy;
     t = a > 0 ? fd.sdd / sqrt(a) : INFINITY;
   }
-  double w = 0.0;
+  double w = 0.0, path = 0.0;
   if (isfinite(t) && t > 0) {
     const double hx = fd.r0[0] + t * dx, hy = fd.r0[1] + t * dy, hz = fd.r0[2] + t * dz;
     double u, v;
@@ -174,22 +206,40 @@ __device__ __forceinline__ float source_weight(const Field& fd, float x, float y
       u = (hx - fd.center[0]) * fd.u_hat[0] + (hy - fd.center[1]) * fd.u_hat[1] + (hz - fd.center[2]) * fd.u_hat[2];
       v = (hx - fd.center[0]) * fd.v_hat[0] + (hy - fd.center[1]) * fd.v_hat[1] + (hz - fd.center[2]) * fd.v_hat[2];
     } else {
-      const double ex = hx - fd.r0[0], ey = hy - fd.r0[1], ez = hz - fd.r0[2];
-      const double depth = -(ex * fd.n_hat[0] + ey * fd.n_hat[1] + ez * fd.n_hat[2]);
-      u = fd.sdd * atan2(ex * fd.u_hat[0] + ey * fd.u_hat[1] + ez * fd.u_hat[2], depth);
-      v = fd.sdd * (ex * fd.v_hat[0] + ey * fd.v_hat[1] + ez * fd.v_hat[2]) / depth;
+      const double ex_ = hx - fd.r0[0], ey = hy - fd.r0[1], ez = hz - fd.r0[2];
+      const double depth = -(ex_ * fd.n_hat[0] + ey * fd.n_hat[1] + ez * fd.n_hat[2]);
+      u = fd.sdd * atan2(ex_ * fd.u_hat[0] + ey * fd.u_hat[1] + ez * fd.u_hat[2], depth);
+      v = fd.sdd * (ex_ * fd.v_hat[0] + ey * fd.v_hat[1] + ez * fd.v_hat[2]) / depth;
     }
-    const bool inside = fabs(u + fd.off_u) <= fd.half_u + fd.margin_u && fabs(v + fd.off_v) <= fd.half_v + fd.margin_v;
-    w = inside ? 1.0 : 0.0;
+    const double edge_u = fd.half_u + fd.margin_u, edge_v = fd.half_v + fd.margin_v;
+    const double au = fabs(u + fd.off_u), av = fabs(v + fd.off_v);
+    if (au <= edge_u && av <= edge_v) {
+      w = 1.0;
+    } else if (ex.n_off > 0) {  // past the field edge: the off-focal fraction of the distance to the field rectangle
+      const double pu = fmax(au - edge_u, 0.0), pv = fmax(av - edge_v, 0.0);
+      const double dist = sqrt(pu * pu + pv * pv);
+      if (dist <= ex.off_nodes[ex.n_off - 1]) {
+        int above = 0;  // nodes <= dist
+        while (above < ex.n_off && ex.off_nodes[above] <= dist) ++above;
+        const int i0 = min(max(above - 1, 0), ex.n_off - 1), i1 = min(above, ex.n_off - 1);
+        const double span = ex.off_nodes[i1] - ex.off_nodes[i0];
+        const double f = span > 0 ? fmin(fmax((dist - ex.off_nodes[i0]) / span, 0.0), 1.0) : 0.0;
+        w = ex.off_values[i0] + (ex.off_values[i1] - ex.off_values[i0]) * f;
+      }
+    }
+    if (w != 0.0 && ex.profile) w *= panel_interpolate(ex.profile, ex.rows, ex, u, v);
+    if (ex.thickness) path = panel_interpolate(ex.thickness, ex.t_rows, ex, u, v) * ex.filter_density;
   }
+  if (filter_path) *filter_path = (float)path;
   if (!squared) return (float)w;
   const float fx = x - (float)fd.r0[0], fy = y - (float)fd.r0[1], fz = z - (float)fd.r0[2];
   return (float)w / (fx * fx + fy * fy + fz * fz);
 }
 
-__global__ void source_weight_kernel(Field fd, const double* __restrict__ pts, const double* __restrict__ ax_x,
-                                     const double* __restrict__ ax_y, const double* __restrict__ ax_z, int gc, int gs,
-                                     int64_t P, int squared, float* __restrict__ out) {
+__global__ void source_weight_kernel(Field fd, SourceExtras ex, const double* __restrict__ pts,
+                                     const double* __restrict__ ax_x, const double* __restrict__ ax_y,
+                                     const double* __restrict__ ax_z, int gc, int gs, int64_t P, int squared,
+                                     float* __restrict__ out, float* __restrict__ filter_out) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   float x, y, z;
@@ -203,7 +253,9 @@ __global__ void source_weight_kernel(Field fd, const double* __restrict__ pts, c
     y = (float)ax_y[row];
     z = (float)ax_z[rem - col * gs];
   }
-  out[p] = source_weight(fd, x, y, z, squared);
+  float path;
+  out[p] = source_field(fd, ex, x, y, z, squared, filter_out ? &path : nullptr);
+  if (filter_out) filter_out[p] = path;
 }
 
 // ---- shared point inputs of the first-collision kernels ---------------------------------------------------------
@@ -738,7 +790,11 @@ __device__ __forceinline__ void load_groups(const float* __restrict__ p, int G, 
   }
 }
 
-template <int kGP, int kMM, int kDirs, bool kVec>
+// kQ1: one point per cell (the point is the cell's centre: no in-cell offsets, no cell attenuation needed). A warp's
+// loads of its next direction's multiple-collision source and path lengths are issued before the table sums of the
+// current one, so their latency hides behind that arithmetic; 3 blocks of 256 threads per SM (80 registers, the
+// 64 KB table window).
+template <int kGP, int kMM, int kDirs, bool kVec, bool kQ1>
 __global__ void __launch_bounds__(32 * kEmitWarps, 3) emission_warps_kernel(
     FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, int K,
     const float* __restrict__ tau /*[K, NC, G], or [K, NC, TM] path lengths with tau_mu*/,
@@ -797,7 +853,7 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 3) emission_warps_kernel(
     offx = dx * ((float)(j - jc * F) - half);
     offz = dz * ((float)(k - kc * F) - half);
     h = heights ? __ldg(heights + v) : 0.f;
-    if (F > 1) {
+    if (!kQ1) {
 #pragma unroll
       for (int q = 0; q < kGP; ++q)
         if (q < G) muc[q] = __ldg(mu + (int64_t)q * NC + cell);
@@ -811,19 +867,33 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 3) emission_warps_kernel(
 
   auto directions = [&](auto windowed) {
     constexpr bool kWin = decltype(windowed)::value;
+    float smc_n[kGP], P_n[kMM];
+    auto fetch = [&](int dd) {
+      if (valid && dd < nd) {
+        const int64_t dc = (d0 + dd) * NC + cell;
+        load_groups<kGP, kVec>(multiple + dc * G, G, smc_n);
+        if (tau_mu != nullptr) {
+#pragma unroll
+          for (int m = 0; m < kMM; ++m) P_n[m] = m < TM ? __ldg(tau + dc * TM + m) : 0.f;
+        }
+      }
+    };
+    fetch(warp);
     for (int dd = warp; dd < nd; dd += kEmitWarps) {
       const int64_t d = d0 + dd;
       float e[kGP];
 #pragma unroll
       for (int q = 0; q < kGP; ++q) e[q] = 0.f;
+      float smc[kGP], P[kMM];
+#pragma unroll
+      for (int q = 0; q < kGP; ++q) smc[q] = smc_n[q];
+#pragma unroll
+      for (int m = 0; m < kMM; ++m) P[m] = P_n[m];
+      fetch(dd + kEmitWarps);  // the next direction's loads in flight during this one's table sums
       if (valid) {
         const int64_t dc = d * NC + cell;
-        float smc[kGP], t[kGP];
-        load_groups<kGP, kVec>(multiple + dc * G, G, smc);  // issued first: the longest latency
+        float t[kGP];
         if (tau_mu != nullptr) {  // sum_m mu[m, g] P_m, in material order
-          float P[kMM];
-#pragma unroll
-          for (int m = 0; m < kMM; ++m) P[m] = m < TM ? __ldg(tau + dc * TM + m) : 0.f;
 #pragma unroll
           for (int q = 0; q < kGP; ++q) t[q] = 0.f;
 #pragma unroll
@@ -840,7 +910,7 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 3) emission_warps_kernel(
         int i0;
         float w;
         table_position(tb, cosine, i0, w);
-        const float offset = pg.f > 1 ? oy * offy + ox * offx + oz * offz : 0.f;
+        const float offset = kQ1 ? 0.f : oy * offy + ox * offx + oz * offz;
         float src[kGP];
 #pragma unroll
         for (int q = 0; q < kGP; ++q) src[q] = 0.f;
@@ -862,7 +932,7 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 3) emission_warps_kernel(
 #pragma unroll
         for (int g = 0; g < kGP; ++g) {
           if (g >= G) break;
-          const float depth = pg.f > 1 ? fmaxf(t[g] - muc[g] * offset, 0.f) : fmaxf(t[g], 0.f);
+          const float depth = kQ1 ? fmaxf(t[g], 0.f) : fmaxf(t[g] - muc[g] * offset, 0.f);
           e[g] = (src[g] + smc[g]) * __expf(-depth);  // the fast exponential: within a few ulp for these depths
         }
       }
@@ -1052,11 +1122,12 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_correction_kernel(
 // writes the source values to the cache; the warps' partial sums are then added in warp order, and the float64
 // factors formed as fc_correction_kernel forms them. The sums differ from fc_correction_kernel's at rounding level
 // (another order of the same terms).
+// 3 blocks of 256 threads per SM (80 registers): at 2 (128 registers) the table gathers' latency went unhidden
 constexpr int kFcWarps = 8;
 constexpr int kFcDirBatch = 32;
 
 template <int kGP, int kMM, bool kVec>
-__global__ void __launch_bounds__(32 * kFcWarps, 2) fc_correction_warps_kernel(
+__global__ void __launch_bounds__(32 * kFcWarps, 3) fc_correction_warps_kernel(
     FCInputs in, Table tb, PointGrid pg, const float* __restrict__ omegas, const float* __restrict__ weights, int K,
     const float* __restrict__ moments /*[M, 2, G, G]*/, float* __restrict__ sums /*[5, G, V] or null*/,
     float* __restrict__ scale, float* __restrict__ beta, float* __restrict__ cache /*[K, G, V] or null*/) {
@@ -1442,11 +1513,22 @@ extern "C" int citrus_group_transmission(const float* path, int64_t num_material
   return launch_status("citrus_group_transmission");
 }
 
-extern "C" int citrus_source_weight(const double* field, const double* points, const double* axis_x,
-                                    const double* axis_y, const double* axis_z, const int64_t* point_dims,
-                                    int64_t num_points, int32_t divide_by_distance_squared, float* out, void* stream) {
-  CITRUS_REQUIRE(field && out, "citrus_source_weight: null pointer");
-  CITRUS_REQUIRE(points || (axis_x && axis_y && axis_z && point_dims), "citrus_source_weight: no points");
+extern "C" int citrus_source_field(const double* field, const double* panel, const double* profile,
+                                   const double* thickness, int64_t thickness_rows, double filter_density,
+                                   const double* off_focal_nodes, const double* off_focal_values,
+                                   int64_t num_off_focal, const double* points, const double* axis_x,
+                                   const double* axis_y, const double* axis_z, const int64_t* point_dims,
+                                   int64_t num_points, int32_t divide_by_distance_squared, float* out,
+                                   float* filter_path_out, void* stream) {
+  CITRUS_REQUIRE(field && out, "citrus_source_field: null pointer");
+  CITRUS_REQUIRE(points || (axis_x && axis_y && axis_z && point_dims), "citrus_source_field: no points");
+  CITRUS_REQUIRE(num_points >= 0 && num_off_focal >= 0, "citrus_source_field: negative size");
+  CITRUS_REQUIRE((num_off_focal == 0) == (off_focal_nodes == nullptr) &&
+                     (off_focal_nodes == nullptr) == (off_focal_values == nullptr),
+                 "citrus_source_field: the off-focal nodes and values go together with their count");
+  CITRUS_REQUIRE((thickness == nullptr) == (filter_path_out == nullptr),
+                 "citrus_source_field: the filter thickness and the filter-path output go together");
+  CITRUS_REQUIRE(!(profile || thickness) || panel, "citrus_source_field: a profile or a filter needs the panel");
   Field fd;
   fd.curved = field[0] != 0.0;
   for (int a = 0; a < 3; ++a) {
@@ -1463,6 +1545,26 @@ extern "C" int citrus_source_weight(const double* field, const double* points, c
   fd.half_v = field[20];
   fd.margin_u = field[21];
   fd.margin_v = field[22];
+  SourceExtras ex{};
+  ex.profile = profile;
+  ex.thickness = thickness;
+  ex.off_nodes = off_focal_nodes;
+  ex.off_values = off_focal_values;
+  ex.n_off = (int)num_off_focal;
+  ex.filter_density = filter_density;
+  if (panel) {
+    ex.rows = (int)panel[0];
+    ex.channels = (int)panel[1];
+    ex.d_row = panel[2];
+    ex.d_ch = panel[3];
+    ex.off_row = panel[4];
+    ex.off_ch = panel[5];
+    CITRUS_REQUIRE(ex.rows >= 1 && ex.channels >= 1 && ex.d_row > 0 && ex.d_ch > 0,
+                   "citrus_source_field: bad panel");
+  }
+  ex.t_rows = (int)thickness_rows;
+  CITRUS_REQUIRE(!thickness || thickness_rows == 1 || thickness_rows == ex.rows,
+                 "citrus_source_field: the filter thickness must have 1 or all rows");
   int gc = 1, gs = 1;
   if (!points) {
     gc = (int)point_dims[1];
@@ -1470,9 +1572,16 @@ extern "C" int citrus_source_weight(const double* field, const double* points, c
   }
   if (num_points == 0) return CITRUS_OK;
   source_weight_kernel<<<(unsigned)cdiv(num_points, 128), 128, 0, as_stream(stream)>>>(
-      fd, points, axis_x, axis_y, axis_z, gc, gs, num_points, divide_by_distance_squared, out);
+      fd, ex, points, axis_x, axis_y, axis_z, gc, gs, num_points, divide_by_distance_squared, out, filter_path_out);
   note_launches();
-  return launch_status("citrus_source_weight");
+  return launch_status("citrus_source_field");
+}
+
+extern "C" int citrus_source_weight(const double* field, const double* points, const double* axis_x,
+                                    const double* axis_y, const double* axis_z, const int64_t* point_dims,
+                                    int64_t num_points, int32_t divide_by_distance_squared, float* out, void* stream) {
+  return citrus_source_field(field, nullptr, nullptr, nullptr, 0, 0.0, nullptr, nullptr, 0, points, axis_x, axis_y,
+                             axis_z, point_dims, num_points, divide_by_distance_squared, out, nullptr, stream);
 }
 
 extern "C" int citrus_first_collision_source(const float* rho, int64_t num_materials, const float* phi,
@@ -1748,21 +1857,34 @@ int launch_emission(dim3 grid, int G, cudaStream_t s, const FCInputs& in, const 
                                                harmonics, moments, NS, heights, signal_weight, deltas, out, partial);
 }
 
+template <int kGP, int kMM, int kDirs, bool kVec, bool kQ1>
+int launch_emission_warps_q(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
+                            const float* omegas, int K, const float* tau, const float* tau_mu, int TM,
+                            const float* mu, const float* multiple, const float* heights, const float* signal_weight,
+                            const double* deltas, float* out, float* partial) {
+  constexpr int bytes = emission_window_bytes(kDirs);
+  cudaError_t e = cudaFuncSetAttribute(emission_warps_kernel<kGP, kMM, kDirs, kVec, kQ1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "emission window: %s", cudaGetErrorString(e));
+  grid.y = (unsigned)cdiv(K, kDirs);
+  emission_warps_kernel<kGP, kMM, kDirs, kVec, kQ1><<<grid, 32 * kEmitWarps, bytes, s>>>(
+      in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, heights, signal_weight, (float)deltas[0],
+      (float)deltas[1], (float)deltas[2], out, partial);
+  note_launches();
+  return CITRUS_OK;
+}
+
 template <int kGP, int kMM, int kDirs, bool kVec>
 int launch_emission_warps_d(dim3 grid, cudaStream_t s, const FCInputs& in, const Table& tb, const PointGrid& pg,
                             const float* omegas, int K, const float* tau, const float* tau_mu, int TM,
                             const float* mu, const float* multiple, const float* heights, const float* signal_weight,
                             const double* deltas, float* out, float* partial) {
-  constexpr int bytes = emission_window_bytes(kDirs);
-  cudaError_t e = cudaFuncSetAttribute(emission_warps_kernel<kGP, kMM, kDirs, kVec>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "emission window: %s", cudaGetErrorString(e));
-  grid.y = (unsigned)cdiv(K, kDirs);
-  emission_warps_kernel<kGP, kMM, kDirs, kVec><<<grid, 32 * kEmitWarps, bytes, s>>>(
-      in, tb, pg, omegas, K, tau, tau_mu, TM, mu, multiple, heights, signal_weight, (float)deltas[0],
-      (float)deltas[1], (float)deltas[2], out, partial);
-  note_launches();
-  return CITRUS_OK;
+  if (pg.f == 1)
+    return launch_emission_warps_q<kGP, kMM, kDirs, kVec, true>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
+                                                                multiple, heights, signal_weight, deltas, out,
+                                                                partial);
+  return launch_emission_warps_q<kGP, kMM, kDirs, kVec, false>(grid, s, in, tb, pg, omegas, K, tau, tau_mu, TM, mu,
+                                                               multiple, heights, signal_weight, deltas, out, partial);
 }
 
 template <int kGP, int kMM, bool kVec>

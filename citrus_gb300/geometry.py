@@ -254,6 +254,20 @@ class ConeGeometry:
         to_axis[..., 2] = 0.0
         return to_axis / np.linalg.norm(to_axis, axis=-1, keepdims=True)
 
+    def local_panel_axes_np(self, points: np.ndarray, angle: float) -> tuple:
+        """float64 (u_hat, v_hat, n_hat) [..., 3] of the panel surface at panel points (reference
+        ``geometry.py:624-646``): the panel axes on a flat panel; on a curved one the horizontal normal toward the
+        cylinder axis, the vertical v_hat and u_hat = n_hat x v_hat along the arc."""
+        points = np.asarray(points, dtype=np.float64)
+        u_hat, v_hat, n_hat = (np.broadcast_to(np.asarray(a, dtype=np.float64), points.shape)
+                               for a in self.panel_axes(angle))
+        if not self.use_curved_detector:
+            return u_hat, v_hat, n_hat
+        to_axis = np.asarray(self.source_position(angle)) - points
+        to_axis = to_axis - (to_axis * v_hat).sum(-1, keepdims=True) * v_hat
+        n_local = to_axis / np.linalg.norm(to_axis, axis=-1, keepdims=True)
+        return np.cross(n_local, v_hat), v_hat, n_local
+
     def panel_distance_along_np(self, points: np.ndarray, omega: np.ndarray, angle: float) -> np.ndarray:
         """Distance t with ``points + t omega`` on the panel surface (reference ``geometry.py:673-732``)."""
         points = np.asarray(points, dtype=np.float64)

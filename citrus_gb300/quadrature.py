@@ -208,7 +208,7 @@ def spherical_harmonic_basis(L: int, quadrature: Quadrature) -> SphericalHarmoni
 def to_device(a: np.ndarray, device, dtype=torch.float32) -> Tensor:
     """A host table as a contiguous device tensor; a CUDA copy goes through pinned memory and is queued on the
     current stream without waiting for it (a copy from pageable memory blocks until the stream has drained)."""
-    t = torch.tensor(np.asarray(a), dtype=dtype)
+    t = torch.tensor(np.ascontiguousarray(a), dtype=dtype)  # torch.tensor keeps a transposed array's strides
     if torch.device(device).type != "cuda":
         return t.to(device)
     return t.pin_memory().to(device, non_blocking=True)

@@ -69,6 +69,12 @@ class HostArgs:
         self._keep.append(arr)
         return ctypes.addressof(arr)
 
+    def pointers(self, addresses) -> int:
+        """A host array of device addresses."""
+        arr = (ctypes.c_void_p * len(addresses))(*[int(a) for a in addresses])
+        self._keep.append(arr)
+        return ctypes.addressof(arr)
+
 
 def _grid_args(host: HostArgs, grid: Grid) -> tuple:
     return host.doubles(list(grid.lower_corner()) + list(grid.deltas)), host.int64s(

@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import math
 import os
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 from typing import Optional
 
 import numpy as np
@@ -25,7 +25,8 @@ from .cross_sections import MultigroupLibrary
 from .geometry import ConeGeometry, Grid
 from .quadrature import Quadrature, hemisphere_quadrature, real_spherical_harmonics, to_device
 from .ray_tracing import HostArgs
-from .responses import DetectorResponse, GridResponse, SourceModel, detector_angle
+from .responses import (DetectorResponse, GridResponse, SourceModel, detector_angle, grid_angles,
+                        septa_dependence)
 from .uncollided import _FCArgs, group_transmission, present_materials
 
 IMAGE_CHUNK_MAX_DIRECTIONS = 32
@@ -67,18 +68,35 @@ def panel_direction_set(geometry: ConeGeometry, angle: float, counts: tuple, max
 
 
 @dataclass(eq=False)
+class PixelSepta:
+    """One set of septa whose grid angles vary along the rows and the channels together (reference ``_PixelGrid``,
+    ``scatter_image.py:437-486``, its "sum" form): theta(k, r, c) = theta_channels[:, k, c] + theta_pixels[:, r, c],
+    and the table at the group energies. Device float32."""
+
+    theta_channels: Tensor  # [2, K, Cd]
+    theta_pixels: Tensor    # [2, Rd, Cd]
+    table: Tensor           # [G, T1, T2]
+    theta1_nodes: Tensor    # [T1]
+    theta2_nodes: Tensor    # [T2]
+
+
+@dataclass(eq=False)
 class DirectionSetContext:
-    """The emission-independent part of one view's image (reference ``scatter_image.py:137-405``, for detector
-    responses that depend on energy and incidence and grid responses that do not depend on the angles).
+    """The emission-independent part of one view's image (reference ``scatter_image.py:137-405``).
 
     Device tensors (float32): omega [K, 3], weight [K], cos_theta0 [K], cell_width [K, 2]; ``signal_group_weight``
-    [K, G] when the signal weights are the same at every pixel (flat panel), else ``signal_channel_weight``
-    [K, G, Cd] (curved panel: incidence per channel); ``planar_weight`` [K, 1 | Cd]. A curved panel whose detector
-    response separates into a factor of the energy and a factor of the incidence (the ideal counting response, for
-    one) also has ``signal_group_weight`` [K, G] and ``signal_column_weight`` [K, Cd] with
+    [K, G] when the signal weights are the same at every pixel (flat panel, a grid that varies only with the
+    direction), else ``signal_channel_weight`` [K, G, Cd] (curved panel: incidence per channel; septa along the
+    rows); ``planar_weight`` [K, 1 | Cd]. A curved panel whose detector response separates into a factor of the
+    energy and a factor of the incidence (the ideal counting response, for one) also has ``signal_group_weight``
+    [K, G] and ``signal_column_weight`` [K, Cd] with
     ``signal_channel_weight[k, g, c] = signal_group_weight[k, g] * signal_column_weight[k, c]``: the signal image is
     then the group sum weighted in the emission, blurred, and weighted per channel in the sum over the directions
     (the channel blur acts before the channel weights in the reference, and the row blur commutes with them).
+    An anti-scatter grid that varies along the rows adds ``signal_row_weight`` [K, G, Rd], septa that vary along
+    the rows and the channels together add ``pixel_septa``; the signal is then accumulated by
+    ``citrus_grid_signal_sum`` from the blurred per-group images (the reference applies these weights after the
+    footprint blur too).
     """
 
     quadrature: Quadrature
@@ -95,6 +113,9 @@ class DirectionSetContext:
     chunk_bounds: tuple
     image_shape: tuple
     signal_column_weight: Optional[Tensor] = None
+    signal_row_weight: Optional[Tensor] = None
+    pixel_septa: tuple = ()
+    septa_kinds: tuple = ()
     _cache: dict = field(default_factory=dict, repr=False)
 
     @property
@@ -104,6 +125,11 @@ class DirectionSetContext:
     @property
     def device(self) -> torch.device:
         return self.omega.device
+
+    @property
+    def grid_varies_over_panel(self) -> bool:
+        """True when the signal needs ``citrus_grid_signal_sum`` (weights per row, or per pixel)."""
+        return self.signal_row_weight is not None or bool(self.pixel_septa)
 
     def harmonics(self, L: int) -> Tensor:
         key = ("Y", int(L))
@@ -128,6 +154,50 @@ class DirectionSetContext:
         return self._cache[key]
 
 
+def _grid_factors(grid_response: GridResponse, energy: np.ndarray, omega: np.ndarray, geometry: ConeGeometry,
+                  angle: float, device) -> tuple:
+    """Septa factors of one view (reference ``scatter_image.py:605-657``): ([G, K] per direction, [G, K, Rd] per row
+    or None, [G, K, Cd] per channel or None, pixel septa, kinds). How each set of septa varies over the panel is
+    decided from probe directions (the inward normal and three of the set's directions)."""
+    G, K = energy.size, omega.shape[0]
+    pixels = geometry.pixel_centers_np(angle)
+    n_hat = np.asarray(geometry.panel_axes(angle)[2])
+    probe = -n_hat[None]
+    if K:
+        probe = np.concatenate([probe, omega[[0, K // 2, K - 1]]])
+    direction = np.ones((G, K))
+    rows = channels = None
+    pixel = []
+    kinds = []
+    for septa in grid_response.septa_sets():
+        kind = septa_dependence(septa, probe, pixels, geometry, angle)
+        kinds.append(kind)
+        if kind == "none":
+            direction = direction * septa.at(energy, 0.0, 0.0)[:, None]
+        elif kind == "direction":
+            direction = direction * septa.transmission_at(energy, omega, pixels[:1, :1], geometry, angle)[:, :, 0, 0]
+        elif kind == "rows":
+            t = septa.transmission_at(energy, omega, pixels[:, :1], geometry, angle)[..., 0]        # [G, K, Rd]
+            rows = t if rows is None else rows * t
+        elif kind == "channels":
+            t = septa.transmission_at(energy, omega, pixels[:1], geometry, angle)[:, :, 0]          # [G, K, Cd]
+            channels = t if channels is None else channels * t
+        elif kind == "sum":
+            first_row = np.stack(grid_angles(omega, pixels[:1], geometry, angle, septa.focal_distance_cm,
+                                             septa.septa_along))                                     # [2, K, 1, Cd]
+            one = np.stack(grid_angles(omega[:1], pixels, geometry, angle, septa.focal_distance_cm,
+                                       septa.septa_along))                                           # [2, 1, Rd, Cd]
+            pixel.append(PixelSepta(to_device(np.ascontiguousarray(first_row[:, :, 0]), device),
+                                    to_device(np.ascontiguousarray((one - one[:, :, :1])[:, 0]), device),
+                                    to_device(np.ascontiguousarray(septa.table_at_energy(energy)), device),
+                                    to_device(septa.theta1_rad, device), to_device(septa.theta2_rad, device)))
+        else:
+            raise NotImplementedError(
+                f"{septa.name}: grid angles that are not a part per direction and channel plus a part per pixel "
+                "(the reference's 'general' septa) are not evaluated on this path")
+    return direction, rows, channels, tuple(pixel), tuple(kinds)
+
+
 def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle: float, detector: DetectorResponse,
                            grid_response: GridResponse, library: MultigroupLibrary, device,
                            chunk: int = 8) -> DirectionSetContext:
@@ -145,29 +215,42 @@ def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle
     cos64 = (omega * (-n_hat)).sum(-1)
     K = kept.size
     Rd, Cd = geometry.image_shape
-    grid_t = grid_response.at_energy(energy)                                    # [G]
+    grid_direction, grid_rows, grid_channels, pixel_septa, kinds = _grid_factors(grid_response, energy, omega,
+                                                                                 geometry, angle, device)
+    row_weight = None if grid_rows is None else to_device(np.ascontiguousarray(grid_rows.transpose(1, 0, 2)), device)
     if geometry.use_curved_detector:
         pixels = geometry.pixel_centers_np(angle)
         normals = geometry.local_normals_np(pixels[0], angle)                   # [Cd, 3]
         cos_channel = np.clip(omega @ (-normals).T, 0.0, 1.0)                   # [K, Cd]
         planar = weight[:, None] * cos_channel
         response = detector.at(energy, np.arccos(cos_channel))                 # [G, K, Cd]
-        channel = planar[None] * response * grid_t[:, None, None]              # [G, K, Cd]
+        channel = planar[None] * response * grid_direction[:, :, None]         # [G, K, Cd]
+        if grid_channels is not None:
+            channel = channel * grid_channels
         signal_group, signal_channel = None, to_device(channel.transpose(1, 0, 2), device)
         planar_weight = to_device(planar, device)
         # a response D(E, theta) = f(E) h(theta): group factors f_g / f_0 and channel factors D(E_0, theta_kc)
         first = response[:1]
-        if K and np.all(first > 0):
+        if K and np.all(first > 0) and grid_channels is None:
             ratio = response / first
             if np.allclose(ratio, ratio[:, :1, :1], rtol=1e-12, atol=0.0):
-                group = np.broadcast_to((ratio[:, 0, 0] * grid_t)[None, :], (K, G))
-                signal_group = to_device(np.ascontiguousarray(group), device)
+                group = ratio[:, 0, 0][:, None] * grid_direction                # [G, K]
+                signal_group = to_device(np.ascontiguousarray(group.T), device)
                 signal_column = to_device(planar * first[0], device)
     else:
         response = detector.at(energy, detector_angle(omega, geometry, angle)) if K else np.zeros((G, 0))
-        direction = (weight * cos64)[None] * response * grid_t[:, None]          # [G, K]
-        signal_group, signal_channel = to_device(direction.T, device), None
+        direction = (weight * cos64)[None] * response * grid_direction          # [G, K]
+        if grid_channels is None:
+            signal_group, signal_channel = to_device(direction.T, device), None
+        else:
+            signal_group = None
+            signal_channel = to_device((direction[:, :, None] * grid_channels).transpose(1, 0, 2), device)
         planar_weight = to_device((weight * cos64)[:, None], device)
+    if row_weight is not None or pixel_septa:
+        # weights that vary along the rows: the groups cannot be summed in the emission
+        if signal_channel is None:
+            signal_channel = signal_group.reshape(K, G, 1).contiguous()
+        signal_group = signal_column = None
     chunk = max(1, int(chunk))
     ctx = DirectionSetContext(
         quadrature=quadrature, geometry=geometry, angle=float(angle), group_energy=energy, omega=to_device(omega, device),
@@ -175,7 +258,7 @@ def make_direction_context(quadrature: Quadrature, geometry: ConeGeometry, angle
         cell_width=to_device(quadrature.cell_width[kept], device), signal_group_weight=signal_group,
         signal_channel_weight=signal_channel, planar_weight=planar_weight,
         chunk_bounds=tuple((s, min(s + chunk, K)) for s in range(0, K, chunk)), image_shape=(Rd, Cd),
-        signal_column_weight=signal_column)
+        signal_column_weight=signal_column, signal_row_weight=row_weight, pixel_septa=pixel_septa, septa_kinds=kinds)
     ctx._omega64 = omega
     return ctx
 
@@ -194,6 +277,26 @@ def _blur(src: Tensor, dst: Tensor, lines: int, length: int, strides_in: tuple, 
     _lib.call("citrus_box_blur", src.data_ptr(), dst.data_ptr(), k, lines, length, *strides_in, *strides_out, None,
               height_sums.data_ptr(), cell_width.data_ptr(), axis, float(pitch), float(center_height),
               _lib.stream_handle(src.device))
+
+
+def _grid_signal_sum(context: DirectionSetContext, img: Tensor, s: int, e: int, strides: tuple, acc: Tensor,
+                     per_group: bool, stream) -> None:
+    """Signal of directions [s, e) behind a grid that varies over the panel (``citrus_grid_signal_sum``)."""
+    k, Rd, G, Cd = img.shape
+    w = context.signal_channel_weight[s:e].contiguous()                       # [k, G, Cd | 1]
+    rows = None if context.signal_row_weight is None else context.signal_row_weight[s:e].contiguous()
+    host = HostArgs()
+    septa = context.pixel_septa
+    theta_ch = [ps.theta_channels[:, s:e].contiguous() for ps in septa]       # kept alive for the call
+    ptrs = lambda ts: host.pointers([t.data_ptr() for t in ts]) if ts else None  # noqa: E731
+    _lib.call("citrus_grid_signal_sum", img.data_ptr(), k, G, Rd, Cd, *strides, w.data_ptr(), int(w.shape[-1]),
+              None if rows is None else rows.data_ptr(), len(septa), ptrs(theta_ch),
+              ptrs([ps.theta_pixels for ps in septa]), ptrs([ps.table for ps in septa]),
+              ptrs([ps.theta1_nodes for ps in septa]),
+              host.int64s([ps.theta1_nodes.numel() for ps in septa]) if septa else None,
+              ptrs([ps.theta2_nodes for ps in septa]),
+              host.int64s([ps.theta2_nodes.numel() for ps in septa]) if septa else None,
+              acc.data_ptr(), int(per_group), 1, stream)
 
 
 def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, phi_uncollided: Tensor,
@@ -259,7 +362,10 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
         head = (*fc.common(), f, deltas, fc.focal, fc.table.data_ptr(), fc.num_eta, fc.eta_lo, fc.eta_hi,
                 dirs.data_ptr(), k, tau.data_ptr(), None if traced is None else tau_mu.data_ptr(),
                 0 if traced is None else int(traced.shape[0]), mu.data_ptr())
-        tail = (heights.data_ptr(), context.signal_group_weight[s:e].contiguous().data_ptr() if flat_signal else None,
+        # every tensor whose address a call takes stays bound until the call is queued: a temporary's memory returns
+        # to the allocator when the expression ends, before the kernel reads it
+        group_weight = context.signal_group_weight[s:e].contiguous() if flat_signal else None
+        tail = (heights.data_ptr(), None if group_weight is None else group_weight.data_ptr(),
                 emission.data_ptr(), partial.data_ptr(), partial.numel(), sums.data_ptr(), stream)
         if EMISSION_FORM == "fused":
             _lib.call("citrus_attenuated_emission_moments", *head, Yk.data_ptr(), T.data_ptr(), N_sh, *tail)
@@ -280,10 +386,11 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
             blurred = torch.empty_like(rows_outer)  # channels: lines (row, channel-group) of Cd contiguous pixels
             _blur(rows_outer, blurred, Rd * C, Cd, (Rd * C * Cd, Cd, 1), (Rd * C * Cd, Cd, 1), k, sums, cw, 0,
                   geometry.delta_det_channel, center_height)
-        if signal_only and not flat_signal:
+        grid_sum = context.grid_varies_over_panel
+        if signal_only and not flat_signal and not grid_sum:
             single = torch.empty(k, Rd, Cd, device=device)
-            _lib.call("citrus_weighted_group_sum", blurred.data_ptr(),
-                      context.signal_channel_weight[s:e].contiguous().data_ptr(), k, Rd, G, Cd, Cd,
+            channel_weight = context.signal_channel_weight[s:e].contiguous()
+            _lib.call("citrus_weighted_group_sum", blurred.data_ptr(), channel_weight.data_ptr(), k, Rd, G, Cd, Cd,
                       single.data_ptr(), stream)
             image, C_img = single, 1
         else:
@@ -298,18 +405,24 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
             _lib.call("citrus_weighted_direction_sum", image.data_ptr(), k, 1, Rd, Cd, Rd * Cd, Rd * Cd, Cd, 1,
                       columns.data_ptr(), 1, Cd, acc.data_ptr(), 1, stream)
             continue
-        if signal_only:
+        img = image.view(k, Rd, C_img, Cd)  # rows-outer [k, Rd, G, Cd] seen as [k, G, Rd, Cd] through strides
+        strides = (Rd * C_img * Cd, Cd, C_img * Cd, 1)
+        if grid_sum:
+            _grid_signal_sum(context, img, s, e, strides, acc if signal_only else acc[2], not signal_only, stream)
+            if signal_only:
+                continue
+        elif signal_only:
             _lib.call("citrus_sum_directions", image.data_ptr(), k, Rd * Cd, Rd * Cd, acc.data_ptr(), 1, stream)
             continue
-        img = image.view(k, Rd, G, Cd)  # rows-outer [k, Rd, G, Cd] seen as [k, G, Rd, Cd] through strides
-        strides = (Rd * G * Cd, Cd, G * Cd, 1)
         ones = context.weight[s:e].reshape(k, 1, 1, 1).expand(k, G, 1, 1).contiguous()
         planar = context.planar_weight[s:e]
         planar = planar.reshape(k, 1, 1, -1).expand(k, G, 1, planar.shape[-1]).contiguous()
-        signal = (context.signal_channel_weight[s:e].reshape(k, G, 1, Cd).contiguous()
-                  if context.signal_channel_weight is not None
-                  else context.signal_group_weight[s:e].reshape(k, G, 1, 1).contiguous())
-        for j, w in enumerate((ones, planar, signal)):
+        weights = [ones, planar]
+        if not grid_sum:
+            weights.append(context.signal_channel_weight[s:e].reshape(k, G, 1, Cd).contiguous()
+                           if context.signal_channel_weight is not None
+                           else context.signal_group_weight[s:e].reshape(k, G, 1, 1).contiguous())
+        for j, w in enumerate(weights):
             _lib.call("citrus_weighted_direction_sum", img.data_ptr(), k, G, Rd, Cd, *strides, w.data_ptr(), 1,
                       w.shape[-1], acc[j].data_ptr(), 1, stream)
     if signal_only:
@@ -319,28 +432,72 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
 
 # ---- primary ---------------------------------------------------------------------------------------------------------
 
-def primary_path_lengths(projectors, rho: Tensor, grid: Grid, geometry: ConeGeometry, angle: float) -> Tensor:
-    """[M', Rd, Cd] density line integrals to the pixel centres (reference ``scatter_image.py:1368-1392``)."""
-    return projectors.primary_project(rho, grid, geometry, angle)
+def primary_subpixel_geometry(geometry: ConeGeometry, samples_per_pixel_axis: int) -> ConeGeometry:
+    """The panel with n times finer pixels on which the n^2 sub-rays of every pixel are traced: sub-pixel (i, j) of
+    pixel (r, c) is pixel (r n + i, c n + j) (reference ``scatter_image.py:1330-1348``)."""
+    n = int(samples_per_pixel_axis)
+    if n < 1:
+        raise ValueError("samples_per_pixel_axis must be >= 1")
+    if n == 1:
+        return geometry
+    return replace(geometry, num_det_rows=geometry.num_det_rows * n, num_det_channels=geometry.num_det_channels * n,
+                   delta_det_row=geometry.delta_det_row / n, delta_det_channel=geometry.delta_det_channel / n)
+
+
+def primary_samples_per_pixel_axis(projectors, samples_per_pixel_axis: Optional[int]) -> int:
+    """The given sub-pixel samples per axis, else the projector's own, else 1 (reference ``:1351-1365``)."""
+    n = (int(samples_per_pixel_axis) if samples_per_pixel_axis is not None
+         else int(getattr(projectors, "samples_per_pixel_axis", 1) or 1))
+    if n < 1:
+        raise ValueError("samples_per_pixel_axis must be >= 1")
+    return n
+
+
+def primary_path_lengths(projectors, rho: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
+                         samples_per_pixel_axis: Optional[int] = None) -> Tensor:
+    """[M', Rd n, Cd n] density line integrals to the pixel (or sub-pixel) centres, the sub-rays traced as the pixels
+    of the refined panel (reference ``scatter_image.py:1368-1392``)."""
+    n = primary_samples_per_pixel_axis(projectors, samples_per_pixel_axis)
+    fine = primary_subpixel_geometry(geometry, n)
+    if getattr(projectors, "samples_per_pixel_axis", None) is not None:  # the projector's own sub-sampling off
+        return projectors.primary_project(rho, grid, fine, angle, samples_per_pixel_axis=1)
+    return projectors.primary_project(rho, grid, fine, angle)
 
 
 def primary_from_path_lengths(library: MultigroupLibrary, path: Tensor, materials, geometry: ConeGeometry,
                               angle: float, source: SourceModel, detector: DetectorResponse,
                               grid_response: GridResponse) -> dict:
-    """Primary image from per-material line integrals, exact in energy (reference ``scatter_image.py:1419-1471``)."""
+    """Primary image from per-material line integrals [M', Rd n, Cd n], exact in energy (reference
+    ``scatter_image.py:1395-1471``): the fine-energy transmission, with the source's beam filter on every ray, is
+    averaged over the n x n sub-pixels of every pixel; the inverse square, the collimation and the responses are
+    evaluated at the pixel centres, the grid transmission at every pixel's grid angles."""
     device = path.device
-    T = group_transmission(library, path, materials)                          # [G, Rd, Cd]
+    Rd, Cd = geometry.image_shape
+    n = int(path.shape[1]) // Rd if path.dim() == 3 else 0
+    if n < 1 or tuple(path.shape[1:]) != (Rd * n, Cd * n):
+        raise ValueError(f"path must be [M', {Rd} n, {Cd} n] (n >= 1 sub-pixels per axis), got {tuple(path.shape)}")
+    r0 = np.asarray(geometry.source_position(angle))
+    filter_path = None
+    if source.has_filter:
+        sub = primary_subpixel_geometry(geometry, n).pixel_centers_np(angle)
+        filter_path = source.filter_path_np(sub - r0, geometry, angle)
+    T = group_transmission(library, path, materials,
+                           filter_path=None if filter_path is None else to_device(filter_path, device),
+                           filter_attenuation=source.filter_attenuation(library))         # [G, Rd n, Cd n]
+    if n > 1:
+        T = T.reshape(-1, Rd, n, Cd, n).mean(dim=(2, 4))
     pixels = geometry.pixel_centers_np(angle)
-    d = pixels - np.asarray(geometry.source_position(angle))
+    d = pixels - r0
     dist2 = (d * d).sum(-1)
     b = source.angular_weight_np(d, geometry, angle)
     omega_p = d / np.sqrt(dist2)[..., None]
     energy = library.group_energy
     theta0 = detector_angle(omega_p, geometry, angle, pixels)
+    grid_t = (grid_response.transmission_at(energy, omega_p, pixels, geometry, angle)
+              if grid_response.depends_on_angles else grid_response.at_energy(energy)[:, None, None])
     fluence_factor = to_device(b / dist2, device)
     planar_factor = to_device(b / dist2 * np.cos(theta0), device)
-    signal_factor = to_device((b / dist2 * np.cos(theta0))[None] * detector.at(energy, theta0)
-                              * grid_response.at_energy(energy)[:, None, None], device)
+    signal_factor = to_device((b / dist2 * np.cos(theta0))[None] * detector.at(energy, theta0) * grid_t, device)
     fluence = T * fluence_factor
     signal_per_group = T * signal_factor
     return {"fluence": fluence, "planar_fluence": T * planar_factor, "signal_per_group": signal_per_group,
@@ -348,11 +505,12 @@ def primary_from_path_lengths(library: MultigroupLibrary, path: Tensor, material
 
 
 def primary_image(library: MultigroupLibrary, rho: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
-                  source: SourceModel, projectors, detector: DetectorResponse, grid_response: GridResponse) -> dict:
+                  source: SourceModel, projectors, detector: DetectorResponse, grid_response: GridResponse,
+                  samples_per_pixel_axis: Optional[int] = None) -> dict:
     """Primary image of one view from the density maps (reference ``scatter_image.py:1474-1506``)."""
     present = present_materials(rho)
     traced = rho if present is None else rho[present]
-    path = primary_path_lengths(projectors, traced.contiguous(), grid, geometry, angle)
+    path = primary_path_lengths(projectors, traced.contiguous(), grid, geometry, angle, samples_per_pixel_axis)
     return primary_from_path_lengths(library, path, present, geometry, angle, source, detector, grid_response)
 
 

@@ -25,7 +25,7 @@ from .cross_sections import MultigroupLibrary, mu_t_volume, transfer_moments_vol
 from .geometry import ConeGeometry, Grid, resample_conservative
 from .quadrature import Quadrature, product_quadrature
 from .ray_tracing import GB300Projectors
-from .responses import DetectorResponse, GridResponse, SourceModel
+from .responses import DetectorResponse, GridResponse, SourceModel, group_averaged_responses
 from .scatter_image import (combined_scatter_image, make_direction_context, panel_direction_set, primary_image,
                             scatter_fraction)
 from .source_iteration import (SourceIterationResult, multiple_collision_source_moments, scatter_moments,
@@ -58,6 +58,7 @@ class SolverConfig:
     direction_chunk: int = 8
     dtype: str = "float32"
     moment_precision: str = "fp32"  # the spherical-harmonic products: "fp32" or "bf16x3" (tensor-core hi/lo split)
+    group_averaged_responses: bool = False  # the responses as their means over each group's fine energies
 
     def quadrature_points(self, fine_voxel_cm: float) -> int:
         """q = min(max(1, round(cell / spacing)), max(1, round(cell / voxel))) (reference ``config.py:130-144``)."""
@@ -85,6 +86,8 @@ class SolverConfig:
             raise ValueError("cone counts and direction_chunk must be >= 1")
         if self.dtype != "float32":
             raise ValueError("the GB300 path computes in float32 (the oracle is the float64 reference)")
+        if not isinstance(self.group_averaged_responses, bool):
+            raise ValueError(f"group_averaged_responses must be True or False, got {self.group_averaged_responses!r}")
 
 
 @dataclass(frozen=True, eq=False)
@@ -122,7 +125,8 @@ class ScatterSolver:
 
     def __init__(self, library: MultigroupLibrary, config: SolverConfig, geometry: ConeGeometry, projectors=None,
                  detector: Optional[DetectorResponse] = None, grid_response: Optional[GridResponse] = None,
-                 source: Optional[SourceModel] = None, device="cuda", direction_context_cache_size: int = 128):
+                 source: Optional[SourceModel] = None, device="cuda", direction_context_cache_size: int = 128,
+                 primary_samples_per_pixel_axis: Optional[int] = None):
         if detector is None or grid_response is None:
             raise TypeError("ScatterSolver needs a detector and a grid_response")
         config.validate()
@@ -143,6 +147,9 @@ class ScatterSolver:
         self.detector = detector
         self.grid_response = grid_response
         self.source = source if source is not None else SourceModel()
+        self._averaged_responses = None
+        # sub-pixel samples per axis of the primary (n^2 sub-rays per pixel); None: the projector's own, else 1
+        self.primary_samples_per_pixel_axis = primary_samples_per_pixel_axis
         self._sweep_contexts: dict = {}
         self._transport_grids: dict = {}
         self._cone_quadratures: dict = {}
@@ -211,8 +218,8 @@ class ScatterSolver:
         if ctx is not None and ctx.quadrature is quadrature:
             self._direction_contexts.move_to_end(key)
             return ctx
-        ctx = make_direction_context(quadrature, self.geometry, angle, self.detector, self.grid_response,
-                                     self.library, self.device, chunk=chunk)
+        ctx = make_direction_context(quadrature, self.geometry, angle, *self.responses(), self.library, self.device,
+                                     chunk=chunk)
         if self.direction_context_cache_size > 0:
             self._direction_contexts[key] = ctx
             while len(self._direction_contexts) > self.direction_context_cache_size:
@@ -332,7 +339,20 @@ class ScatterSolver:
 
     def primary(self, fields: MaterialFields, angle: float) -> dict:
         return primary_image(self.library, fields.rho_fine, fields.grid_fine, self.geometry, angle, self.source,
-                             self.projectors, self.detector, self.grid_response)
+                             self.projectors, *self.responses(),
+                             samples_per_pixel_axis=self.primary_samples_per_pixel_axis)
+
+    def responses(self) -> tuple:
+        """(detector, grid response) the solver evaluates: as given, or with ``config.group_averaged_responses`` their
+        means over each group's fine energies, computed once per library and responses (reference
+        ``scatter_solver.py:401-415``)."""
+        if not self.config.group_averaged_responses:
+            return self.detector, self.grid_response
+        inputs = (self.detector, self.grid_response, self.library)
+        cached = self._averaged_responses
+        if cached is None or any(a is not b for a, b in zip(cached[0], inputs)):
+            self._averaged_responses = cached = (inputs, group_averaged_responses(*inputs))
+        return cached[1]
 
     # ---- one view ------------------------------------------------------------------------------------------------
     @contextmanager

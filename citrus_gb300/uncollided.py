@@ -79,22 +79,39 @@ def _eta_range(library: MultigroupLibrary) -> tuple:
 
 # ---- uncollided fluence -------------------------------------------------------------------------------------------
 
-def source_weight(source: SourceModel, geometry: ConeGeometry, angle: float, points: Grid, device,
-                  divide_by_distance_squared: bool = True) -> Tensor:
-    """[V] b(Omega) / |r - r0|^2 at the centres of a point grid."""
+def source_field(source: SourceModel, geometry: ConeGeometry, angle: float, points: Grid, device,
+                 divide_by_distance_squared: bool = True) -> tuple:
+    """([V] b(Omega) / |r - r0|^2, [V] filter path in g/cm^2 or None) at the centres of a point grid (reference
+    ``source.py:368-430`` at ``uncollided.py:183-197``)."""
     host = HostArgs()
     ax = points.device_axes(device, torch.float64)
     out = torch.empty(points.num_voxels, device=device, dtype=torch.float32)
-    _lib.call("citrus_source_weight", host.doubles(source.field_args(geometry, angle)), None, ax[0].data_ptr(),
-              ax[1].data_ptr(), ax[2].data_ptr(), host.int64s(points.shape), points.num_voxels,
-              int(divide_by_distance_squared), out.data_ptr(), _lib.stream_handle(device))
-    return out
+    tables = source.device_tables(geometry, angle, device)
+    thickness = tables["thickness"]
+    path = None if thickness is None else torch.empty(points.num_voxels, device=device, dtype=torch.float32)
+    ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+    extras = tables["profile"] is not None or thickness is not None
+    _lib.call("citrus_source_field", host.doubles(source.field_args(geometry, angle)),
+              host.doubles(source.panel_args(geometry)) if extras else None, ptr(tables["profile"]), ptr(thickness),
+              0 if thickness is None else int(thickness.shape[0]), source.filter_density, ptr(tables["off_nodes"]),
+              ptr(tables["off_values"]), 0 if tables["off_nodes"] is None else int(tables["off_nodes"].numel()), None,
+              ax[0].data_ptr(), ax[1].data_ptr(), ax[2].data_ptr(), host.int64s(points.shape), points.num_voxels,
+              int(divide_by_distance_squared), out.data_ptr(), ptr(path), _lib.stream_handle(device))
+    return out, path
+
+
+def source_weight(source: SourceModel, geometry: ConeGeometry, angle: float, points: Grid, device,
+                  divide_by_distance_squared: bool = True) -> Tensor:
+    """[V] b(Omega) / |r - r0|^2 at the centres of a point grid."""
+    return source_field(source, geometry, angle, points, device, divide_by_distance_squared)[0]
 
 
 def group_transmission(library: MultigroupLibrary, path: Tensor, materials: Optional[Sequence[int]] = None,
-                       factor: Optional[Tensor] = None) -> Tensor:
+                       factor: Optional[Tensor] = None, filter_path: Optional[Tensor] = None,
+                       filter_attenuation=None) -> Tensor:
     """[G, ...] fine-energy group transmission of line integrals path [M', ...] in g/cm^2, times ``factor`` [...]
-    (reference ``cross_sections.py:797-883``)."""
+    (reference ``cross_sections.py:797-883``); a beam filter adds ``filter_attenuation[e] * filter_path`` to each
+    exponent (``transmission_kernels.py:187-275``)."""
     device = path.device
     Mp = int(path.shape[0])
     spatial = tuple(path.shape[1:])
@@ -102,6 +119,8 @@ def group_transmission(library: MultigroupLibrary, path: Tensor, materials: Opti
     fine_mu = library.fine_mu_t if materials is None else library.fine_mu_t[list(materials)]
     if fine_mu.shape[0] != Mp:
         raise ValueError(f"path has {Mp} materials, the library {fine_mu.shape[0]}")
+    if (filter_path is None) != (filter_attenuation is None):
+        raise ValueError("filter_path and filter_attenuation go together")
     key = ("fine", None if materials is None else tuple(int(m) for m in materials), str(device))
     cached = library._device_cache.get(key)
     if cached is None:
@@ -114,9 +133,15 @@ def group_transmission(library: MultigroupLibrary, path: Tensor, materials: Opti
     G = library.num_groups
     out = torch.empty(G, P, device=device, dtype=torch.float32)
     fac = None if factor is None else factor.to(torch.float32).reshape(P).contiguous()
+    fp = fmu = None
+    if filter_path is not None:
+        fp = filter_path.to(device=device, dtype=torch.float32).reshape(P).contiguous()
+        fmu = torch.as_tensor(np.asarray(filter_attenuation, dtype=np.float64), dtype=torch.float32).to(device)
+        if fmu.numel() != w.numel():
+            raise ValueError(f"filter_attenuation has {fmu.numel()} energies, the library {w.numel()}")
     _lib.call("citrus_group_transmission", p.data_ptr(), Mp, P, mu.data_ptr(), w.data_ptr(), g.data_ptr(),
-              int(w.numel()), G, None, None, None if fac is None else fac.data_ptr(), out.data_ptr(),
-              _lib.stream_handle(device))
+              int(w.numel()), G, None if fp is None else fp.data_ptr(), None if fmu is None else fmu.data_ptr(),
+              None if fac is None else fac.data_ptr(), out.data_ptr(), _lib.stream_handle(device))
     return out.reshape(G, *spatial)
 
 
@@ -132,8 +157,9 @@ def uncollided_path_lengths(projectors, rho: Tensor, grid: Grid, geometry: ConeG
 def uncollided_from_path_lengths(library: MultigroupLibrary, path_lengths: Tensor, materials, points: Grid,
                                  geometry: ConeGeometry, angle: float, source: SourceModel) -> Tensor:
     """[G, *points.shape] phi_UC = b / |r - r0|^2 sum_e w_e exp(-sum_m P_m mu_m(e)) (reference ``uncollided.py:160-197``)."""
-    factor = source_weight(source, geometry, angle, points, path_lengths.device)
-    return group_transmission(library, path_lengths, materials, factor)
+    factor, filter_path = source_field(source, geometry, angle, points, path_lengths.device)
+    return group_transmission(library, path_lengths, materials, factor, filter_path,
+                              source.filter_attenuation(library) if filter_path is not None else None)
 
 
 def uncollided_fluence(library: MultigroupLibrary, rho: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
@@ -239,9 +265,10 @@ def first_collision_means_at_directions(library: MultigroupLibrary, rho: Tensor,
         out = torch.empty(expected, device=a.device)
     elif out.numel() != K * a.V * a.G or not out.is_contiguous() or out.dtype != torch.float32:
         raise ValueError(f"out must be a contiguous float32 tensor of {K * a.V * a.G} elements")
+    scale, beta = correction.scale.contiguous(), correction.beta.contiguous()  # bound until the call is queued
     _lib.call("citrus_first_collision_means", a.G, a.axes.data_ptr(), a.dims, a.focal, om.data_ptr(), K,
-              correction.scale.contiguous().data_ptr(), correction.beta.contiguous().data_ptr(),
-              correction.cache.data_ptr(), index.data_ptr(), out.data_ptr(), a.V * a.G, a.stream)
+              scale.data_ptr(), beta.data_ptr(), correction.cache.data_ptr(), index.data_ptr(), out.data_ptr(),
+              a.V * a.G, a.stream)
     return out.view(expected)
 
 

@@ -231,6 +231,21 @@ int citrus_source_weight(const double* field, const double* points, const double
                          const double* axis_z, const int64_t* point_dims, int64_t num_points,
                          int32_t divide_by_distance_squared, float* out, void* stream);
 
+/* The same weight with the rest of the source model: b(Omega) is the field weight (1 inside the field, past its edge
+ * the off-focal fraction of the distance to the field rectangle, linear between off_focal_nodes [n] with values
+ * off_focal_values [n], 0 past the last node; no table: 0) times the emission profile [rows, channels] interpolated
+ * bilinearly at the ray's panel point and held at the outermost pixel centres; with a filter thickness
+ * [thickness_rows = 1 | rows, channels] in cm, filter_path_out [P] receives filter_density * thickness interpolated
+ * the same way (g/cm^2). panel (host double [6]) = rows, channels, row pitch, channel pitch, row offset, channel
+ * offset. All tables are float64 device arrays; null profile, thickness and off-focal nodes leave them out.
+ * Replaces SourceModel.angular_weight / filter_path (source.py:289-430) with panel_interpolate (source.py:484-510). */
+int citrus_source_field(const double* field, const double* panel, const double* profile, const double* thickness,
+                        int64_t thickness_rows, double filter_density, const double* off_focal_nodes,
+                        const double* off_focal_values, int64_t num_off_focal, const double* points,
+                        const double* axis_x, const double* axis_y, const double* axis_z, const int64_t* point_dims,
+                        int64_t num_points, int32_t divide_by_distance_squared, float* out, float* filter_path_out,
+                        void* stream);
+
 /* Shared arguments of the first-collision kernels: rho [M, V] densities on the point grid, phi [G, V] uncollided
  * fluence, axes = float32 point coordinates x [cols], y [rows], z [slices] back to back, point_dims (host) = rows,
  * cols, slices, focal_spot (host double [3]), table [M, N_eta, G_out, G_in] per-steradian transfer (zero for
@@ -335,6 +350,23 @@ int citrus_weighted_direction_sum(const float* image, int64_t num_directions, in
                                   int64_t cols, int64_t is_k, int64_t is_g, int64_t is_r, int64_t is_c,
                                   const float* weights, int64_t weight_rows, int64_t weight_cols, float* accumulator,
                                   int32_t accumulate, void* stream);
+
+/* Signal behind an anti-scatter grid that varies over the panel: accumulator[g, r, c] (per_group) or
+ * accumulator[r, c] (+)= sum_k W image[k, g, r, c] (image element strides), with
+ * W = weights[k, g, c | 0] * row_weights[k, g, r] (null: 1) * prod_s T_s(g, theta1_s, theta2_s) where, for each of
+ * num_septa <= 2 sets of septa, theta_i = theta_channels_s[i, k, c] + theta_pixels_s[i, r, c] (float32, [2, K, cols]
+ * and [2, rows, cols]) and T_s is tables_s [G, T1, T2] interpolated bilinearly at |theta1|, |theta2| in the nodes
+ * theta1_nodes_s [T1], theta2_nodes_s [T2], clamped to the end nodes. The septa arguments are host arrays of
+ * num_septa device pointers (and host counts). groups <= 32.
+ * Replaces DirectionSetContext.pixel_signal_weight and the signal accumulation with _PixelGrid and signal_row_weight
+ * (scatter_image.py:340-389, 437-486, 1290-1313). */
+int citrus_grid_signal_sum(const float* image, int64_t num_directions, int64_t groups, int64_t rows, int64_t cols,
+                           int64_t is_k, int64_t is_g, int64_t is_r, int64_t is_c, const float* weights,
+                           int64_t weight_cols, const float* row_weights, int64_t num_septa,
+                           const float* const* theta_channels, const float* const* theta_pixels,
+                           const float* const* tables, const float* const* theta1_nodes, const int64_t* num_theta1,
+                           const float* const* theta2_nodes, const int64_t* num_theta2, float* accumulator,
+                           int32_t per_group, int32_t accumulate, void* stream);
 
 /* accumulator[p] (+)= sum_k image[k * stride_k + p], directions in order (scatter_image.py:1289-1319). */
 int citrus_sum_directions(const float* image, int64_t num_directions, int64_t pixels, int64_t stride_k,

@@ -13,7 +13,7 @@ import math
 import numpy as np
 
 from citrus_gb300.quadrature import real_spherical_harmonics
-from oracle import physics, siddon
+from oracle import physics, responses, siddon
 
 
 def box_matrix(N, w):
@@ -48,8 +48,10 @@ def direction_weights(omega, weight, geometry, angle, detector, group_energy):
 
 
 def combined_image(library, rho_q, phi_uc, grid_q, q, T, L, geometry, angle, omega_set, weight_set, cell_width_set,
-                   mu_t_coarse, detector, footprint=True):
-    """fluence, planar, signal_per_group [G, Rd, Cd] and signal [Rd, Cd] of one view (scatter_image.py:1141-1323)."""
+                   mu_t_coarse, detector, footprint=True, grid=None):
+    """fluence, planar, signal_per_group [G, Rd, Cd] and signal [Rd, Cd] of one view (scatter_image.py:1141-1323);
+    ``grid`` (a GridResponse) weights the signal with its transmission at every direction and pixel, after the
+    footprint blur (scatter_image.py:1281-1313)."""
     keep, w, planar_w, signal_w = direction_weights(omega_set, weight_set, geometry, angle, detector,
                                                     library.group_energy)
     omega, cw = omega_set[keep], cell_width_set[keep]
@@ -89,7 +91,10 @@ def combined_image(library, rho_q, phi_uc, grid_q, q, T, L, geometry, angle, ome
         image = np.einsum("krj,kgjc->kgrc", box_matrix(Rd, wr), image)
     fluence = np.einsum("kgrc,k->grc", image, w)
     planar = np.einsum("kgrc,kc->grc", image, np.broadcast_to(planar_w, (k, Cd)))
-    signal_pg = np.einsum("kgrc,kgc->grc", image, np.broadcast_to(signal_w, (k, G, Cd)))
+    signal = np.broadcast_to(signal_w, (k, G, Cd))[:, :, None, :]
+    if grid is not None:
+        signal = signal * responses.grid_transmission(grid, omega, geometry, angle, library.group_energy)
+    signal_pg = np.einsum("kgrc,kgrc->grc", image, np.broadcast_to(signal, image.shape))
     return {"fluence": fluence, "planar_fluence": planar, "signal_per_group": signal_pg, "signal": signal_pg.sum(0)}
 
 

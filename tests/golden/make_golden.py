@@ -467,6 +467,134 @@ def state_store_codec():
     save("state_store_codec", phi=phi, decoded=store.get(0), stored=store._data[0].float(), scale=store._scale[0])
 
 
+def _filter_mass_attenuation(e):
+    """A synthetic aluminium-like total mass attenuation in cm^2/g (the photon data is not part of the fixtures)."""
+    e = np.asarray(e, dtype=np.float64)
+    return 0.16 + 4.0 * (e / 30.0) ** -2.8
+
+
+@case
+def grid_and_source():
+    """The reference's anti-scatter grid and source model on the scatter-step path: the focused 1-D grid table (its
+    geometric septum-shadow model with its own lead attenuation), grid angles and transmissions for flat and curved
+    panels (septa along the channels and the rows, focused, unfocused and at a shorter focal distance, crossed), the
+    collapsed-cone image behind the grid for the seven panel/septa routes of its own scatter-image test, and the
+    uncollided fluence and primary with an emission profile, an off-focal table and a beam filter. The filter's mass
+    attenuation is the synthetic ``_filter_mass_attenuation`` (patched into the reference's fine-energy lookup, since
+    the photon data is not read here)."""
+    from dataclasses import replace
+    import citrus.scatter_solver.source as ref_source
+    from citrus.scatter_solver.angular_quadrature import scatter_source_moments
+    from citrus.scatter_solver.cross_sections import Material, mu_t_volume, transfer_moments_volume
+    from citrus.scatter_solver.detector import (DetectorResponse, focused_1d_grid, grid_angles,
+                                                lead_mass_attenuation)
+    from citrus.scatter_solver.geometry import ConeGeometry, Grid
+    from citrus.scatter_solver.ray_tracing import SiddonProjectors
+    from citrus.scatter_solver.scatter_image import (combined_scatter_image, make_direction_context,
+                                                     panel_direction_set, primary_image)
+    from citrus.scatter_solver.source import SourceModel, bowtie_emission_profile
+    from citrus.scatter_solver.uncollided import DENSE, uncollided_fluence
+
+    g = torch.Generator().manual_seed(31)
+    energies = np.arange(10.0, 150.1, 5.0)
+    grid = focused_1d_grid(energies=energies)
+    arrays = dict(grid_energy=grid.energy_kev, grid_theta1=grid.theta1_rad, grid_theta2=grid.theta2_rad,
+                  grid_table=grid.transmission, grid_focal=np.array(grid.focal_distance_cm),
+                  lead_mu=lead_mass_attenuation(energies))
+    # grid angles and transmissions
+    omegas = torch.nn.functional.normalize(torch.randn(6, 3, generator=g, dtype=F64), dim=-1)
+    arrays["angles_omega"] = omegas
+    e_query = torch.tensor([18.0, 47.5, 93.2, 140.0], dtype=F64)
+    arrays["angles_energy"] = e_query
+    for curved in (False, True):
+        geo = ConeGeometry(100.0, 150.0, 5, 7, 4.0, 4.0, det_row_offset=1.0, use_curved_detector=curved)
+        pix = geo.pixel_centers(0.9, dtype=F64)
+        pre = "curved" if curved else "flat"
+        # the primary directions turned away from the normal in both panel axes, so every angle is nonzero
+        for septa in ("channels", "rows"):
+            for focal, fname in ((None, "default"), (math.inf, "unfocused"), (120.0, "f120")):
+                t1, t2 = grid_angles(omegas, pix, geo, 0.9, focal, septa)
+                arrays[f"angles_{pre}_{septa}_{fname}_theta1"] = t1
+                arrays[f"angles_{pre}_{septa}_{fname}_theta2"] = t2
+            sep = replace(grid, septa_along=septa)
+            arrays[f"transmission_{pre}_{septa}"] = sep.transmission_at(e_query, omegas, pix, geo, 0.9)
+        crossed = replace(grid, crossed=replace(grid, septa_along="rows"))
+        arrays[f"transmission_{pre}_crossed"] = crossed.transmission_at(e_query, omegas, pix, geo, 0.9)
+    # the image behind the grid (the scatter-image test's routes, on the small image setup)
+    library = reference_library(small_spectral_library())
+    L = 2
+    grid_q = Grid((6, 6, 4), 2.0)
+    q = 2
+    grid_c = grid_q.coarsen(q)
+    rho = torch.rand(2, *grid_q.shape, generator=g, dtype=F64) * torch.tensor([1.0, 0.5], dtype=F64)[:, None, None,
+                                                                                                         None]
+    rho_c = rho.reshape(2, 3, 2, 3, 2, 2, 2).mean(dim=(2, 4, 6))
+    mu_c = mu_t_volume(library, rho_c)
+    phi_coll = torch.rand(library.num_groups, (L + 1) ** 2, *grid_c.shape, generator=g, dtype=F64) * 1e-4
+    T = scatter_source_moments(transfer_moments_volume(library, rho_c)[:, :, :L + 1], phi_coll)
+    e, th, table = scintillator_table()
+    det = DetectorResponse(torch.as_tensor(e), torch.as_tensor(th), torch.as_tensor(table))
+    arrays.update(image_rho=rho, image_T=T)
+    along_rows = replace(grid, septa_along="rows")
+    crossed = replace(grid, crossed=along_rows)
+    routes = {"flat_rows": (False, grid), "flat_channels": (False, along_rows), "flat_crossed": (False, crossed),
+              "curved_rows": (True, along_rows), "curved_pixel": (True, grid), "curved_crossed": (True, crossed)}
+    proj = SiddonProjectors(backend="torch")
+    for name, (curved, grid_response) in routes.items():
+        geo = ConeGeometry(50.0, 80.0, 10, 14, 1.5, 1.5, det_channel_offset=0.4, use_curved_detector=curved)
+        angle = 0.8
+        phi = uncollided_fluence(library, rho, grid_q, geo, angle, SourceModel(), proj)
+        cone = panel_direction_set(geo, angle, (3, 6), max_polar_angle=grid_c, dtype=F64)
+        ctx = make_direction_context(cone, geo, angle, det, grid_response, library, "cpu", F64, chunk=5)
+        full = combined_scatter_image(library, rho, phi, grid_q, q, T, L, geo, angle, cone, mu_c, proj, det,
+                                      grid_response, ctx, pairs=DENSE, grid_coarse=grid_c)
+        sig = combined_scatter_image(library, rho, phi, grid_q, q, T, L, geo, angle, cone, mu_c, proj, det,
+                                     grid_response, ctx, pairs=DENSE, grid_coarse=grid_c,
+                                     signal_only=True)["signal"]
+        prim = primary_image(library, rho, grid_q, geo, angle, SourceModel(), proj, det, grid_response)
+        arrays.update({f"image_{name}_phi": phi, f"image_{name}_signal_pg": full["signal_per_group"],
+                       f"image_{name}_signal": full["signal"], f"image_{name}_signal_only": sig,
+                       f"image_{name}_fluence": full["fluence"], f"image_{name}_primary": prim["signal"]})
+        if name == "flat_rows":
+            arrays.update(image_cone_omega=cone.omega, image_cone_weight=cone.weight, image_cone_width=cone.cell_width)
+    # the responses averaged over each group's fine energies (SolverConfig.group_averaged_responses)
+    from citrus.scatter_solver.detector import group_averaged_responses
+    avg_det, avg_grid = group_averaged_responses(det, crossed, library)
+    arrays.update(avg_det_energy=avg_det.energy_kev, avg_det_table=avg_det.response,
+                  avg_grid_energy=avg_grid.energy_kev, avg_grid_table=avg_grid.transmission,
+                  avg_crossed_energy=avg_grid.crossed.energy_kev, avg_crossed_table=avg_grid.crossed.transmission)
+    # the source model: emission profile, off-focal table and beam filter
+    filter_material = Material("filter", 2.7, "Al")
+    ref_source._fine_attenuation = lambda energies, key, definition: torch.as_tensor(
+        _filter_mass_attenuation(energies.detach().cpu().numpy()), dtype=key[4]).to(key[3])
+    arrays["filter_mu"] = _filter_mass_attenuation(library.fine_energy)
+    for curved in (False, True):
+        pre = "curved" if curved else "flat"
+        geo = ConeGeometry(50.0, 80.0, 10, 14, 1.5, 1.5, det_channel_offset=0.4, use_curved_detector=curved)
+        profile = bowtie_emission_profile(geo, 0.3)
+        profile = profile * (1.0 + 0.05 * torch.arange(10, dtype=F64))[:, None]
+        thickness = 0.1 + 0.02 * torch.arange(14, dtype=F64) ** 1.5
+        source = SourceModel(emission_profile=profile, field_margin_channels_cm=0.5, field_margin_rows_cm=0.25,
+                             off_focal_distance_cm=[0.0, 1.0, 3.0], off_focal_fraction=[0.3, 0.1, 0.02],
+                             filter_material=filter_material, filter_thickness_cm=thickness)
+        arrays.update({f"source_{pre}_profile": profile, f"source_{pre}_thickness": thickness})
+        big = Grid((8, 10, 6), 3.0)  # wider than the field, so points see the margins and the off-focal table
+        rho_b = torch.rand(2, *big.shape, generator=g, dtype=F64) * torch.tensor([1.0, 0.4], dtype=F64)[:, None,
+                                                                                                          None, None]
+        arrays[f"source_{pre}_rho"] = rho_b
+        arrays[f"source_{pre}_phi"] = uncollided_fluence(library, rho_b, big, geo, 0.8, source, proj)
+        d = big.center_coordinates(dtype=F64).reshape(-1, 3) - torch.tensor(geo.source_position(0.8), dtype=F64)
+        arrays[f"source_{pre}_b"] = source.angular_weight(d, geo, 0.8)
+        arrays[f"source_{pre}_filter_path"] = source.filter_path(d, geo, 0.8)
+        prim = primary_image(library, rho_b, big, geo, 0.8, source, proj, det, grid)
+        arrays[f"source_{pre}_primary"] = prim["signal"]
+        arrays[f"source_{pre}_primary_fluence"] = prim["fluence"]
+        # 2 x 2 sub-rays per pixel: the fine-energy transmission (filter included) averaged over the sub-pixels
+        prim2 = primary_image(library, rho_b, big, geo, 0.8, source, proj, det, grid, samples_per_pixel_axis=2)
+        arrays[f"source_{pre}_primary_n2"] = prim2["signal"]
+    save("grid_and_source", **arrays)
+
+
 @case
 def library_file():
     """A library written by the reference's own ``MultigroupLibrary.save`` (``torch.save`` of a dict of every field),
