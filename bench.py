@@ -636,7 +636,8 @@ STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_atte
               "citrus_downstream_cumulative": downstream_bytes,
               "citrus_sweep_persistent": sweep_bytes, "citrus_sweep_persistent_config": sweep_bytes,
               "citrus_sweep_tiled": tiled_sweep_bytes,
-              "citrus_oblique_project": None, "citrus_box_blur": None, "citrus_small_k_gemm": None,
+              "citrus_oblique_project": None, "citrus_oblique_project_scratch": None, "citrus_box_blur": None,
+              "citrus_small_k_gemm": None,
               "citrus_small_k_gemm_config": None, "citrus_small_k_gemm_bf16x3": None, "citrus_first_collision_moments": None,
               "citrus_first_collision_means": None, "citrus_source_expansion_first": None,
               "citrus_first_collision_correction": None, "citrus_scattering_moments": None}

@@ -42,6 +42,7 @@ SIGNATURES = {
     "citrus_trace_from_source": [P, I64, P, P, P, P, P, P, P, P, I64, P, P],
     "citrus_downstream_cumulative": [P, I64, P, P, P, P, I64, P, F64, P, I64, I64, I64, P, I64, P],
     "citrus_oblique_project": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P],
+    "citrus_oblique_project_scratch": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P, I64, P],
     "citrus_group_transmission": [P, I64, I64, P, P, P, I64, I64, P, P, P, P, P],
     "citrus_source_weight": [P, P, P, P, P, P, I64, I32, P, P],
     "citrus_source_field": [P, P, P, P, I64, F64, P, P, I64, P, P, P, P, P, I64, I32, P, P, P],
@@ -65,6 +66,7 @@ SIGNATURES = {
     "citrus_conv3d_forward_config": [P, I64, P, I64, I32, P, P, P, I64, I64, I64, I64, I64, I32, I32, I32, P, P],
     "citrus_conv3d_backward_input_config": [P, I64, P, P, I64, P, P, I64, I64, I64, I64, I64, I32, I32, P, P],
     "citrus_conv3d_weight_grad_splits": [I64, I64, I64, I64, I64, I64, I64, I32],
+    "citrus_oblique_scratch_bytes": [I64],
     "citrus_conv3d_backward_weight": [P, I64, P, I64, P, I64, I32, P, P, I64, I64, I64, I64, I32, P, I64, P],
     "citrus_avg_pool2": [P, P, I64, I64, I64, I64, P],
     "citrus_avg_pool2_backward": [P, P, P, I32, I64, I64, I64, I64, P],
@@ -97,6 +99,7 @@ def library() -> ctypes.CDLL:
         lib.citrus_last_error_string.restype = ctypes.c_char_p
         lib.citrus_launch_count.restype = ctypes.c_int64
         lib.citrus_conv3d_weight_grad_splits.restype = ctypes.c_int64
+        lib.citrus_oblique_scratch_bytes.restype = ctypes.c_int64
         _LIBRARY = lib
     return _LIBRARY
 

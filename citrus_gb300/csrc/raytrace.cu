@@ -810,35 +810,60 @@ __global__ void __launch_bounds__(kThreads) downstream_lattice_kernel(Box b, con
 // (ray_setup_pair), and in float64 for a line within its tolerances of a face, an edge or a voxel plane: a line that
 // grazes a face of the box is inside or outside exactly as in float64, where a float32 rounding of the pixel centre
 // could move it onto the face and integrate a whole slice.
+// The float64 constants of direction k and their float pairs (the divisions and the square root of the set-up).
+__device__ __forceinline__ void oblique_direction(const Box& b, const float* __restrict__ omegas, int k, double cx,
+                                                  double cy, double cz, double half, DirConst& dc, DirPair& dp) {
+  dc.w[0] = omegas[3 * k];
+  dc.w[1] = omegas[3 * k + 1];
+  dc.w[2] = omegas[3 * k + 2];
+  const double sq = add_rn(add_rn(mul_rn(dc.w[0], dc.w[0]), mul_rn(dc.w[1], dc.w[1])), mul_rn(dc.w[2], dc.w[2]));
+  dc.h = half / sqrt(sq);
+  dc.inv_w2 = 1.0 / sq;
+  for (int a = 0; a < 3; ++a) {
+    dc.d[a] = mul_rn(2.0 * dc.h, dc.w[a]);
+    dc.inv_d[a] = dc.d[a] != 0 ? 1.0 / dc.d[a] : 0.0;
+    dc.hi[a] = add_rn(b.lo[a], mul_rn(b.delta[a], (double)b.n[a]));
+  }
+  const double c[3] = {cx, cy, cz};
+  make_dir_pair(b, dc, c, dp);
+}
+
+// One thread per direction: the constants every block of that direction reads (float64 on this GPU runs at a small
+// fraction of float32, and a block per 128 pixels would otherwise repeat them hundreds of times per direction)
+__global__ void oblique_setup_kernel(Box b, const float* __restrict__ omegas, int K, double cx, double cy, double cz,
+                                     double half, DirConst* __restrict__ dcs, DirPair* __restrict__ dps) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  DirConst dc;
+  DirPair dp;
+  oblique_direction(b, omegas, k, cx, cy, cz, half, dc, dp);
+  dcs[k] = dc;
+  dps[k] = dp;
+}
+
 template <int kC>
 __global__ void __launch_bounds__(kThreads) oblique_kernel(Box b, const float* __restrict__ vol, int C,
                                                            int64_t field_stride, const float* __restrict__ omegas,
                                                            const double* __restrict__ pixels, int64_t P, double cx,
                                                            double cy, double cz, double half,
                                                            float* __restrict__ out, int64_t os_k, int64_t os_c,
-                                                           int64_t os_r, int64_t os_col, int64_t cols) {
+                                                           int64_t os_r, int64_t os_col, int64_t cols,
+                                                           const DirConst* __restrict__ dcs,
+                                                           const DirPair* __restrict__ dps) {
   const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int k = blockIdx.y;
-  // the direction's constants, once per block (the block shares the direction): float64 on this GPU runs at a small
-  // fraction of float32, so every division of the set-up is made here rather than per ray
+  // the direction's constants: from the set-up kernel's table when given, else formed once per block by thread 0
   __shared__ DirConst s_dc;
   __shared__ DirPair s_dp;
-  if (threadIdx.x == 0) {
-    DirConst dc;
-    dc.w[0] = omegas[3 * k];
-    dc.w[1] = omegas[3 * k + 1];
-    dc.w[2] = omegas[3 * k + 2];
-    const double sq = add_rn(add_rn(mul_rn(dc.w[0], dc.w[0]), mul_rn(dc.w[1], dc.w[1])), mul_rn(dc.w[2], dc.w[2]));
-    dc.h = half / sqrt(sq);
-    dc.inv_w2 = 1.0 / sq;
-    for (int a = 0; a < 3; ++a) {
-      dc.d[a] = mul_rn(2.0 * dc.h, dc.w[a]);
-      dc.inv_d[a] = dc.d[a] != 0 ? 1.0 / dc.d[a] : 0.0;
-      dc.hi[a] = add_rn(b.lo[a], mul_rn(b.delta[a], (double)b.n[a]));
+  if (dcs != nullptr) {
+    constexpr int nc = sizeof(DirConst) / 4, np = sizeof(DirPair) / 4;
+    static_assert(sizeof(DirConst) % 4 == 0 && sizeof(DirPair) % 4 == 0, "4-byte words");
+    for (int i = threadIdx.x; i < nc + np; i += kThreads) {
+      if (i < nc) reinterpret_cast<int*>(&s_dc)[i] = reinterpret_cast<const int*>(dcs + k)[i];
+      else reinterpret_cast<int*>(&s_dp)[i - nc] = reinterpret_cast<const int*>(dps + k)[i - nc];
     }
-    s_dc = dc;
-    const double c[3] = {cx, cy, cz};
-    make_dir_pair(b, dc, c, s_dp);
+  } else if (threadIdx.x == 0) {
+    oblique_direction(b, omegas, k, cx, cy, cz, half, s_dc, s_dp);
   }
   __syncthreads();
   if (p >= P) return;
@@ -985,15 +1010,24 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
   return launch_status("citrus_downstream_cumulative");
 }
 
-extern "C" int citrus_oblique_project(const float* field, int64_t channels, int64_t field_stride, const double* box,
-                                      const int64_t* dims, const float* omegas, int64_t num_directions,
-                                      const double* pixels, int64_t num_rows, int64_t num_cols, float* out,
-                                      int64_t os_k, int64_t os_c, int64_t os_r, int64_t os_col, void* stream) {
+extern "C" int64_t citrus_oblique_scratch_bytes(int64_t num_directions) {
+  return num_directions <= 0 ? 0 : num_directions * (int64_t)(sizeof(DirConst) + sizeof(DirPair)) + 16;
+}
+
+extern "C" int citrus_oblique_project_scratch(const float* field, int64_t channels, int64_t field_stride,
+                                              const double* box, const int64_t* dims, const float* omegas,
+                                              int64_t num_directions, const double* pixels, int64_t num_rows,
+                                              int64_t num_cols, float* out, int64_t os_k, int64_t os_c, int64_t os_r,
+                                              int64_t os_col, void* direction_scratch, int64_t scratch_bytes,
+                                              void* stream) {
   int status = check_common(field, channels, box, dims, out);
   if (status) return status;
   CITRUS_REQUIRE(omegas && pixels, "citrus_oblique_project: null directions or pixels");
   CITRUS_REQUIRE(num_directions >= 0 && num_directions <= 65535 && num_rows >= 0 && num_cols >= 1,
                  "citrus_oblique_project: bad sizes");
+  CITRUS_REQUIRE(direction_scratch == nullptr || scratch_bytes >= citrus_oblique_scratch_bytes(num_directions),
+                 "citrus_oblique_project: the direction scratch holds %lld bytes, needs %lld",
+                 (long long)scratch_bytes, (long long)citrus_oblique_scratch_bytes(num_directions));
   const int64_t num_pixels = num_rows * num_cols;
   if (num_directions == 0 || num_pixels == 0) return CITRUS_OK;
   const Box b = make_box(box, dims);
@@ -1005,9 +1039,27 @@ extern "C" int citrus_oblique_project(const float* field, int64_t channels, int6
   }
   const double half = 0.5 * sqrt(diag2) * (1 + 1e-6) + 1e-6;
   const int C = (int)channels;
+  DirConst* dcs = nullptr;
+  DirPair* dps = nullptr;
+  if (direction_scratch != nullptr) {  // 16-byte aligned tables: the constants of every direction, then their pairs
+    const uintptr_t base = ((uintptr_t)direction_scratch + 15) & ~(uintptr_t)15;
+    dcs = reinterpret_cast<DirConst*>(base);
+    dps = reinterpret_cast<DirPair*>(base + num_directions * sizeof(DirConst));
+    oblique_setup_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, as_stream(stream)>>>(
+        b, omegas, (int)num_directions, center[0], center[1], center[2], half, dcs, dps);
+    note_launches();
+  }
   dim3 grid((unsigned)cdiv(num_pixels, kThreads), (unsigned)num_directions);
   CITRUS_CHANNEL_DISPATCH(C, oblique_kernel, grid, as_stream(stream), b, field, C, field_stride, omegas, pixels,
                           num_pixels, center[0], center[1], center[2], half, out, os_k, os_c, os_r, os_col,
-                          num_cols)
+                          num_cols, dcs, dps)
   return launch_status("citrus_oblique_project");
+}
+
+extern "C" int citrus_oblique_project(const float* field, int64_t channels, int64_t field_stride, const double* box,
+                                      const int64_t* dims, const float* omegas, int64_t num_directions,
+                                      const double* pixels, int64_t num_rows, int64_t num_cols, float* out,
+                                      int64_t os_k, int64_t os_c, int64_t os_r, int64_t os_col, void* stream) {
+  return citrus_oblique_project_scratch(field, channels, field_stride, box, dims, omegas, num_directions, pixels,
+                                        num_rows, num_cols, out, os_k, os_c, os_r, os_col, nullptr, 0, stream);
 }

@@ -245,7 +245,9 @@ class GB300Projectors:
             raise ValueError(f"out must be [K, C, Rd, Cd] = {(K, C, Rd, Cd)}, got {tuple(out.shape)}")
         host = HostArgs()
         box, dims = _grid_args(host, grid)
-        _lib.call("citrus_oblique_project", vol.data_ptr(), C, stride, box, dims, omegas.data_ptr(), K,
+        scratch_bytes = int(_lib.library().citrus_oblique_scratch_bytes(K))
+        scratch = torch.empty(max(1, scratch_bytes), device=device, dtype=torch.uint8)  # per-direction constants
+        _lib.call("citrus_oblique_project_scratch", vol.data_ptr(), C, stride, box, dims, omegas.data_ptr(), K,
                   pixels.data_ptr(), Rd, Cd, out.data_ptr(), out.stride(0), out.stride(1), out.stride(2),
-                  out.stride(3), _lib.stream_handle(device))
+                  out.stride(3), scratch.data_ptr(), scratch_bytes, _lib.stream_handle(device))
         return out

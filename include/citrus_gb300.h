@@ -210,6 +210,16 @@ int citrus_oblique_project(const float* field, int64_t channels, int64_t field_s
                            int64_t num_rows, int64_t num_cols, float* out, int64_t os_k, int64_t os_c, int64_t os_r,
                            int64_t os_col, void* stream);
 
+/* The same with a caller-owned device scratch of at least citrus_oblique_scratch_bytes(num_directions) bytes: one
+ * thread per direction forms the direction's float64 set-up constants there first, and every block of the direction
+ * reads them instead of forming them itself (the same values; NULL scratch: formed per block). */
+int64_t citrus_oblique_scratch_bytes(int64_t num_directions);
+int citrus_oblique_project_scratch(const float* field, int64_t channels, int64_t field_stride, const double* box,
+                                   const int64_t* dims, const float* omegas, int64_t num_directions,
+                                   const double* pixels, int64_t num_rows, int64_t num_cols, float* out, int64_t os_k,
+                                   int64_t os_c, int64_t os_r, int64_t os_col, void* direction_scratch,
+                                   int64_t scratch_bytes, void* stream);
+
 /* ------------------------------------------------------------------------------------------------------------------
  * Uncollided fluence and first-collision source.
  * ------------------------------------------------------------------------------------------------------------------ */

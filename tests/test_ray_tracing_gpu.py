@@ -132,3 +132,40 @@ def test_downstream_lattice_walk_matches_per_ray_walk_and_oracle(cuda_device, ch
     assert np.array_equal(np.isinf(lattice), np.isinf(ref))
     assert finite_rel_err(lattice, walk) < 1e-5
     assert finite_rel_err(lattice, ref) < 1e-5
+
+
+@pytest.mark.parametrize("channels, curved", [(1, False), (2, True), (8, True), (3, False)])
+def test_oblique_direction_table_equals_per_block_set_up(cuda_device, channels, curved):
+    """The oblique projection with its per-direction constants formed once by the set-up kernel (the scratch entry
+    point) gives the same bits as with the constants formed in every block."""
+    from citrus_gb300 import _lib
+    from citrus_gb300.ray_tracing import HostArgs, _grid_args, _pixel_centers
+    grid = Grid((9, 11, 7), 0.7)
+    geo = ConeGeometry(40.0, 70.0, 24, 30, 0.6, 0.5, det_channel_offset=0.3, use_curved_detector=curved)
+    rng = np.random.default_rng(channels)
+    K = 37
+    om = rng.normal(size=(K, 3))
+    om /= np.linalg.norm(om, axis=1, keepdims=True)
+    omegas = torch.as_tensor(om, dtype=torch.float32, device=cuda_device)
+    field = torch.as_tensor(rng.random((K, grid.num_voxels, channels)), dtype=torch.float32, device=cuda_device)
+    pixels = _pixel_centers(geo, 1.3, cuda_device)
+    Rd, Cd = geo.image_shape
+    host = HostArgs()
+    box, dims = _grid_args(host, grid)
+    outs = []
+    for scratch in (False, True):
+        out = torch.full((K, channels, Rd, Cd), float("nan"), device=cuda_device)
+        head = (field.data_ptr(), channels, grid.num_voxels * channels, box, dims, omegas.data_ptr(), K,
+                pixels.data_ptr(), Rd, Cd, out.data_ptr(), *out.stride())
+        if scratch:
+            n = int(_lib.library().citrus_oblique_scratch_bytes(K))
+            buf = torch.empty(n, device=cuda_device, dtype=torch.uint8)
+            _lib.call("citrus_oblique_project_scratch", *head, buf.data_ptr(), n, _lib.stream_handle(cuda_device))
+            with pytest.raises(_lib.CitrusKernelError, match="direction scratch"):
+                _lib.call("citrus_oblique_project_scratch", *head, buf.data_ptr(), n - 17,
+                          _lib.stream_handle(cuda_device))
+        else:
+            _lib.call("citrus_oblique_project", *head, _lib.stream_handle(cuda_device))
+        outs.append(out)
+    assert torch.isfinite(outs[0]).all() and float(outs[0].abs().max()) > 0
+    assert torch.equal(outs[0], outs[1])
