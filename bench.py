@@ -640,6 +640,7 @@ STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_atte
               "citrus_small_k_gemm": None,
               "citrus_small_k_gemm_config": None, "citrus_small_k_gemm_bf16x3": None, "citrus_first_collision_moments": None,
               "citrus_first_collision_means": None, "citrus_source_expansion_first": None,
+              "citrus_source_expansion_first_bf16x3": None,
               "citrus_first_collision_correction": None, "citrus_scattering_moments": None}
 
 

@@ -16,8 +16,13 @@
 //     128-lane x 128-column float32 accumulator in tensor memory and commits them to an mbarrier; every wait on it is
 //     bounded by a wall-clock limit, after which the CTA records the error and leaves.
 //   * The four warps read their 32 lanes of the accumulator (tcgen05.ld 32x32b) and store or add the rows of C.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <mutex>
 #include <stdlib.h>
+#include <string.h>
 
 #include "tcgen05.cuh"
 
@@ -240,9 +245,11 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
 // ---- the warp-specialised form ------------------------------------------------------------------------------------
 // The same product as gemm_tc_kernel with its stages overlapped, one CTA per SM walking its tiles in order:
 //
-//   * loader (one thread of warp 13): the K rows of a 128-column tile of B are contiguous 512-byte runs, each fetched
-//     by one bulk asynchronous copy (cp.async.bulk, completing on the stage's mbarrier with its byte count) into a
-//     ring of kWsRaw float32 stages;
+//   * loader (one thread of warp 13): the [K x 128] float32 tile of B comes in one tensor copy (cp.async.bulk.tensor
+//     through a tensor map of B as [batch][K][J], completing on the stage's mbarrier with the box's byte count;
+//     columns past J read as zeros), or, where the map cannot be made, as K bulk copies of its 512-byte row runs, into
+//     a ring of float32 stages (as many as the shared memory holds, up to kWsRawMax). One request per tile instead of
+//     K: the per-request cost of K small copies held the loads near 1.3 TB/s;
 //   * converters (warps 8 to 11): thread t splits column t of a raw stage into the bfloat16 high and low operand
 //     tiles in the K-major core-matrix layout (kWsOps stages), then frees the raw stage;
 //   * MMA issuer (one thread of warp 12): 3 x (K / 16) tcgen05.mma per tile into one of two float32 accumulators in
@@ -253,7 +260,7 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
 // The MMAs run in gemm_tc_kernel's order and the epilogue adds in its order: the two forms give the same bits. Every
 // mbarrier wait is bounded by kTcTimeoutNs; a role whose wait runs out records the error and stops, the others then
 // stop at their own bounded waits, the issuer waits (bounded) for its last MMAs, and the CTA frees its tensor memory.
-constexpr int kWsRaw = 3;                 // float32 stages of B
+constexpr int kWsRawMax = 3;              // float32 stages of B (deeper rings measured no faster with tensor copies)
 constexpr int kWsOps = 2;                 // bf16 hi/lo operand stages
 constexpr int kWsThreads = 14 * 32;       // 8 epilogue, 4 converter, 1 MMA and 1 loader warps
 constexpr int kWsEpilogueWarps = 8;
@@ -288,7 +295,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
                                                                 int accumulate, int64_t tiles_per_batch,
                                                                 int64_t num_tiles, uint32_t* __restrict__ error_word,
                                                                 const float* __restrict__ F, int64_t ldf,
-                                                                int64_t stride_f) {
+                                                                int64_t stride_f, int raw_stages,
+                                                                const __grid_constant__ CUtensorMap b_map,
+                                                                int use_map) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int KS = (K + 15) / 16;
   const uint32_t a_step = kTcM * 16 * 2, b_step = kTcN * 16 * 2;
@@ -298,14 +307,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   uint8_t* a_lo = a_hi + KS * a_step;
   uint8_t* ops = a_lo + KS * a_step;                                 // kWsOps x (hi, lo)
   const uint32_t op_bytes = 2u * KS * b_step;
-  float* raw = reinterpret_cast<float*>(ops + kWsOps * op_bytes);   // kWsRaw x [K][128]
-  float (*stage)[33] = reinterpret_cast<float (*)[33]>(reinterpret_cast<uint8_t*>(raw) + kWsRaw * raw_stride);
-  __shared__ __align__(8) uint64_t bar[2 * kWsRaw + 2 * kWsOps + 5];
+  float* raw = reinterpret_cast<float*>(ops + kWsOps * op_bytes);   // raw_stages x [K][128]
+  float (*stage)[33] = reinterpret_cast<float (*)[33]>(reinterpret_cast<uint8_t*>(raw) + raw_stages * raw_stride);
+  __shared__ __align__(8) uint64_t bar[2 * kWsRawMax + 2 * kWsOps + 5];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   uint64_t* raw_full = bar;
-  uint64_t* raw_empty = bar + kWsRaw;
-  uint64_t* op_full = bar + 2 * kWsRaw;
+  uint64_t* raw_empty = bar + kWsRawMax;
+  uint64_t* op_full = bar + 2 * kWsRawMax;
   uint64_t* op_empty = op_full + kWsOps;
   uint64_t* acc_full = op_empty + kWsOps;
   uint64_t* acc_empty = acc_full + 2;
@@ -333,7 +342,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
       }
   if (tid == 0) {
     abort_flag = 0;
-    for (int i = 0; i < kWsRaw; ++i) {
+    for (int i = 0; i < raw_stages; ++i) {
       mbar_init(smem_u32(raw_full + i), 1);
       mbar_init(smem_u32(raw_empty + i), 128);
     }
@@ -371,8 +380,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   if (warp == kWsLoaderWarp) {
     if (lane == 0) {
       for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
-        const int st = (int)(i % kWsRaw);
-        if (!mbar_wait(smem_u32(raw_empty + st), (uint32_t)((i / kWsRaw) & 1) ^ 1u, global_timer_ns())) {
+        const int st = (int)(i % raw_stages);
+        if (!mbar_wait(smem_u32(raw_empty + st), (uint32_t)((i / raw_stages) & 1) ^ 1u, global_timer_ns())) {
           fail();
           break;
         }
@@ -381,17 +390,26 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
         const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
         const uint32_t bytes = (uint32_t)((J - n0 < kTcN ? J - n0 : (int64_t)kTcN) * 4);
         const uint32_t mb = smem_u32(raw_full + st);
-        mbar_expect_tx(mb, bytes * (uint32_t)K);
-        const float* src = B + bz * stride_b + n0;
         const uint32_t dst = smem_u32(reinterpret_cast<uint8_t*>(raw) + st * raw_stride);
-        for (int k = 0; k < K; ++k) bulk_copy_g2s(dst + (uint32_t)k * kTcN * 4, src + (int64_t)k * ldb, bytes, mb);
+        if (use_map) {
+          mbar_expect_tx(mb, (uint32_t)K * kTcN * 4);  // the whole box, its columns past J filled with zeros
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4}], [%5];" ::"r"(dst),
+              "l"(reinterpret_cast<uint64_t>(&b_map)), "r"((int)n0), "r"(0), "r"((int)bz), "r"(mb)
+              : "memory");
+        } else {
+          mbar_expect_tx(mb, bytes * (uint32_t)K);
+          const float* src = B + bz * stride_b + n0;
+          for (int k = 0; k < K; ++k) bulk_copy_g2s(dst + (uint32_t)k * kTcN * 4, src + (int64_t)k * ldb, bytes, mb);
+        }
       }
     }
   } else if (warp >= kWsConverterWarp0 && warp < kWsConverterWarp0 + 4) {
     const int t = tid - kWsConverterWarp0 * 32;  // the tile column this thread splits
     for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
-      const int st = (int)(i % kWsRaw), op = (int)(i % kWsOps);
-      if (!mbar_wait(smem_u32(raw_full + st), (uint32_t)((i / kWsRaw) & 1), global_timer_ns()) ||
+      const int st = (int)(i % raw_stages), op = (int)(i % kWsOps);
+      if (!mbar_wait(smem_u32(raw_full + st), (uint32_t)((i / raw_stages) & 1), global_timer_ns()) ||
           !mbar_wait(smem_u32(op_empty + op), (uint32_t)((i / kWsOps) & 1) ^ 1u, global_timer_ns())) {
         fail();
         break;
@@ -552,14 +570,21 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kCols) : "memory");
 }
 
-// shared memory of the warp-specialised form: A hi/lo, kWsOps operand stages, kWsRaw float32 stages (1 KB aligned),
-// the epilogue's transposes
-size_t ws_smem_bytes(int K) {
+// shared memory of the warp-specialised form: A hi/lo, kWsOps operand stages, the float32 stages (1 KB aligned),
+// the epilogue's transposes; ws_raw_stages: as many float32 stages as fit 227 KB with the rest, up to kWsRawMax
+// (the deeper the ring, the more of B's bytes are in flight per SM while earlier tiles convert and multiply)
+constexpr size_t kWsSmemLimit = 227 * 1024;
+size_t ws_raw_stride(int K) { return (((size_t)K * kTcN * 4) + 1023) & ~(size_t)1023; }
+size_t ws_fixed_bytes(int K) {
   const size_t KS = (size_t)(K + 15) / 16;
-  const size_t raw_stride = (((size_t)K * kTcN * 4) + 1023) & ~(size_t)1023;
-  return KS * 2 * kTcM * 16 * 2 + kWsOps * KS * 2 * kTcN * 16 * 2 + kWsRaw * raw_stride +
-         (size_t)kWsEpilogueWarps * 32 * 33 * 4;
+  return KS * 2 * kTcM * 16 * 2 + kWsOps * KS * 2 * kTcN * 16 * 2 + (size_t)kWsEpilogueWarps * 32 * 33 * 4;
 }
+int ws_raw_stages(int K) {
+  const size_t fixed = ws_fixed_bytes(K), stride = ws_raw_stride(K);
+  const size_t n = fixed < kWsSmemLimit ? (kWsSmemLimit - fixed) / stride : 0;
+  return (int)std::min<size_t>(n, kWsRawMax);
+}
+size_t ws_smem_bytes(int K) { return ws_fixed_bytes(K) + (size_t)std::max(ws_raw_stages(K), 2) * ws_raw_stride(K); }
 
 }  // namespace
 }  // namespace citrus
@@ -568,6 +593,36 @@ using namespace citrus;
 
 namespace citrus {
 namespace {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against the driver library); null when the
+// driver does not provide it
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// B as a float32 tensor [batch][K][J] (J innermost, rows ldb floats apart, batches stride_b floats apart) with a
+// [1][K][128] box: one tensor copy per tile. The launcher has checked the 16-byte alignment of B, ldb and stride_b.
+bool encode_b_map(CUtensorMap* map, const float* B, int64_t K, int64_t J, int64_t ldb, int64_t batch,
+                  int64_t stride_b) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (enc == nullptr || J > 0x7fffffffLL || batch > 0x7fffffffLL) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)J, (cuuint64_t)K, (cuuint64_t)batch};
+  const cuuint64_t strides[2] = {(cuuint64_t)ldb * 4, (cuuint64_t)(batch > 1 ? stride_b : ldb * K) * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)kTcN, (cuuint32_t)K, 1u};
+  const cuuint32_t elem[3] = {1u, 1u, 1u};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(B), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 // CITRUS_TC_FORM=single keeps the single-stage kernel (measurements, and the check that both forms agree); read at
 // every call
@@ -594,22 +649,26 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
   const bool swapped = M <= 64;
   // the warp-specialised form when B's rows are runs of 16-byte units (bulk copies) and its stages fit one CTA
   const size_t ws_smem = ws_smem_bytes((int)K);
-  if (J % 4 == 0 && ldb % 4 == 0 && stride_b % 4 == 0 && ((uintptr_t)B % 16) == 0 && ws_smem <= 227 * 1024 &&
-      !ws_disabled()) {
+  const int raw_stages = ws_raw_stages((int)K);
+  if (J % 4 == 0 && ldb % 4 == 0 && stride_b % 4 == 0 && ((uintptr_t)B % 16) == 0 && raw_stages >= 2 &&
+      ws_smem <= kWsSmemLimit && !ws_disabled()) {
     const void* wfn = swapped ? (const void*)gemm_ws_kernel<true> : (const void*)gemm_ws_kernel<false>;
     cudaError_t we = cudaFuncSetAttribute(wfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem);
     if (we != cudaSuccess) return set_error(CITRUS_ECUDA, "%s: %s", name, cudaGetErrorString(we));
     const int64_t tiles_per_batch = cdiv(J, kTcN);
     const int64_t num_tiles = tiles_per_batch * batch;
     const int64_t grid = std::min<int64_t>(num_tiles, (int64_t)num_sms());
+    CUtensorMap b_map;
+    memset(&b_map, 0, sizeof(b_map));
+    const int use_map = encode_b_map(&b_map, B, K, J, ldb, batch, stride_b) ? 1 : 0;
     if (swapped)
       gemm_ws_kernel<true><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
           A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-          error_word, F, ldf, stride_f);
+          error_word, F, ldf, stride_f, raw_stages, b_map, use_map);
     else
       gemm_ws_kernel<false><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
           A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-          error_word, F, ldf, stride_f);
+          error_word, F, ldf, stride_f, raw_stages, b_map, use_map);
     note_launches();
     return launch_status(name);
   }
