@@ -32,6 +32,7 @@ namespace {
 constexpr int kTcThreads = 128;  // four warps: warp w owns accumulator lanes 32w .. 32w + 31
 constexpr int kTcN = 128;        // MMA columns per tile (B columns)
 constexpr int kTcMaxK = 128;     // inner dimension, padded to a multiple of 16
+constexpr int kSwapMaxM = 128;   // rows of C up to which the swapped form runs (the MMA's N <= 256)
 
 // kT = false: the MMA's A is the small matrix (rows of C), its B the 128-column tile, D = C[:, tile] in 128 x 128
 // accumulator columns. kT = true (M <= 64): the roles swap, D = C[:, tile]^T with the tile's 128 columns as the MMA
@@ -84,12 +85,13 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  constexpr uint32_t kCols = kT ? 64u : (uint32_t)kTcN;  // accumulator columns (a power of two >= 32)
   const int n_t = ((M + 15) / 16) * 16;                   // MMA N of the swapped form
+  // accumulator columns (a power of two >= 32): the swapped form's N rounded up, else the tile's 128
+  const uint32_t acc_cols = kT ? (n_t <= 64 ? 64u : 128u) : (uint32_t)kTcN;
   const uint32_t idesc = kT ? idesc_bf16(n_t) : idesc_bf16(kTcN);
-  if (warp == 0) {  // the accumulator: 128 lanes x kCols float32 columns
+  if (warp == 0) {  // the accumulator: 128 lanes x acc_cols float32 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(kCols)
+                 "r"(acc_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
   }
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(acc_cols) : "memory");
 }
 
 // ---- the warp-specialised form ------------------------------------------------------------------------------------
@@ -297,7 +299,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
                                                                 const float* __restrict__ F, int64_t ldf,
                                                                 int64_t stride_f, int raw_stages,
                                                                 const __grid_constant__ CUtensorMap b_map,
-                                                                int use_map) {
+                                                                int use_map,
+                                                                const __grid_constant__ CUtensorMap f_map,
+                                                                int use_f_map) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int KS = (K + 15) / 16;
   const uint32_t a_step = kTcM * 16 * 2, b_step = kTcN * 16 * 2;
@@ -309,7 +313,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   const uint32_t op_bytes = 2u * KS * b_step;
   float* raw = reinterpret_cast<float*>(ops + kWsOps * op_bytes);   // raw_stages x [K][128]
   float (*stage)[33] = reinterpret_cast<float (*)[33]>(reinterpret_cast<uint8_t*>(raw) + raw_stages * raw_stride);
-  __shared__ __align__(8) uint64_t bar[2 * kWsRawMax + 2 * kWsOps + 5];
+  __shared__ __align__(8) uint64_t bar[2 * kWsRawMax + 2 * kWsOps + 9];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   uint64_t* raw_full = bar;
@@ -319,6 +323,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   uint64_t* acc_full = op_empty + kWsOps;
   uint64_t* acc_empty = acc_full + 2;
   uint64_t* mma_done = acc_empty + 2;  // the issuer's last commit: its MMAs are complete before the CTA frees TMEM
+  // the first-collision means of the swapped form come as [M][32] tiles (the tile's 128 columns / 4) in two stages
+  // of the epilogue-transpose region, which the swapped epilogue does not use (2 x 128 x 128 bytes fit its 33 KB)
+  uint64_t* f_full = mma_done + 1;
+  uint64_t* f_empty = f_full + 2;
+  float* f_stage = reinterpret_cast<float*>(stage);
+  const bool f_tma = kT && F != nullptr && use_f_map != 0;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
   // A, split once (threads 0..127), rows r of every K step, 8 columns at a time
@@ -355,14 +365,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
       mbar_init(smem_u32(acc_empty + i), 32 * kWsEpilogueWarps);
     }
     mbar_init(smem_u32(mma_done), 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(smem_u32(f_full + i), 1);
+      mbar_init(smem_u32(f_empty + i), 32 * kWsEpilogueWarps);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  constexpr uint32_t kCols = kT ? 64u : (uint32_t)kTcN;  // one accumulator; two are allocated
   const int n_t = ((M + 15) / 16) * 16;
+  const uint32_t acc_cols = kT ? (n_t <= 64 ? 64u : 128u) : (uint32_t)kTcN;  // one accumulator; two are allocated
   const uint32_t idesc = kT ? idesc_bf16(n_t) : idesc_bf16(kTcN);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(2 * kCols)
+                 "r"(2 * acc_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -378,6 +392,25 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   };
 
   if (warp == kWsLoaderWarp) {
+    if (lane == 1 && f_tma) {  // the means: one tensor copy of [M][32] per tile, two stages ahead of the epilogue
+      for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
+        const int fs = (int)(i & 1);
+        if (!mbar_wait(smem_u32(f_empty + fs), (uint32_t)((i >> 1) & 1) ^ 1u, global_timer_ns())) {
+          fail();
+          break;
+        }
+        const int64_t tile = blockIdx.x + i * gridDim.x;
+        const int64_t bz = tile / tiles_per_batch;
+        const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
+        const uint32_t mb = smem_u32(f_full + fs);
+        mbar_expect_tx(mb, (uint32_t)M * 32u * 4u);
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];" ::"r"(smem_u32(f_stage + fs * M * 32)),
+            "l"(reinterpret_cast<uint64_t>(&f_map)), "r"((int)(n0 / 4)), "r"(0), "r"((int)bz), "r"(mb)
+            : "memory");
+      }
+    }
     if (lane == 0) {
       for (int64_t i = 0; i < my_tiles && !abort_flag; ++i) {
         const int st = (int)(i % raw_stages);
@@ -448,7 +481,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t d = tmem + (uint32_t)ac * kCols;
+        const uint32_t d = tmem + (uint32_t)ac * acc_cols;
         uint8_t* o_hi = ops + op * op_bytes;
         uint8_t* o_lo = o_hi + KS * b_step;
         for (int s = 0; s < KS; ++s) {
@@ -486,12 +519,41 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
       const int64_t n0 = (tile - bz * tiles_per_batch) * kTcN;
       float* Cz = C + bz * stride_c;
       const float* Fz = F != nullptr ? F + bz * stride_f : nullptr;
-      const uint32_t taddr = tmem + (uint32_t)ac * kCols + ((uint32_t)(quarter * 32) << 16);
+      const uint32_t taddr = tmem + (uint32_t)ac * acc_cols + ((uint32_t)(quarter * 32) << 16);
+      const float* fst = f_stage + (int)(i & 1) * M * 32;
+      if (f_tma && !mbar_wait(smem_u32(f_full + (int)(i & 1)), (uint32_t)((i >> 1) & 1), global_timer_ns())) {
+        fail();
+        break;
+      }
       if (kT) {
         // accumulator lane 32 quarter + lane is column n0 + 32 quarter + lane of C; its columns are the rows of C,
         // split in 16-row steps between the two halves of the epilogue warps
         const int64_t col = n0 + quarter * 32 + lane;
+        const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
         for (int m0 = half * 16; m0 < n_t; m0 += 32) {
+          const int rows = min(16, M - m0);
+          float* out = Cz + (int64_t)m0 * ldc + col;
+          // the loads of C (accumulating) or of the means are issued before the tensor-memory load, so that the two
+          // latencies overlap
+          float prev[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) prev[q] = 0.f;
+          if (col < J) {
+            if (accumulate) {
+#pragma unroll
+              for (int q = 0; q < 16; ++q)
+                if (q < rows) prev[q] = out[(int64_t)q * ldc];
+            } else if (add && f_tma) {
+              const int fc = (quarter * 32 + lane) >> 2;  // the tile's column / 4
+#pragma unroll
+              for (int q = 0; q < 16; ++q)
+                if (q < rows) prev[q] = fst[(m0 + q) * 32 + fc];
+            } else if (add) {
+#pragma unroll
+              for (int q = 0; q < 16; ++q)
+                if (q < rows) prev[q] = __ldg(Fz + (int64_t)(m0 + q) * ldf + (col >> 2));
+            }
+          }
           uint32_t r[16];
           asm volatile(
               "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
@@ -502,17 +564,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
               : "memory");
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
           if (col < J) {
-            const int rows = min(16, M - m0);
-            float* out = Cz + (int64_t)m0 * ldc + col;
-            float prev[16];
-            const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
-            if (accumulate) {
-#pragma unroll
-              for (int q = 0; q < 16; ++q) prev[q] = q < rows ? out[(int64_t)q * ldc] : 0.f;
-            } else if (add) {
-#pragma unroll
-              for (int q = 0; q < 16; ++q) prev[q] = q < rows ? __ldg(Fz + (int64_t)(m0 + q) * ldf + (col >> 2)) : 0.f;
-            }
 #pragma unroll
             for (int q = 0; q < 16; ++q)
               if (q < rows) out[(int64_t)q * ldc] = add ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
@@ -561,13 +612,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(smem_u32(acc_empty + ac));
+      if (f_tma) mbar_arrive(smem_u32(f_empty + (int)(i & 1)));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * acc_cols) : "memory");
 }
 
 // shared memory of the warp-specialised form: A hi/lo, kWsOps operand stages, the float32 stages (1 KB aligned),
@@ -611,6 +663,23 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // B as a float32 tensor [batch][K][J] (J innermost, rows ldb floats apart, batches stride_b floats apart) with a
 // [1][K][128] box: one tensor copy per tile. The launcher has checked the 16-byte alignment of B, ldb and stride_b.
+// the means F as [batch][M][J / 4] with a [1][M][32] box (the 128 columns of a tile / 4); false when F's alignment,
+// row or batch strides do not allow a tensor map (the epilogue then reads F from global memory)
+bool encode_f_map(CUtensorMap* map, const float* F, int64_t M, int64_t J, int64_t ldf, int64_t batch,
+                  int64_t stride_f) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (enc == nullptr || F == nullptr || ((uintptr_t)F % 16) != 0 || ldf % 4 != 0 || (batch > 1 && stride_f % 4 != 0) ||
+      J / 4 > 0x7fffffffLL || batch > 0x7fffffffLL)
+    return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)(J / 4), (cuuint64_t)M, (cuuint64_t)batch};
+  const cuuint64_t strides[2] = {(cuuint64_t)ldf * 4, (cuuint64_t)(batch > 1 ? stride_f : ldf * M) * 4};
+  const cuuint32_t box[3] = {32u, (cuuint32_t)M, 1u};
+  const cuuint32_t elem[3] = {1u, 1u, 1u};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(F), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool encode_b_map(CUtensorMap* map, const float* B, int64_t K, int64_t J, int64_t ldb, int64_t batch,
                   int64_t stride_b) {
   const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
@@ -646,7 +715,10 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
   // more than four CTAs (4 x 128 of the 512 tensor-memory columns) share an SM: every allocation succeeds at once
   const size_t b_bytes = std::max<size_t>((size_t)KS * 2 * kTcN * 16 * 2, (size_t)kTcM * 33 * sizeof(float));
   const size_t smem = std::max<size_t>((size_t)KS * 2 * kTcM * 16 * 2 + b_bytes, 50 * 1024);
-  const bool swapped = M <= 64;
+  // the swapped form (the tile's 128 columns as the MMA's M, the rows of C its N) for every M: its epilogue stores
+  // each accumulator lane's column of C directly (32 consecutive columns per warp store), where the other form turns
+  // 32 x 32 blocks through shared memory; measured faster for the 120-row source expansion as well
+  const bool swapped = M <= kSwapMaxM;
   // the warp-specialised form when B's rows are runs of 16-byte units (bulk copies) and its stages fit one CTA
   const size_t ws_smem = ws_smem_bytes((int)K);
   const int raw_stages = ws_raw_stages((int)K);
@@ -661,14 +733,17 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
     CUtensorMap b_map;
     memset(&b_map, 0, sizeof(b_map));
     const int use_map = encode_b_map(&b_map, B, K, J, ldb, batch, stride_b) ? 1 : 0;
+    CUtensorMap f_map;
+    memset(&f_map, 0, sizeof(f_map));
+    const int use_f_map = F != nullptr && encode_f_map(&f_map, F, M, J, ldf, batch, stride_f) ? 1 : 0;
     if (swapped)
       gemm_ws_kernel<true><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
           A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-          error_word, F, ldf, stride_f, raw_stages, b_map, use_map);
+          error_word, F, ldf, stride_f, raw_stages, b_map, use_map, f_map, use_f_map);
     else
       gemm_ws_kernel<false><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
           A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-          error_word, F, ldf, stride_f, raw_stages, b_map, use_map);
+          error_word, F, ldf, stride_f, raw_stages, b_map, use_map, f_map, 0);
     note_launches();
     return launch_status(name);
   }
