@@ -633,7 +633,7 @@ def tiled_sweep_bytes(args) -> int:
 
 SWEEP_ENTRY_POINTS = ("citrus_sweep_tiled", "citrus_sweep_persistent_config", "citrus_sweep_persistent")
 STEP_TIMED = {"citrus_attenuated_emission_moments": emission_bytes, "citrus_attenuated_emission": product_emission_bytes,
-              "citrus_downstream_cumulative": downstream_bytes,
+              "citrus_downstream_cumulative": downstream_bytes, "citrus_downstream_cumulative_tables": downstream_bytes,
               "citrus_sweep_persistent": sweep_bytes, "citrus_sweep_persistent_config": sweep_bytes,
               "citrus_sweep_tiled": tiled_sweep_bytes,
               "citrus_oblique_project": None, "citrus_oblique_project_scratch": None, "citrus_box_blur": None,

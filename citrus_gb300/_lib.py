@@ -41,6 +41,8 @@ SIGNATURES = {
     "citrus_line_integrals": [P, I64, P, P, P, P, I64, P, P],
     "citrus_trace_from_source": [P, I64, P, P, P, P, P, P, P, P, I64, P, P],
     "citrus_downstream_cumulative": [P, I64, P, P, P, P, I64, P, F64, P, I64, I64, I64, P, I64, P],
+    "citrus_crossing_tables": [P, P, P, I64, P, I64, P],
+    "citrus_downstream_cumulative_tables": [P, I64, P, P, P, P, I64, P, F64, P, I64, I64, I64, P, I64, P],
     "citrus_oblique_project": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P],
     "citrus_oblique_project_scratch": [P, I64, I64, P, P, P, I64, P, I64, I64, P, I64, I64, I64, I64, P, I64, P],
     "citrus_group_transmission": [P, I64, I64, P, P, P, I64, I64, P, P, P, P, P],

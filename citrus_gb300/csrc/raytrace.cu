@@ -955,11 +955,58 @@ extern "C" int citrus_trace_from_source(const float* volume, int64_t channels, c
   return launch_status("citrus_trace_from_source");
 }
 
+namespace citrus {
+namespace {
+int downstream(const float* volume, int64_t channels, const double* box, const int64_t* dims, const float* omegas,
+               const uint8_t* toward, int64_t num_directions, const double* panel, double diagonal, float* out,
+               int64_t os_k, int64_t os_c, int64_t os_v, int32_t* crossings, int64_t crossings_words, bool build,
+               void* stream);
+}  // namespace
+}  // namespace citrus
+
+extern "C" int citrus_crossing_tables(const double* box, const int64_t* dims, const float* omegas,
+                                      int64_t num_directions, int32_t* crossings, int64_t crossings_words,
+                                      void* stream) {
+  CITRUS_REQUIRE(box && dims && omegas && crossings, "citrus_crossing_tables: null pointer argument");
+  CITRUS_REQUIRE(num_directions >= 0 && dims[0] >= 1 && dims[1] >= 1 && dims[2] >= 1,
+                 "citrus_crossing_tables: bad sizes");
+  const int64_t E = dims[0] + dims[1] + dims[2];
+  CITRUS_REQUIRE(crossings_words >= 3 * E * num_directions,
+                 "citrus_crossing_tables: the table holds %lld words, needs %lld", (long long)crossings_words,
+                 (long long)(3 * E * num_directions));
+  if (num_directions == 0) return CITRUS_OK;
+  const Box b = make_box(box, dims);
+  crossing_table_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, as_stream(stream)>>>(
+      b, omegas, (int)num_directions, crossings);
+  note_launches();
+  return launch_status("citrus_crossing_tables");
+}
+
+extern "C" int citrus_downstream_cumulative_tables(const float* volume, int64_t channels, const double* box,
+                                                   const int64_t* dims, const float* omegas, const uint8_t* toward,
+                                                   int64_t num_directions, const double* panel, double diagonal,
+                                                   float* out, int64_t os_k, int64_t os_c, int64_t os_v,
+                                                   const int32_t* crossings, int64_t crossings_words, void* stream) {
+  CITRUS_REQUIRE(crossings != nullptr, "citrus_downstream_cumulative_tables: null crossing tables");
+  return downstream(volume, channels, box, dims, omegas, toward, num_directions, panel, diagonal, out, os_k, os_c,
+                    os_v, const_cast<int32_t*>(crossings), crossings_words, false, stream);
+}
+
 extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channels, const double* box,
                                             const int64_t* dims, const float* omegas, const uint8_t* toward,
                                             int64_t num_directions, const double* panel, double diagonal,
                                             float* out, int64_t os_k, int64_t os_c, int64_t os_v, int32_t* crossings,
                                             int64_t crossings_words, void* stream) {
+  return downstream(volume, channels, box, dims, omegas, toward, num_directions, panel, diagonal, out, os_k, os_c,
+                    os_v, crossings, crossings_words, true, stream);
+}
+
+namespace citrus {
+namespace {
+int downstream(const float* volume, int64_t channels, const double* box, const int64_t* dims, const float* omegas,
+               const uint8_t* toward, int64_t num_directions, const double* panel, double diagonal, float* out,
+               int64_t os_k, int64_t os_c, int64_t os_v, int32_t* crossings, int64_t crossings_words, bool build,
+               void* stream) {
   int status = check_common(volume, channels, box, dims, out);
   if (status) return status;
   CITRUS_REQUIRE(omegas && panel, "citrus_downstream_cumulative: null directions or panel");
@@ -992,8 +1039,11 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
   if (C % 2 == 0) CITRUS_REQUIRE(((uintptr_t)volume % 16) == 0, "citrus_downstream_cumulative: unaligned volume");
   if (C % 4 == 0 && os_c == 1 && os_v == C)
     CITRUS_REQUIRE(((uintptr_t)out % 16) == 0 && os_k % 4 == 0, "citrus_downstream_cumulative: unaligned out");
-  crossing_table_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, s>>>(b, omegas, (int)num_directions, crossings);
-  note_launches();
+  if (build) {  // else the caller's tables of these directions (citrus_crossing_tables)
+    crossing_table_kernel<<<(unsigned)cdiv(num_directions, 64), 64, 0, s>>>(b, omegas, (int)num_directions,
+                                                                           crossings);
+    note_launches();
+  }
   const size_t smem = (size_t)(2 * ((E + 1) & ~1) + 2 * E) * sizeof(int32_t);
 #define CITRUS_LATTICE(KC)                                                                                        \
   downstream_lattice_kernel<KC><<<grid, kThreads, smem, s>>>(b, volume, C, omegas, toward, p, (float)diagonal, V, \
@@ -1009,6 +1059,8 @@ extern "C" int citrus_downstream_cumulative(const float* volume, int64_t channel
   note_launches();
   return launch_status("citrus_downstream_cumulative");
 }
+}  // namespace
+}  // namespace citrus
 
 extern "C" int64_t citrus_oblique_scratch_bytes(int64_t num_directions) {
   return num_directions <= 0 ? 0 : num_directions * (int64_t)(sizeof(DirConst) + sizeof(DirPair)) + 16;

@@ -180,13 +180,28 @@ class GB300Projectors:
         return -(torch.logsumexp(-tau, dim=-1) - math.log(n * n))
 
     # ---- (c) downstream -----------------------------------------------------------------------------------------
+    def crossing_tables(self, grid: Grid, omegas: Tensor) -> Tensor:
+        """[K, 3 (nx + ny + nz)] int32 crossing tables of the lattice walk for directions [K, 3] on ``grid`` (one
+        launch for the whole set; ``downstream_cumulative(crossings=...)`` takes rows of it)."""
+        device = omegas.device
+        om = omegas.to(dtype=torch.float32).reshape(-1, 3).contiguous()
+        K = om.shape[0]
+        E = grid.num_rows + grid.num_cols + grid.num_slices
+        tables = torch.empty(K, 3 * E, dtype=torch.int32, device=device)
+        host = HostArgs()
+        box, dims = _grid_args(host, grid)
+        _lib.call("citrus_crossing_tables", box, dims, om.data_ptr(), K, tables.data_ptr(), tables.numel(),
+                  _lib.stream_handle(device))
+        return tables
+
     def downstream_cumulative(self, mu: Tensor, grid: Grid, geometry: ConeGeometry, angle: float,
                               omegas: Tensor, out: Optional[Tensor] = None, lattice: bool = True,
-                              voxel_major: bool = False) -> Tensor:
+                              voxel_major: bool = False, crossings: Optional[Tensor] = None) -> Tensor:
         """[K, C, R, Cc, S] from every voxel centre along each direction to the panel; +inf where the direction does
         not face the panel (``omega . (-n_hat) <= 0``), 0 beyond the panel. ``lattice`` walks every ray down its
-        direction's shared crossing table (the default), else each ray runs its own walk. ``voxel_major`` returns
-        the same values as a contiguous [K, V, C] tensor (``out`` ignored)."""
+        direction's shared crossing table (the default), else each ray runs its own walk; ``crossings`` gives those
+        tables prebuilt (``crossing_tables`` of these directions on ``grid``). ``voxel_major`` returns the same
+        values as a contiguous [K, V, C] tensor (``out`` ignored)."""
         vol = _voxel_major(mu, grid)
         device = mu.device
         omegas = omegas.to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
@@ -206,8 +221,16 @@ class GB300Projectors:
         host = HostArgs()
         box, dims = _grid_args(host, grid)
         diagonal = math.sqrt(sum(e * e for e in grid.extent)) * (1 + 1e-9) + 1e-9
-        crossings = (torch.empty(3 * (grid.num_rows + grid.num_cols + grid.num_slices) * K, dtype=torch.int32,
-                                 device=device) if lattice else None)
+        E = grid.num_rows + grid.num_cols + grid.num_slices
+        if crossings is not None:
+            if (crossings.dtype != torch.int32 or not crossings.is_contiguous()
+                    or tuple(crossings.shape) != (K, 3 * E) or crossings.device != device):
+                raise ValueError(f"crossings must be the contiguous int32 [{K}, {3 * E}] tables of these directions")
+            _lib.call("citrus_downstream_cumulative_tables", vol.data_ptr(), mu.shape[0], box, dims,
+                      omegas.data_ptr(), toward.data_ptr(), K, panel_args(host, geometry, angle), diagonal,
+                      out.data_ptr(), *strides, crossings.data_ptr(), crossings.numel(), _lib.stream_handle(device))
+            return out
+        crossings = torch.empty(3 * E * K, dtype=torch.int32, device=device) if lattice else None
         _lib.call("citrus_downstream_cumulative", vol.data_ptr(), mu.shape[0], box, dims, omegas.data_ptr(),
                   toward.data_ptr(), K, panel_args(host, geometry, angle), diagonal, out.data_ptr(), *strides,
                   None if crossings is None else crossings.data_ptr(), 0 if crossings is None else crossings.numel(),

@@ -137,6 +137,16 @@ class DirectionSetContext:
             self._cache[key] = to_device(real_spherical_harmonics(L, self._omega64), self.device)
         return self._cache[key]
 
+    def crossing_tables(self, grid: Grid, projectors) -> Optional[Tensor]:
+        """The downstream walk's crossing tables of the set's directions on ``grid``, built once and kept with the
+        set (None for projectors that build their own)."""
+        if not hasattr(projectors, "crossing_tables"):
+            return None
+        key = ("crossings", grid)
+        if key not in self._cache:
+            self._cache[key] = projectors.crossing_tables(grid, self.omega)
+        return self._cache[key]
+
     def footprint(self, grid: Grid) -> tuple:
         """(heights [V] of the point centres above the panel, height of the box centre) (reference ``:1033-1077``)."""
         key = ("footprint", grid)
@@ -348,15 +358,17 @@ def combined_scatter_image(library: MultigroupLibrary, rho_quadrature: Tensor, p
         tau_mu = attenuation.to(device=device, dtype=torch.float32).contiguous()
         if tuple(tau_mu.shape) != (traced.shape[0], G) or tuple(traced.shape[1:]) != tuple(grid_coarse.shape):
             raise ValueError(f"attenuation must be [M, {G}] and rho_coarse [M, {grid_coarse.shape}]")
+    tables = context.crossing_tables(grid_coarse, projectors)
     for s, e in context.chunk_bounds:
         k = e - s
         dirs = context.omega[s:e]
+        walk = {} if tables is None else {"crossings": tables[s:e]}
         if traced is not None:
             tau = projectors.downstream_cumulative(traced, grid_coarse, geometry, angle, dirs,
-                                                   voxel_major=True)                      # [k, cells, M]
+                                                   voxel_major=True, **walk)              # [k, cells, M]
         else:
             tau = projectors.downstream_cumulative(mu_t_coarse, grid_coarse, geometry, angle, dirs,
-                                                   voxel_major=True)                      # [k, cells, G]
+                                                   voxel_major=True, **walk)              # [k, cells, G]
         Yk = Y[s:e].contiguous()
         emission = torch.empty(k, V, C, device=device)
         head = (*fc.common(), f, deltas, fc.focal, fc.table.data_ptr(), fc.num_eta, fc.eta_lo, fc.eta_hi,

@@ -200,6 +200,18 @@ int citrus_downstream_cumulative(const float* volume, int64_t channels, const do
                                  const double* panel, double diagonal, float* out, int64_t os_k, int64_t os_c,
                                  int64_t os_v, int32_t* crossings, int64_t crossings_words, void* stream);
 
+/* The crossing tables of citrus_downstream_cumulative for num_directions directions at once ([K, 3 (nx + ny + nz)]
+ * int32: per direction the distances of the plane crossings from a voxel centre, the flat-index steps and the first
+ * crossing of each axis), and the downstream trace reading such prebuilt tables instead of building them: a
+ * direction set whose tables are kept (one build per view's direction set) needs no build per chunk. */
+int citrus_crossing_tables(const double* box, const int64_t* dims, const float* omegas, int64_t num_directions,
+                           int32_t* crossings, int64_t crossings_words, void* stream);
+int citrus_downstream_cumulative_tables(const float* volume, int64_t channels, const double* box,
+                                        const int64_t* dims, const float* omegas, const uint8_t* toward,
+                                        int64_t num_directions, const double* panel, double diagonal, float* out,
+                                        int64_t os_k, int64_t os_c, int64_t os_v, const int32_t* crossings,
+                                        int64_t crossings_words, void* stream);
+
 /* Line through every pixel centre (float64 pixels [rows, cols, 3]) along each direction, clipped to the box on both
  * sides (float64 set-up);
  * field [K or 1, V, C] with field_stride elements between directions (0: shared); out element (k, c, row, col) at

@@ -169,3 +169,24 @@ def test_oblique_direction_table_equals_per_block_set_up(cuda_device, channels, 
         outs.append(out)
     assert torch.isfinite(outs[0]).all() and float(outs[0].abs().max()) > 0
     assert torch.equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("curved", [False, True])
+def test_prebuilt_crossing_tables_give_the_same_walk(cuda_device, curved):
+    """The downstream walk over crossing tables built once for a whole direction set (``crossing_tables``, taken
+    in row slices per chunk) equals the walk that builds the tables of its own chunk."""
+    grid = Grid((10, 12, 9), 0.8)
+    geo = ConeGeometry(40.0, 70.0, 16, 20, 0.8, 0.8, use_curved_detector=curved)
+    rng = np.random.default_rng(3)
+    mu = torch.as_tensor(rng.random((2, *grid.shape)) * 0.3, dtype=torch.float32, device=cuda_device)
+    om = rng.normal(size=(29, 3))
+    om /= np.linalg.norm(om, axis=1, keepdims=True)
+    omegas = torch.as_tensor(om, dtype=torch.float32, device=cuda_device)
+    p = GB300Projectors()
+    tables = p.crossing_tables(grid, omegas)
+    for s, e in ((0, 13), (13, 29)):
+        own = p.downstream_cumulative(mu, grid, geo, 0.7, omegas[s:e], voxel_major=True)
+        kept = p.downstream_cumulative(mu, grid, geo, 0.7, omegas[s:e], voxel_major=True, crossings=tables[s:e])
+        assert torch.equal(own, kept)
+    with pytest.raises(ValueError, match="crossings"):
+        p.downstream_cumulative(mu, grid, geo, 0.7, omegas[:13], voxel_major=True, crossings=tables[:12])
