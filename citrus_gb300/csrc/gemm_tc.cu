@@ -12,10 +12,12 @@
 //     bytes apart (stride byte offset), one region per 16-wide K step.
 //   * Per tile, thread t reads column t of B in groups of 8 rows (coalesced across the warp), splits it and writes
 //     one 16-byte core-matrix row of B_hi and of B_lo: the same K-major layout with N in place of M.
-//   * One thread issues the 3 x (K / 16) MMAs (M = 128, N = 128, K = 16, kind::f16 with bf16 operands) into a
-//     128-lane x 128-column float32 accumulator in tensor memory and commits them to an mbarrier; every wait on it is
-//     bounded by a wall-clock limit, after which the CTA records the error and leaves.
-//   * The four warps read their 32 lanes of the accumulator (tcgen05.ld 32x32b) and store or add the rows of C.
+//   * One thread issues the 3 x (K / 16) MMAs (kind::f16 with bf16 operands) with the tile's 128 columns as the MMA's
+//     M and the rows of C (rounded up to 16) as its N, so that the float32 accumulator in tensor memory holds C[:,
+//     tile] transposed, and commits them to an mbarrier; every wait on it is bounded by a wall-clock limit, after
+//     which the CTA records the error and leaves.
+//   * Accumulator lane l is column l of the tile: each thread reads its lane (tcgen05.ld 32x32b) and stores (or adds
+//     to) its column of C, 32 consecutive columns of one row per warp store.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -32,14 +34,11 @@ namespace {
 constexpr int kTcThreads = 128;  // four warps: warp w owns accumulator lanes 32w .. 32w + 31
 constexpr int kTcN = 128;        // MMA columns per tile (B columns)
 constexpr int kTcMaxK = 128;     // inner dimension, padded to a multiple of 16
-constexpr int kSwapMaxM = 128;   // rows of C up to which the swapped form runs (the MMA's N <= 256)
 
-// kT = false: the MMA's A is the small matrix (rows of C), its B the 128-column tile, D = C[:, tile] in 128 x 128
-// accumulator columns. kT = true (M <= 64): the roles swap, D = C[:, tile]^T with the tile's 128 columns as the MMA
-// rows and the (M rounded up to 16) rows of C as its N: each accumulator lane is one column of C, stored directly.
-// F (the first-collision means of the source expansion, [M, J / 4] per batch, ldf floats per row and stride_f floats
-// between batches) is added to the first of every four columns of C when not null (with accumulate 0).
-template <bool kT>
+// D = C[:, tile]^T: the tile's 128 columns are the MMA's rows and the (M rounded up to 16) rows of C its N, so each
+// accumulator lane is one column of C, stored directly. F (the first-collision means of the source expansion,
+// [M, J / 4] per batch, ldf floats per row and stride_f floats between batches) is added to the first of every four
+// columns of C when not null (with accumulate 0).
 __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __restrict__ A, int64_t lda,
                                                              const float* __restrict__ B, int64_t ldb,
                                                              float* __restrict__ C, int64_t ldc, int M, int K,
@@ -85,10 +84,9 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  const int n_t = ((M + 15) / 16) * 16;                   // MMA N of the swapped form
-  // accumulator columns (a power of two >= 32): the swapped form's N rounded up, else the tile's 128
-  const uint32_t acc_cols = kT ? (n_t <= 64 ? 64u : 128u) : (uint32_t)kTcN;
-  const uint32_t idesc = kT ? idesc_bf16(n_t) : idesc_bf16(kTcN);
+  const int n_t = ((M + 15) / 16) * 16;                   // MMA N: the rows of C rounded up to 16
+  const uint32_t acc_cols = n_t <= 64 ? 64u : 128u;       // accumulator columns (a power of two >= 32)
+  const uint32_t idesc = idesc_bf16(n_t);
   if (warp == 0) {  // the accumulator: 128 lanes x acc_cols float32 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(acc_cols)
@@ -138,15 +136,9 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
         const uint64_t al = smem_desc(smem_u32(a_lo + s * a_step), 128, 256);
         const uint64_t bh = smem_desc(smem_u32(b_hi + s * b_step), 128, 256);
         const uint64_t bl = smem_desc(smem_u32(b_lo + s * b_step), 128, 256);
-        if (kT) {
-          mma_bf16(tmem, bh, ah, idesc, s > 0 ? 1u : 0u);
-          mma_bf16(tmem, bh, al, idesc, 1u);
-          mma_bf16(tmem, bl, ah, idesc, 1u);
-        } else {
-          mma_bf16(tmem, ah, bh, idesc, s > 0 ? 1u : 0u);
-          mma_bf16(tmem, ah, bl, idesc, 1u);
-          mma_bf16(tmem, al, bh, idesc, 1u);
-        }
+        mma_bf16(tmem, bh, ah, idesc, s > 0 ? 1u : 0u);
+        mma_bf16(tmem, bh, al, idesc, 1u);
+        mma_bf16(tmem, bl, ah, idesc, 1u);
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
                    : "memory");
@@ -160,8 +152,8 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (abort_flag) break;
-    if (kT) {
-      // epilogue of the swapped form: lane 32 warp + lane is column n0 + 32 warp + lane of C, its accumulator
+    {
+      // epilogue: lane 32 warp + lane is column n0 + 32 warp + lane of C, its accumulator
       // columns the rows of C; every store covers 32 consecutive columns of one row
       const int64_t col = n0 + warp * 32 + lane;
 #pragma unroll 1
@@ -192,49 +184,6 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
             if (q < rows) out[(int64_t)q * ldc] = add ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      continue;
-    }
-    // epilogue, 32 columns at a time: warp w reads accumulator lanes (rows) 32w .. 32w + 31 and turns them through
-    // shared memory (the B region, free once the MMAs completed), so that every store (and load, when accumulating)
-    // of C covers 32 consecutive columns of one row: 128 contiguous bytes
-    float (*stage)[33] = reinterpret_cast<float (*)[33]>(b_hi) + warp * 32;
-#pragma unroll 1
-    for (int c0 = 0; c0 < kTcN; c0 += 32) {
-      uint32_t r[32];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int q = 0; q < 32; ++q) stage[lane][q] = __uint_as_float(r[q]);
-      __syncwarp();
-      const int64_t col = n0 + c0 + lane;
-      const int rows = min(32, M - warp * 32);
-      if (col < J && rows > 0) {
-        float* out = Cz + (int64_t)(warp * 32) * ldc + col;
-        float prev[32];
-        if (accumulate) {  // every load issued before the first store
-#pragma unroll
-          for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? out[(int64_t)rr * ldc] : 0.f;
-        } else if (Fz != nullptr && (col & 3) == 0) {  // the mean of the quadruple's first column
-          const float* f = Fz + (int64_t)(warp * 32) * ldf + (col >> 2);
-#pragma unroll
-          for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? __ldg(f + (int64_t)rr * ldf) : 0.f;
-        }
-        const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
-#pragma unroll
-        for (int rr = 0; rr < 32; ++rr)
-          if (rr < rows) out[(int64_t)rr * ldc] = add ? prev[rr] + stage[rr][lane] : stage[rr][lane];
-      }
-      __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();  // the accumulator and the B tile are free for the next tile
@@ -256,8 +205,9 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(const float* __rest
 //     tiles in the K-major core-matrix layout (kWsOps stages), then frees the raw stage;
 //   * MMA issuer (one thread of warp 12): 3 x (K / 16) tcgen05.mma per tile into one of two float32 accumulators in
 //     tensor memory, committed to the operand stage (freed once read) and to the accumulator (full);
-//   * epilogue (warps 0 to 7): warp w reads accumulator lanes 32 (w % 4) .. + 31 and half of the columns, and writes
-//     (or adds to) C, so that the stores of one tile overlap the loads, splits and MMAs of the next.
+//   * epilogue (warps 0 to 7): warp w reads accumulator lanes 32 (w % 4) .. + 31 (columns of C) and every other
+//     16 of its rows, and writes (or adds to) C, so that the stores of one tile overlap the loads, splits and MMAs
+//     of the next; the means come from their own two-stage ring (one tensor copy of [M][32] per tile).
 //
 // The MMAs run in gemm_tc_kernel's order and the epilogue adds in its order: the two forms give the same bits. Every
 // mbarrier wait is bounded by kTcTimeoutNs; a role whose wait runs out records the error and stops, the others then
@@ -269,6 +219,7 @@ constexpr int kWsEpilogueWarps = 8;
 constexpr int kWsConverterWarp0 = 8;
 constexpr int kWsMmaWarp = 12;
 constexpr int kWsLoaderWarp = 13;
+constexpr size_t kWsMeansBytes = 2 * kTcM * 32 * 4;  // two [M <= 128][32] float32 tiles of the means
 
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
@@ -289,7 +240,6 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-template <bool kT>
 __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __restrict__ A, int64_t lda,
                                                                 const float* __restrict__ B, int64_t ldb,
                                                                 float* __restrict__ C, int64_t ldc, int M, int K,
@@ -312,7 +262,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   uint8_t* ops = a_lo + KS * a_step;                                 // kWsOps x (hi, lo)
   const uint32_t op_bytes = 2u * KS * b_step;
   float* raw = reinterpret_cast<float*>(ops + kWsOps * op_bytes);   // raw_stages x [K][128]
-  float (*stage)[33] = reinterpret_cast<float (*)[33]>(reinterpret_cast<uint8_t*>(raw) + raw_stages * raw_stride);
   __shared__ __align__(8) uint64_t bar[2 * kWsRawMax + 2 * kWsOps + 9];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
@@ -323,12 +272,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
   uint64_t* acc_full = op_empty + kWsOps;
   uint64_t* acc_empty = acc_full + 2;
   uint64_t* mma_done = acc_empty + 2;  // the issuer's last commit: its MMAs are complete before the CTA frees TMEM
-  // the first-collision means of the swapped form come as [M][32] tiles (the tile's 128 columns / 4) in two stages
-  // of the epilogue-transpose region, which the swapped epilogue does not use (2 x 128 x 128 bytes fit its 33 KB)
+  // the first-collision means come as [M][32] tiles (the tile's 128 columns / 4) in two stages after the float32 ring
   uint64_t* f_full = mma_done + 1;
   uint64_t* f_empty = f_full + 2;
-  float* f_stage = reinterpret_cast<float*>(stage);
-  const bool f_tma = kT && F != nullptr && use_f_map != 0;
+  float* f_stage = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(raw) + raw_stages * raw_stride);
+  const bool f_tma = F != nullptr && use_f_map != 0;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
   // A, split once (threads 0..127), rows r of every K step, 8 columns at a time
@@ -372,8 +320,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   const int n_t = ((M + 15) / 16) * 16;
-  const uint32_t acc_cols = kT ? (n_t <= 64 ? 64u : 128u) : (uint32_t)kTcN;  // one accumulator; two are allocated
-  const uint32_t idesc = kT ? idesc_bf16(n_t) : idesc_bf16(kTcN);
+  const uint32_t acc_cols = n_t <= 64 ? 64u : 128u;  // one accumulator; two are allocated
+  const uint32_t idesc = idesc_bf16(n_t);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(2 * acc_cols)
@@ -489,15 +437,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
           const uint64_t al = smem_desc(smem_u32(a_lo + s * a_step), 128, 256);
           const uint64_t bh = smem_desc(smem_u32(o_hi + s * b_step), 128, 256);
           const uint64_t bl = smem_desc(smem_u32(o_lo + s * b_step), 128, 256);
-          if (kT) {
-            mma_bf16(d, bh, ah, idesc, s > 0 ? 1u : 0u);
-            mma_bf16(d, bh, al, idesc, 1u);
-            mma_bf16(d, bl, ah, idesc, 1u);
-          } else {
-            mma_bf16(d, ah, bh, idesc, s > 0 ? 1u : 0u);
-            mma_bf16(d, ah, bl, idesc, 1u);
-            mma_bf16(d, al, bh, idesc, 1u);
-          }
+          mma_bf16(d, bh, ah, idesc, s > 0 ? 1u : 0u);
+          mma_bf16(d, bh, al, idesc, 1u);
+          mma_bf16(d, bl, ah, idesc, 1u);
         }
         tc_commit(smem_u32(op_empty + op));
         tc_commit(smem_u32(acc_full + ac));
@@ -525,7 +467,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
         fail();
         break;
       }
-      if (kT) {
+      {
         // accumulator lane 32 quarter + lane is column n0 + 32 quarter + lane of C; its columns are the rows of C,
         // split in 16-row steps between the two halves of the epilogue warps
         const int64_t col = n0 + quarter * 32 + lane;
@@ -569,46 +511,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
               if (q < rows) out[(int64_t)q * ldc] = add ? prev[q] + __uint_as_float(r[q]) : __uint_as_float(r[q]);
           }
         }
-      } else {
-        // rows 32 quarter .. + 31 of C, columns 64 half .. + 63 of the tile, 32 at a time turned through shared
-        // memory so that every store covers 32 consecutive columns of one row
-        float (*stg)[33] = stage + warp * 32;
-        const int rows = min(32, M - quarter * 32);
-        for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
-          uint32_t r[32];
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-              "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-                "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
-                "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-                "=r"(r[30]), "=r"(r[31])
-              : "r"(taddr + (uint32_t)c0)
-              : "memory");
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-          for (int q = 0; q < 32; ++q) stg[lane][q] = __uint_as_float(r[q]);
-          __syncwarp();
-          const int64_t col = n0 + c0 + lane;
-          if (col < J && rows > 0) {
-            float* out = Cz + (int64_t)(quarter * 32) * ldc + col;
-            float prev[32];
-            const bool add = accumulate || (Fz != nullptr && (col & 3) == 0);
-            if (accumulate) {
-#pragma unroll
-              for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? out[(int64_t)rr * ldc] : 0.f;
-            } else if (add) {
-              const float* f = Fz + (int64_t)(quarter * 32) * ldf + (col >> 2);
-#pragma unroll
-              for (int rr = 0; rr < 32; ++rr) prev[rr] = rr < rows ? __ldg(f + (int64_t)rr * ldf) : 0.f;
-            }
-#pragma unroll
-            for (int rr = 0; rr < 32; ++rr)
-              if (rr < rows) out[(int64_t)rr * ldc] = add ? prev[rr] + stg[rr][lane] : stg[rr][lane];
-          }
-          __syncwarp();
-        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(smem_u32(acc_empty + ac));
@@ -623,13 +525,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) gemm_ws_kernel(const float* __r
 }
 
 // shared memory of the warp-specialised form: A hi/lo, kWsOps operand stages, the float32 stages (1 KB aligned),
-// the epilogue's transposes; ws_raw_stages: as many float32 stages as fit 227 KB with the rest, up to kWsRawMax
-// (the deeper the ring, the more of B's bytes are in flight per SM while earlier tiles convert and multiply)
+// the two stages of the means; ws_raw_stages: as many float32 stages as fit 227 KB with the rest, up to kWsRawMax
 constexpr size_t kWsSmemLimit = 227 * 1024;
 size_t ws_raw_stride(int K) { return (((size_t)K * kTcN * 4) + 1023) & ~(size_t)1023; }
 size_t ws_fixed_bytes(int K) {
   const size_t KS = (size_t)(K + 15) / 16;
-  return KS * 2 * kTcM * 16 * 2 + kWsOps * KS * 2 * kTcN * 16 * 2 + (size_t)kWsEpilogueWarps * 32 * 33 * 4;
+  return KS * 2 * kTcM * 16 * 2 + kWsOps * KS * 2 * kTcN * 16 * 2 + kWsMeansBytes;
 }
 int ws_raw_stages(int K) {
   const size_t fixed = ws_fixed_bytes(K), stride = ws_raw_stride(K);
@@ -713,18 +614,14 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
   const int KS = (int)((K + 15) / 16);
   // A and B operands (the epilogue's staging, 128 x 33 floats, reuses the B region), and at least 50 KB so that no
   // more than four CTAs (4 x 128 of the 512 tensor-memory columns) share an SM: every allocation succeeds at once
-  const size_t b_bytes = std::max<size_t>((size_t)KS * 2 * kTcN * 16 * 2, (size_t)kTcM * 33 * sizeof(float));
+  const size_t b_bytes = (size_t)KS * 2 * kTcN * 16 * 2;
   const size_t smem = std::max<size_t>((size_t)KS * 2 * kTcM * 16 * 2 + b_bytes, 50 * 1024);
-  // the swapped form (the tile's 128 columns as the MMA's M, the rows of C its N) for every M: its epilogue stores
-  // each accumulator lane's column of C directly (32 consecutive columns per warp store), where the other form turns
-  // 32 x 32 blocks through shared memory; measured faster for the 120-row source expansion as well
-  const bool swapped = M <= kSwapMaxM;
   // the warp-specialised form when B's rows are runs of 16-byte units (bulk copies) and its stages fit one CTA
   const size_t ws_smem = ws_smem_bytes((int)K);
   const int raw_stages = ws_raw_stages((int)K);
   if (J % 4 == 0 && ldb % 4 == 0 && stride_b % 4 == 0 && ((uintptr_t)B % 16) == 0 && raw_stages >= 2 &&
       ws_smem <= kWsSmemLimit && !ws_disabled()) {
-    const void* wfn = swapped ? (const void*)gemm_ws_kernel<true> : (const void*)gemm_ws_kernel<false>;
+    const void* wfn = (const void*)gemm_ws_kernel;
     cudaError_t we = cudaFuncSetAttribute(wfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem);
     if (we != cudaSuccess) return set_error(CITRUS_ECUDA, "%s: %s", name, cudaGetErrorString(we));
     const int64_t tiles_per_batch = cdiv(J, kTcN);
@@ -736,18 +633,13 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
     CUtensorMap f_map;
     memset(&f_map, 0, sizeof(f_map));
     const int use_f_map = F != nullptr && encode_f_map(&f_map, F, M, J, ldf, batch, stride_f) ? 1 : 0;
-    if (swapped)
-      gemm_ws_kernel<true><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
-          A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-          error_word, F, ldf, stride_f, raw_stages, b_map, use_map, f_map, use_f_map);
-    else
-      gemm_ws_kernel<false><<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
-          A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-          error_word, F, ldf, stride_f, raw_stages, b_map, use_map, f_map, 0);
+    gemm_ws_kernel<<<(unsigned)grid, kWsThreads, ws_smem, as_stream(stream)>>>(
+        A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
+        error_word, F, ldf, stride_f, raw_stages, b_map, use_map, f_map, use_f_map);
     note_launches();
     return launch_status(name);
   }
-  const void* fn = swapped ? (const void*)gemm_tc_kernel<true> : (const void*)gemm_tc_kernel<false>;
+  const void* fn = (const void*)gemm_tc_kernel;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   // all of the unified L1 / shared-memory capacity as shared memory, so that four CTAs fit an SM
   if (e == cudaSuccess)
@@ -758,14 +650,9 @@ int launch_gemm_tc(const char* name, const float* A, int64_t lda, const float* B
   // four CTAs per SM: the shared-memory floor keeps a fifth from becoming resident (tensor memory holds four
   // 128-column accumulators), and CTAs beyond what fits simply wait for a free slot
   const int64_t grid = std::min<int64_t>(num_tiles, 4 * (int64_t)num_sms());
-  if (swapped)
-    gemm_tc_kernel<true><<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
-        A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-        error_word, F, ldf, stride_f);
-  else
-    gemm_tc_kernel<false><<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
-        A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
-        error_word, F, ldf, stride_f);
+  gemm_tc_kernel<<<(unsigned)grid, kTcThreads, smem, as_stream(stream)>>>(
+      A, lda, B, ldb, C, ldc, (int)M, (int)K, J, stride_b, stride_c, accumulate, tiles_per_batch, num_tiles,
+      error_word, F, ldf, stride_f);
   note_launches();
   return launch_status(name);
 }

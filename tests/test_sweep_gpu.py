@@ -246,9 +246,11 @@ def test_tensor_core_source_expansion_with_means_against_float64(cuda_device, M,
                                                                (17, 20, 260, 2, True, False)])
 def test_warp_specialised_tensor_core_product_equals_single_stage(cuda_device, monkeypatch, M, K, J, batch,
                                                                   accumulate, means):
-    """The warp-specialised tcgen05 product (bulk-copy loader, converters, MMA issuer, double-buffered accumulators,
-    epilogue warps) performs the single-stage kernel's MMAs in the same order and the same epilogue: the same bits,
-    in both roles (M <= 64 swapped), with accumulation, with the first-collision means and a partial last tile."""
+    """The warp-specialised tcgen05 product (tensor-copy loader, converters, MMA issuer, double-buffered accumulators,
+    epilogue warps, the means by tensor copy where their strides allow a tensor map) performs the single-stage
+    kernel's MMAs in the same order and the same epilogue: the same bits, for 17 to 120 rows, with accumulation, with
+    the first-collision means (by tensor copy, and read directly where J / 4 is not a multiple of 4) and a partial last
+    tile."""
     rng = np.random.default_rng(M * 5 + K + J)
     dev = lambda x: torch.as_tensor(x, dtype=torch.float32, device=cuda_device)  # noqa: E731
     A, B = dev(rng.standard_normal((M, K))), dev(rng.standard_normal((batch, K, J)))
