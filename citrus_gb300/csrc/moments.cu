@@ -25,8 +25,10 @@ __global__ void __launch_bounds__(kThreads) moments_vec4_kernel(const float* __r
                                                                int GI, int GO, int num_legendre, int64_t X,
                                                                int64_t ps_g, int64_t ps_n, int64_t ps_x, int64_t os_g,
                                                                int64_t os_n, int64_t os_x) {
-  const int64_t x = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-  const int n = blockIdx.y;
+  // the moments are the fastest block index: the blocks of one range of points run back to back over all moments,
+  // so the transfer rows of a degree, shared by its 2l + 1 moments, are read from DRAM once and then from L2
+  const int64_t x = (int64_t)blockIdx.y * kThreads + threadIdx.x;
+  const int n = blockIdx.x;
   if (x >= X) return;
   const int l = degree_of(n);
   float4 ph[kMax];
@@ -59,8 +61,8 @@ __global__ void __launch_bounds__(kThreads) moments_scalar_kernel(const float* _
                                                                  int64_t ps_n, int64_t ps_k, int64_t ps_x,
                                                                  int64_t os_g, int64_t os_n, int64_t os_k,
                                                                  int64_t os_x) {
-  const int64_t x = (int64_t)blockIdx.x * kThreads + threadIdx.x;
-  const int n = blockIdx.y, k = blockIdx.z;
+  const int64_t x = (int64_t)blockIdx.y * kThreads + threadIdx.x;  // the moments fastest, as above
+  const int n = blockIdx.x, k = blockIdx.z;
   if (x >= X) return;
   const int l = degree_of(n);
   float ph[kMax];
@@ -103,14 +105,16 @@ extern "C" int citrus_scattering_moments(const float* transfer, const float* phi
   const bool vec = k_count == 4 && ps_k == 1 && os_k == 1 && ps_g % 4 == 0 && ps_n % 4 == 0 && ps_x % 4 == 0 &&
                    os_g % 4 == 0 && os_n % 4 == 0 && os_x % 4 == 0 && ((uintptr_t)phi % 16) == 0 &&
                    ((uintptr_t)out % 16) == 0;
+  CITRUS_REQUIRE(cdiv(num_points, kThreads) <= 65535, "citrus_scattering_moments: %lld points exceed the grid",
+                 (long long)num_points);
   const unsigned bx = (unsigned)cdiv(num_points, kThreads);
   const int GI = (int)g_in, GO = (int)g_out, NL = (int)num_legendre;
 #define CITRUS_MOMENTS_LAUNCH(KMAX)                                                                                   \
   if (vec) {                                                                                                          \
-    moments_vec4_kernel<KMAX><<<dim3(bx, (unsigned)num_moments), kThreads, 0, s>>>(                                   \
+    moments_vec4_kernel<KMAX><<<dim3((unsigned)num_moments, bx), kThreads, 0, s>>>(                                   \
         transfer, phi, out, GI, GO, NL, num_points, ps_g, ps_n, ps_x, os_g, os_n, os_x);                              \
   } else {                                                                                                            \
-    moments_scalar_kernel<KMAX><<<dim3(bx, (unsigned)num_moments, (unsigned)k_count), kThreads, 0, s>>>(              \
+    moments_scalar_kernel<KMAX><<<dim3((unsigned)num_moments, bx, (unsigned)k_count), kThreads, 0, s>>>(              \
         transfer, phi, out, GI, GO, NL, num_points, ps_g, ps_n, ps_k, ps_x, os_g, os_n, os_k, os_x);                  \
   }
   if (GI <= 4) {
