@@ -219,7 +219,7 @@ def test_bf16x3_tensor_core_gemm_error_against_float64(cuda_device, M, K, J, bat
 def test_tensor_core_source_expansion_with_means_against_float64(cuda_device, M, K, J, batch):
     """The source of an accumulator sweep in the mixed precision (tcgen05, bfloat16 hi/lo split, the first-collision
     means added in the epilogue): C = A B + (F, 0, 0, 0) against float64 within the split's ~1e-5 of the largest
-    term, over 128-row launches (M = 240), the swapped form (M <= 64) and partial column tiles."""
+    term, over 128-row launches (M = 240), row counts from 5 to 128 and partial column tiles."""
     rng = np.random.default_rng(M + 3 * K + J)
     A = rng.standard_normal((M, K))
     B = rng.standard_normal((batch, K, J))
