@@ -148,6 +148,12 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* 
   // four rows at a time: eight independent multiply-add chains per thread
   for (int r0 = 0; r0 < rows; r0 += 4) {
     float a0[4] = {0.f, 0.f, 0.f, 0.f}, a1[4] = {0.f, 0.f, 0.f, 0.f};
+    // the four means (first column of each quadruple) are loaded before the products, which hide their latency
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    if (kMode == 2 && (col & 3) == 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) f[q] = r0 + q < rows ? F[(int64_t)(row0 + r0 + q) * ldf + (col >> 2)] : 0.f;
+    }
 #pragma unroll
     for (int k = 0; k < kKP; k += 4) {
 #pragma unroll
@@ -182,10 +188,7 @@ __global__ void __launch_bounds__(kStreamThreads) gemm_cols_kernel(const float* 
         a1[q] += o[q].y;
       }
     }
-    if (kMode == 2 && (col & 3) == 0) {  // the four means before the first store
-      float f[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) f[q] = r0 + q < rows ? F[(int64_t)(row0 + r0 + q) * ldf + (col >> 2)] : 0.f;
+    if (kMode == 2 && (col & 3) == 0) {  // the means added before the first store
 #pragma unroll
       for (int q = 0; q < 4; ++q) a0[q] += f[q];
     }
