@@ -54,10 +54,10 @@ __global__ void box_blur_kernel(const float* __restrict__ in, float* __restrict_
   out[k * os_k + line * os_l + (int64_t)c * os_p] = acc / (hi - lo);
 }
 
-// The same filter with O(1) work per output pixel: a block owns one line, stages its N pixels in shared memory with
-// their prefix sums (a block scan, float32 pairs), and each output pixel is its partial first pixel, the prefix-sum
-// difference over the fully covered pixels and its partial last pixel, divided by the window length.
-constexpr int kScanThreads = 256;
+// The same filter with O(1) work per output pixel (box_blur_warp_kernel below): a warp owns one line, stages its N
+// pixels in shared memory with their prefix sums (a warp scan, float32 pairs), and each output pixel is its partial
+// first pixel, the prefix-sum difference over the fully covered pixels and its partial last pixel, divided by the
+// window length.
 constexpr int kScanMaxN = 1024;
 
 // A float32 pair (hi, lo) that carries a sum to about 2^-40 of its magnitude: the prefix sums of the scan below are
@@ -78,37 +78,41 @@ __device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
 
 __device__ __forceinline__ F2 f2_neg(F2 a) { return F2{-a.hi, -a.lo}; }
 
-__global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float* __restrict__ in,
-                                                                     float* __restrict__ out, int64_t lines, int N,
-                                                                     int64_t is_k, int64_t is_l, int64_t is_p,
-                                                                     int64_t os_k, int64_t os_l, int64_t os_p,
-                                                                     WidthArgs wa) {
-  __shared__ float x[kScanMaxN];
-  __shared__ float P_hi[kScanMaxN + 1], P_lo[kScanMaxN + 1];   // P[j] = sum of x[0 .. j - 1]
-  __shared__ F2 warp_tot[kScanThreads / 32];
+// One warp per line and kBlurLines lines per block: a lane sums a contiguous run of ceil(N / 32) pixels, a
+// warp-level scan of the run sums gives the prefix sums, and no block barrier is needed, so a block's eight lines
+// proceed independently (a block of 256 threads per line, as before, left most of its threads waiting at the
+// scan's barriers). Lines of strided pixels (the row blur) are adjacent in memory across the block's warps, so
+// the eight warps share the sectors of their loads and stores.
+constexpr int kBlurLines = 8;
+
+__global__ void __launch_bounds__(32 * kBlurLines) box_blur_warp_kernel(const float* __restrict__ in,
+                                                                        float* __restrict__ out, int64_t lines, int N,
+                                                                        int64_t is_k, int64_t is_l, int64_t is_p,
+                                                                        int64_t os_k, int64_t os_l, int64_t os_p,
+                                                                        WidthArgs wa) {
+  extern __shared__ float s_blur[];  // per warp: x [N], P_hi [N + 1], P_lo [N + 1]
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
   const int k = blockIdx.y;
-  const int64_t line = blockIdx.x;
+  const int64_t line = (int64_t)blockIdx.x * kBlurLines + warp;
+  if (line >= lines) return;  // the whole warp: no block barrier follows
+  float* x = s_blur + (int64_t)warp * (3 * N + 2);
+  float* P_hi = x + N;
+  float* P_lo = P_hi + N + 1;
   const float* src = in + k * is_k + line * is_l;
-  for (int j = threadIdx.x; j < N; j += kScanThreads) x[j] = src[j * is_p];
-  __syncthreads();
-  // each thread sums a contiguous run of per = ceil(N / 256) pixels; a block-wide exclusive scan of the run sums
-  const int per = (N + kScanThreads - 1) / kScanThreads;
-  const int j0 = threadIdx.x * per, j1 = min(N, j0 + per);
+  for (int j = lane; j < N; j += 32) x[j] = src[j * is_p];
+  __syncwarp();
+  const int per = (N + 31) / 32;
+  const int j0 = min(N, lane * per), j1 = min(N, j0 + per);
   F2 run{0.f, 0.f};
   for (int j = j0; j < j1; ++j) run = f2_add(run, F2{x[j], 0.f});
-  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
   F2 incl = run;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
     const F2 y{__shfl_up_sync(0xffffffffu, incl.hi, off), __shfl_up_sync(0xffffffffu, incl.lo, off)};
     if (lane >= off) incl = f2_add(incl, y);
   }
-  if (lane == 31) warp_tot[warp] = incl;
-  __syncthreads();
-  F2 base{0.f, 0.f};
-  for (int w = 0; w < warp; ++w) base = f2_add(base, warp_tot[w]);
-  F2 acc = f2_add(base, f2_add(incl, f2_neg(run)));    // exclusive prefix of this thread's run
-  if (threadIdx.x == 0) {
+  F2 acc = f2_add(incl, f2_neg(run));  // exclusive prefix of this lane's run
+  if (lane == 0) {
     P_hi[0] = 0.f;
     P_lo[0] = 0.f;
   }
@@ -117,11 +121,11 @@ __global__ void __launch_bounds__(kScanThreads) box_blur_scan_kernel(const float
     P_hi[j + 1] = acc.hi;
     P_lo[j + 1] = acc.lo;
   }
-  __syncthreads();
+  __syncwarp();
   const float half = 0.5f * fmaxf(blur_width(wa, k), 1e-3f);
   const float nf = (float)N;
   float* dst = out + k * os_k + line * os_l;
-  for (int c = threadIdx.x; c < N; c += kScanThreads) {
+  for (int c = lane; c < N; c += 32) {
     const float center = (float)c + 0.5f;
     const float lo = fminf(fmaxf(center - half, 0.f), nf), hi = fminf(fmaxf(center + half, 0.f), nf);
     const int a = max(0, (int)floorf(lo)), b = min(N - 1, (int)ceilf(hi) - 1);
@@ -225,10 +229,14 @@ extern "C" int citrus_box_blur(const float* in, float* out, int64_t num_directio
   CITRUS_REQUIRE(in != out, "citrus_box_blur: in and out must not alias");
   if (num_directions == 0 || lines == 0) return CITRUS_OK;
   WidthArgs wa{widths, height_sums, cell_width, axis, (float)(pitch > 0 ? 1.0 / pitch : 0.0), (float)center_height};
-  if (length <= kScanMaxN && lines <= 0x7fffffff) {
-    dim3 grid((unsigned)lines, (unsigned)num_directions);
-    box_blur_scan_kernel<<<grid, kScanThreads, 0, as_stream(stream)>>>(in, out, lines, (int)length, is_k, is_l, is_p,
-                                                                       os_k, os_l, os_p, wa);
+  if (length <= kScanMaxN && cdiv(lines, kBlurLines) <= 0x7fffffff) {
+    const size_t smem = (size_t)kBlurLines * (3 * length + 2) * sizeof(float);  // 96 KB at the longest lines
+    cudaError_t e = cudaFuncSetAttribute(box_blur_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)((size_t)kBlurLines * (3 * kScanMaxN + 2) * sizeof(float)));
+    if (e != cudaSuccess) return set_error(CITRUS_ECUDA, "citrus_box_blur: %s", cudaGetErrorString(e));
+    dim3 grid((unsigned)cdiv(lines, kBlurLines), (unsigned)num_directions);
+    box_blur_warp_kernel<<<grid, 32 * kBlurLines, smem, as_stream(stream)>>>(in, out, lines, (int)length, is_k, is_l,
+                                                                             is_p, os_k, os_l, os_p, wa);
   } else {
     dim3 grid((unsigned)cdiv(lines * length, 256), (unsigned)num_directions);
     box_blur_kernel<<<grid, 256, 0, as_stream(stream)>>>(in, out, (int)num_directions, lines, (int)length, is_k,
