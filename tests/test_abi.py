@@ -91,3 +91,48 @@ def test_allocation_free_sweep_checks_its_arguments(library):
     for timeout in (0, -5):
         status = lib.citrus_sweep_persistent_static(*args, offsets.ctypes.data, 4, 8, 1, 1, 1, None, timeout, None)
         assert status == 1 and b"timeout_ns" in lib.citrus_last_error_string()
+
+
+def test_grid_source_and_table_entry_points_check_their_arguments(library):
+    """The anti-scatter-grid accumulation, the source field, the crossing tables, the tables' downstream trace and
+    the oblique projection's scratch refuse bad arguments with CITRUS_EINVAL before any CUDA call (the fake
+    addresses below are never dereferenced)."""
+    import ctypes
+    lib = _lib.library()
+    fake = 256
+    # more than 32 groups, more than two sets of septa, weights neither per channel nor shared
+    status = lib.citrus_grid_signal_sum(fake, 2, 33, 4, 5, 1, 1, 1, 1, fake, 5, None, 0, None, None, None, None,
+                                        None, None, None, fake, 1, 0, None)
+    assert status == 1 and b"groups <= 32" in lib.citrus_last_error_string()
+    status = lib.citrus_grid_signal_sum(fake, 2, 3, 4, 5, 1, 1, 1, 1, fake, 5, None, 3, None, None, None, None,
+                                        None, None, None, fake, 1, 0, None)
+    assert status == 1 and b"two sets" in lib.citrus_last_error_string()
+    status = lib.citrus_grid_signal_sum(fake, 2, 3, 4, 5, 1, 1, 1, 1, fake, 4, None, 0, None, None, None, None,
+                                        None, None, None, fake, 1, 0, None)
+    assert status == 1 and b"cols | 1" in lib.citrus_last_error_string()
+    status = lib.citrus_grid_signal_sum(fake, 2, 3, 4, 5, 1, 1, 1, 1, fake, 5, None, 1, None, None, None, None,
+                                        None, None, None, fake, 1, 0, None)
+    assert status == 1 and b"septa arrays" in lib.citrus_last_error_string()
+    field = (ctypes.c_double * 23)()
+    dims = (ctypes.c_int64 * 3)(2, 2, 2)
+    # a profile without the panel; off-focal nodes without their count; a thickness without the path output
+    status = lib.citrus_source_field(field, None, fake, None, 0, 0.0, None, None, 0, fake, None, None, None, None, 8,
+                                     1, fake, None, None)
+    assert status == 1 and b"needs the panel" in lib.citrus_last_error_string()
+    status = lib.citrus_source_field(field, None, None, None, 0, 0.0, fake, fake, 0, fake, None, None, None, None, 8,
+                                     1, fake, None, None)
+    assert status == 1 and b"off-focal" in lib.citrus_last_error_string()
+    status = lib.citrus_source_field(field, None, None, fake, 1, 2.7, None, None, 0, fake, None, None, None, None, 8,
+                                     1, fake, None, None)
+    assert status == 1 and b"filter-path output" in lib.citrus_last_error_string()
+    box = (ctypes.c_double * 6)(0, 0, 0, 1, 1, 1)
+    status = lib.citrus_crossing_tables(box, dims, fake, 4, fake, 4 * 3 * 6 - 1, None)
+    assert status == 1 and b"needs 72" in lib.citrus_last_error_string()
+    status = lib.citrus_downstream_cumulative_tables(fake, 2, box, dims, fake, fake, 4, fake, 1.0, fake, 1, 1, 1,
+                                                     None, 0, None)
+    assert status == 1 and b"null crossing tables" in lib.citrus_last_error_string()
+    need = int(lib.citrus_oblique_scratch_bytes(7))
+    assert need > 7 * 100 and int(lib.citrus_oblique_scratch_bytes(0)) == 0
+    status = lib.citrus_oblique_project_scratch(fake, 1, 0, box, dims, fake, 7, fake, 4, 4, fake, 1, 1, 1, 1, fake,
+                                                need - 1, None)
+    assert status == 1 and b"direction scratch" in lib.citrus_last_error_string()
