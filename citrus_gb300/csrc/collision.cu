@@ -1405,16 +1405,27 @@ __global__ void __launch_bounds__(kEmitPoints * kGP) fc_means_kernel(
   const int d0 = blockIdx.y * kFcBatch, dlast = min(K, d0 + kFcBatch);
   for (int p0 = d0; p0 < dlast; p0 += kPass) {
     const int np = min(kPass, dlast - p0);
-#pragma unroll 4
-    for (int q = 0; q < np; ++q) {
-      const int d = p0 + q;
-      float r = 0.f;
-      if (x < n) {
-        const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
-        const float cosine = ux * ox + uy * oy + uz * oz;
-        r = __ldg(cache + ((int64_t)__ldg(cache_index + d) * G + g) * in.V + c) * sc * (1.f + be * cosine);
+    // eight directions' cache loads in flight per thread before their products and shared-memory stores
+    constexpr int kU = 8;
+    for (int q0 = 0; q0 < np; q0 += kU) {
+      float v[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+        v[u] = (x < n && q0 + u < np)
+                   ? __ldg(cache + ((int64_t)__ldg(cache_index + p0 + q0 + u) * G + g) * in.V + c)
+                   : 0.f;
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (q0 + u >= np) break;
+        const int d = p0 + q0 + u;
+        float r = 0.f;
+        if (x < n) {
+          const float ox = __ldg(omegas + 3 * d), oy = __ldg(omegas + 3 * d + 1), oz = __ldg(omegas + 3 * d + 2);
+          const float cosine = ux * ox + uy * oy + uz * oz;
+          r = v[u] * sc * (1.f + be * cosine);
+        }
+        s_out[q0 + u][x * G + g] = r;
       }
-      s_out[q][x * G + g] = r;
     }
     __syncthreads();
     for (int q = 0; q < np; ++q)
