@@ -12,7 +12,6 @@ store (``citrus_first_collision_moments``).
 
 from __future__ import annotations
 
-import ctypes
 from dataclasses import dataclass
 from typing import Optional, Sequence
 

@@ -8,7 +8,6 @@ from path lengths).
 
 from __future__ import annotations
 
-import math
 
 import numpy as np
 
