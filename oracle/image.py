@@ -8,7 +8,6 @@ from path lengths).
 
 from __future__ import annotations
 
-
 import numpy as np
 
 from citrus_gb300.quadrature import real_spherical_harmonics
