@@ -8,6 +8,8 @@ from path lengths).
 
 from __future__ import annotations
 
+import dataclasses
+
 import numpy as np
 
 from citrus_gb300.quadrature import real_spherical_harmonics
@@ -111,3 +113,41 @@ def primary(library, rho, grid, geometry, angle, detector):
     planar = fluence * np.cos(theta0)
     signal_pg = planar * detector.at(library.group_energy, theta0)
     return {"fluence": fluence, "planar_fluence": planar, "signal_per_group": signal_pg, "signal": signal_pg.sum(0)}
+
+
+def primary_with_source(library, rho, grid, geometry, angle, detector, n=1, grid_response=None, margins=(0.0, 0.0),
+                        off_focal=None, profile=None, thickness=None, filter_density=0.0, filter_mu=None):
+    """Primary signal [Rd, Cd] with sub-pixel rays, the source model and an anti-scatter grid
+    (scatter_image.py:1395-1471): the fine-energy transmission, the beam filter's path included, averaged over the
+    n x n sub-pixels of every pixel; the source weight, the inverse square, the detector response and the grid
+    transmission (each set of septa at its own grid angles) at the pixel centres."""
+    fine = geometry if n == 1 else dataclasses.replace(
+        geometry, num_det_rows=geometry.num_det_rows * n, num_det_channels=geometry.num_det_channels * n,
+        delta_det_row=geometry.delta_det_row / n, delta_det_channel=geometry.delta_det_channel / n)
+    r0 = np.asarray(geometry.source_position(angle))
+    path = siddon.primary_project(rho, grid, fine, angle)                       # [M, Rd n, Cd n]
+    tau = np.einsum("me,mrc->erc", library.fine_mu_t, path)
+    if thickness is not None:
+        fp = responses.filter_path(geometry, angle, fine.pixel_centers_np(angle) - r0, thickness, filter_density)
+        tau = tau + np.asarray(filter_mu)[:, None, None] * fp[None]
+    W = (library.fine_group[None, :] == np.arange(library.num_groups)[:, None]) * library.fine_weight[None, :]
+    T = np.einsum("ge,erc->grc", W, np.exp(-tau))
+    Rd, Cd = geometry.image_shape
+    T = T.reshape(-1, Rd, n, Cd, n).mean(axis=(2, 4))
+    pixels = geometry.pixel_centers_np(angle)
+    d = pixels - r0
+    dist2 = (d * d).sum(-1)
+    b = responses.source_weight(geometry, angle, d, margins, off_focal, profile)
+    omega_p = d / np.sqrt(dist2)[..., None]
+    normal = geometry.local_normals_np(pixels, angle)
+    theta0 = np.arccos(np.clip((omega_p * (-normal)).sum(-1), -1.0, 1.0))
+    signal = (b / dist2 * np.cos(theta0))[None] * T * detector.at(library.group_energy, theta0)
+    if grid_response is not None:
+        for septa in ((grid_response,) if grid_response.crossed is None
+                      else (grid_response, grid_response.crossed)):
+            t1, t2 = responses.grid_angles(omega_p, pixels, geometry, angle, septa.focal_distance_cm,
+                                           septa.septa_along)
+            signal = signal * responses.table_value(septa.energy_kev, septa.theta1_rad, septa.theta2_rad,
+                                                    septa.transmission, library.group_energy, t1, t2)
+    return signal.sum(0)
+

@@ -3,13 +3,15 @@
 Follows citrus/scatter_solver/uncollided.py:74-349 (primary directions, uncollided fluence from path lengths, the
 first-collision source, restriction to LD moments), :357-461 and :538-636 (exact moments, quadrature sums, correction
 factors), cross_sections.py:797-883 (group transmission), :905-995 (eta-table interpolation) and source.py:289-382
-(focal-spot weight).
+(focal-spot weight); the source model's off-focal table, emission profile and beam filter through
+``oracle/responses.py``.
 """
 
 from __future__ import annotations
 
 import numpy as np
 
+from oracle import responses
 from oracle.siddon import centers, upstream_to_points
 
 
@@ -51,6 +53,25 @@ def uncollided_fluence(library, rho, grid, geometry, angle, points=None):
     d = c - np.asarray(geometry.source_position(angle))
     b = source_weight(geometry, angle, c)
     return T.reshape(-1, *pg.shape) * (b / (d * d).sum(-1))[None]
+
+
+def uncollided_fluence_with_source(library, rho, grid, geometry, angle, margins=(0.0, 0.0), off_focal=None,
+                                   profile=None, thickness=None, filter_density=0.0, filter_mu=None):
+    """[G, *grid.shape] uncollided fluence of a source with field margins, an off-focal table, an emission profile
+    and a beam filter (uncollided.py:160-197 with source.py:289-430): the filter's path adds filter_mu[e] times it to
+    every exponent."""
+    c = centers(grid)
+    r0 = np.asarray(geometry.source_position(angle))
+    d = c - r0
+    path = upstream_to_points(rho, grid, geometry.source_position(angle), c.reshape(-1, 3))
+    tau = np.einsum("me,mp->ep", library.fine_mu_t, path.reshape(path.shape[0], -1))
+    if thickness is not None:
+        fp = responses.filter_path(geometry, angle, d.reshape(-1, 3), thickness, filter_density)
+        tau = tau + np.asarray(filter_mu)[:, None] * fp[None]
+    W = (library.fine_group[None, :] == np.arange(library.num_groups)[:, None]) * library.fine_weight[None, :]
+    T = (W @ np.exp(-tau)).reshape(-1, *grid.shape)
+    b = responses.source_weight(geometry, angle, d, margins, off_focal, profile)
+    return T * (b / (d * d).sum(-1))[None]
 
 
 def transfer_at(library, rho, eta):

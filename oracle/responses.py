@@ -48,7 +48,8 @@ def local_axes(geometry, angle, points):
 
 
 def grid_angles(omega, pixels, geometry, angle, focal_distance, septa_along):
-    """[K, Rd, Cd] theta1 and theta2 of directions [K, 3] arriving at pixels [Rd, Cd, 3]."""
+    """[K, Rd, Cd] theta1 and theta2 of directions [K, 3] arriving at pixels [Rd, Cd, 3] (or [Rd, Cd] for one
+    direction per pixel, [Rd, Cd, 3])."""
     f = float(geometry.source_detector_dist) if focal_distance is None else float(focal_distance)
     u, v, n = local_axes(geometry, angle, pixels)
     center = np.asarray(geometry.panel_center(angle))
@@ -61,11 +62,12 @@ def grid_angles(omega, pixels, geometry, angle, focal_distance, septa_along):
     else:
         focus = pixels + f * n
     across, along = (v, u) if septa_along == "channels" else (u, v)
-    a = -np.asarray(omega, dtype=np.float64)[:, None, None, :]
+    omega = np.asarray(omega, dtype=np.float64)
+    a = -omega[:, None, None, :] if omega.ndim == 2 else -omega  # [K, 3] directions, or one per pixel
     an = (a * n).sum(-1)
     to_focus = focus - pixels
     theta_f = np.arctan2((to_focus * across).sum(-1), (to_focus * n).sum(-1))
-    theta1 = np.arctan2((a * across).sum(-1), an) - theta_f[None]
+    theta1 = np.arctan2((a * across).sum(-1), an) - (theta_f[None] if omega.ndim == 2 else theta_f)
     theta2 = np.arctan2((a * along).sum(-1), an)
     return theta1, theta2
 

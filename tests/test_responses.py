@@ -192,3 +192,27 @@ def test_group_averaged_responses_match_reference():
     # evaluated at a group energy, the averaged table returns the group's mean
     e = np.asarray(library.group_energy)
     np.testing.assert_allclose(avg_det.at(e, [0.0])[:, 0], avg_det.response[1::2, 0][::-1], rtol=1e-13)
+
+
+@pytest.mark.parametrize("curved", [False, True])
+def test_oracle_primary_and_uncollided_with_source_and_grid_match_reference(curved):
+    """The oracle's primary (2 x 2 sub-rays and one ray per pixel) behind the focused grid and its uncollided fluence,
+    both with the profiled, off-focal, filtered source, against the reference's own float64 runs."""
+    from oracle import image as oimage
+    from oracle import physics
+    from test_oracle_golden import _image_setup
+    g = golden("grid_and_source")
+    _, library, _, det, _ = _image_setup()
+    pre = "curved" if curved else "flat"
+    geo = image_geometry(curved)
+    big = Grid((8, 10, 6), 3.0)
+    source = dict(margins=(0.5, 0.25), off_focal=([0.0, 1.0, 3.0], [0.3, 0.1, 0.02]),
+                  profile=g[f"source_{pre}_profile"], thickness=g[f"source_{pre}_thickness"], filter_density=2.7,
+                  filter_mu=filter_attenuation(library.fine_energy))
+    for n, key in ((1, f"source_{pre}_primary"), (2, f"source_{pre}_primary_n2")):
+        got = oimage.primary_with_source(library, g[f"source_{pre}_rho"], big, geo, 0.8, det, n=n,
+                                         grid_response=fixture_grid(g), **source)
+        np.testing.assert_allclose(got, g[key], rtol=0, atol=1e-12 * np.abs(g[key]).max())
+    phi = physics.uncollided_fluence_with_source(library, g[f"source_{pre}_rho"], big, geo, 0.8, **source)
+    ref = g[f"source_{pre}_phi"]
+    np.testing.assert_allclose(phi, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
